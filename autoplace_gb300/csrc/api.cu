@@ -1,0 +1,368 @@
+// The C ABI of libgp103 (include/gp103.h): argument checks and launch order; no allocation, no host sync.
+#include <string.h>
+
+#include "field.cuh"
+#include "gp103.cuh"
+#include "kernels.cuh"
+#include "step.cuh"
+
+using namespace gp103;
+
+#define REQUIRE(cond)                    \
+    do {                                 \
+        if (!(cond)) return GP103_ERR_ARG; \
+    } while (0)
+#define TRY(call)                        \
+    do {                                 \
+        int st_ = (call);                \
+        if (st_) return st_;             \
+    } while (0)
+
+extern "C" int gp103_version(void) { return 1; }
+
+extern "C" const char* gp103_status_string(int status) {
+    switch (status) {
+        case GP103_OK: return "ok";
+        case GP103_ERR_ARG: return "invalid argument (null pointer, negative size or empty grid)";
+        case GP103_ERR_CUDA: return "a CUDA launch failed";
+        case GP103_ERR_SHAPE: return "grid not supported by the tensor-core field (multiples of 128 bins per side)";
+        default: return "unknown status";
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ part 1
+extern "C" int gp103_wa(const float* pos, const int* pin_cell, const float* pin_off, const int* net_start,
+                        const int* cell_start, const int* cell_pin, int num_nets, int num_mov, const float* gamma,
+                        float* pin_grad, float* out, float* grad, cudaStream_t stream) {
+    REQUIRE(num_nets >= 0 && num_mov >= 0 && net_start && gamma && cell_start);
+    REQUIRE(num_nets == 0 || (pin_cell && pin_off && pin_grad && out && pos));
+    REQUIRE(num_mov == 0 || (grad && cell_pin));
+    if (num_nets > 0) {
+        WaJob j = {};
+        j.pos_a = j.pos_b = (const float2*)pos;
+        j.pin_cell = pin_cell;
+        j.pin_off = (const float2*)pin_off;
+        j.net_start = net_start;
+        j.num_nets = num_nets;
+        j.num_mov = num_mov;
+        j.gamma = gamma;
+        j.pin_grad = (float2*)pin_grad;
+        j.out = (float2*)out;
+        TRY(launch_wa_net(j, stream));
+    }
+    return launch_wa_cell((const float2*)pin_grad, cell_start, cell_pin, num_mov, (float2*)grad, stream);
+}
+
+extern "C" int gp103_density_map(const float* pos, const float* size, const float* ratio, int num_nodes, int num_mov,
+                                 float bx, float by, int nbx, int nby, unsigned long long* map, const float* fixed,
+                                 float target, float* rho, float* over, cudaStream_t stream) {
+    REQUIRE(num_nodes >= 0 && num_mov >= 0 && nbx > 0 && nby > 0 && map && fixed && rho && over);
+    REQUIRE(num_nodes == 0 || (pos && size && ratio));
+    REQUIRE(bx > 0.f && by > 0.f);
+    const int mov = num_mov < num_nodes ? num_mov : num_nodes;
+    if (cudaMemsetAsync(map, 0, sizeof(unsigned long long) * 2 * (size_t)nbx * nby, stream) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    ScatterJob j = {};
+    j.pos_a = j.pos_b = (const float2*)pos;
+    j.size = (const float2*)size;
+    j.ratio = ratio;
+    j.num_nodes = num_nodes;
+    j.num_mov = mov;
+    j.inv_bx = 1.f / bx;
+    j.inv_by = 1.f / by;
+    j.nbx = nbx;
+    j.nby = nby;
+    j.map0 = map;
+    j.map1 = map + (size_t)nbx * nby;
+    TRY(launch_scatter(j, stream));
+    return launch_post_mirror(map, fixed, target, nbx, nby, rho, over, stream);
+}
+
+extern "C" int gp103_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,
+                                   const float* alpha, const float* coef, int n, float* u_next, float* v_next,
+                                   cudaStream_t stream) {
+    REQUIRE(n >= 0 && alpha && coef);
+    REQUIRE(n == 0 || (u && v && g && lo && hi && u_next && v_next));
+    return launch_nesterov_step(u, v, g, lo, hi, alpha, coef, n, u_next, v_next, stream);
+}
+
+extern "C" int gp103_density_grad(const float* pos, const float* size, const float* ratio, const float* field,
+                                  const float* wl_grad, const float* pins, const float* area, int num_nodes,
+                                  int num_wl, const float* weight, const float* precond, float bx, float by, int nbx,
+                                  int nby, float* grad, cudaStream_t stream) {
+    REQUIRE(num_nodes >= 0 && num_wl >= 0 && nbx > 0 && nby > 0 && weight && precond && bx > 0.f && by > 0.f);
+    REQUIRE(num_nodes == 0 || (pos && size && ratio && field && pins && area && grad));
+    REQUIRE(num_wl == 0 || wl_grad);
+    return launch_gather_mirror(pos, size, ratio, field, wl_grad, pins, area, num_nodes, num_wl, weight, precond, bx,
+                                by, nbx, nby, grad, stream);
+}
+
+extern "C" int gp103_control(double* S, float* kp, const double* c, const float* moved, const float* turned,
+                             const float* hpwl, const float* ovf, const float* wa, cudaStream_t stream) {
+    REQUIRE(S && kp && c && moved && turned && hpwl && ovf && wa);
+    return launch_control(S, kp, c, moved, turned, hpwl, ovf, wa, stream);
+}
+
+extern "C" int gp103_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
+                            const float* g_next, float* best, int n, cudaStream_t stream) {
+    REQUIRE(S && n >= 0);
+    REQUIRE(n == 0 || (u && v && g && u_next && v_next && g_next && best));
+    return launch_select(S, u, v, g, u_next, v_next, g_next, best, n, stream);
+}
+
+// ------------------------------------------------------------------------------------------------ part 2
+static FieldLayout layout_of(const gp103_plan* p) {
+    FieldLayout L = field_layout(p->nbx, p->nby, p->field_mode);
+    L.bx = p->bx;
+    L.by = p->by;
+    return L;
+}
+
+extern "C" int gp103_plan_offsets(size_t* out, int n) {
+#define OFF(f) offsetof(gp103_plan, f)
+    const size_t off[] = {
+        OFF(num_nodes), OFF(num_mov), OFF(num_nets), OFF(num_pins), OFF(nbx), OFF(nby), OFF(jnbx), OFF(jnby),
+        OFF(field_mode), OFF(pin_cell), OFF(pin_off), OFF(net_start), OFF(cell_start), OFF(cell_pin), OFF(size),
+        OFF(ratio), OFF(pins), OFF(area), OFF(lo), OFF(hi), OFF(bx), OFF(by), OFF(target), OFF(fixed),
+        OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
+        OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
+        OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters)};
+#undef OFF
+    const int count = (int)(sizeof(off) / sizeof(off[0]));
+    for (int i = 0; i < count && i < n; i++) out[i] = off[i];
+    if (n > count) out[count] = sizeof(gp103_plan);
+    return count;
+}
+
+extern "C" int gp103_plan_sizes(int nbx, int nby, int field_mode, gp103_sizes* out) {
+    REQUIRE(out && nbx > 0 && nby > 0);
+    REQUIRE(field_mode == GP103_FIELD_FP32 || field_mode == GP103_FIELD_BF16X3 || field_mode == GP103_FIELD_BF16X6);
+    if (field_mode != GP103_FIELD_FP32 && !field_tc_supported(nbx, nby)) return GP103_ERR_SHAPE;
+    FieldLayout L = field_layout(nbx, nby, field_mode);
+    out->field_const = L.const_bytes;
+    out->field_work = L.work_bytes;
+    out->red = RED_DOUBLES;
+    return GP103_OK;
+}
+
+static int check_plan(const gp103_plan* p) {
+    REQUIRE(p && p->num_nodes >= 0 && p->num_mov >= 0 && p->num_mov <= p->num_nodes && p->num_nets >= 0);
+    REQUIRE(p->nbx > 0 && p->nby > 0 && p->bx > 0.f && p->by > 0.f);
+    REQUIRE(p->field_const && p->field_work && p->ex && p->ey && p->red && p->counters && p->map && p->kp);
+    REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
+    if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
+    return GP103_OK;
+}
+
+extern "C" int gp103_field_constants(const gp103_plan* plan, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    return field_constants(layout_of(plan), plan->field_const, stream);
+}
+
+static int run_field(const gp103_plan* p, const float* density, cudaStream_t s) {
+    const FieldLayout L = layout_of(p);
+    if (p->field_mode == GP103_FIELD_FP32) return field_fp32(L, p->field_const, p->field_work, density, p->ex, p->ey, s);
+    return field_tc(L, p->field_const, p->field_work, density, p->ex, p->ey, s);
+}
+
+extern "C" int gp103_field(const gp103_plan* plan, const float* density, float* ex, float* ey, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    REQUIRE(density && ex && ey);
+    gp103_plan q = *plan;
+    q.ex = ex;
+    q.ey = ey;
+    return run_field(&q, density, stream);
+}
+
+// Density map(s) at the chosen positions, post-processing, field: the force grid's plain density goes straight into
+// the field's first operand (float32 plane or bf16 terms).
+static int density_and_field(const gp103_plan* p, const float* pos_a, const float* pos_b, const int* sel,
+                             cudaStream_t s) {
+    const size_t nb = (size_t)p->nbx * p->nby;
+    ScatterJob sj = {};
+    sj.pos_a = (const float2*)pos_a;
+    sj.pos_b = (const float2*)pos_b;
+    sj.sel = sel;
+    sj.size = (const float2*)p->size;
+    sj.ratio = p->ratio;
+    sj.num_nodes = p->num_nodes;
+    sj.num_mov = p->num_mov;
+    sj.inv_bx = 1.f / p->bx;
+    sj.inv_by = 1.f / p->by;
+    sj.nbx = p->nbx;
+    sj.nby = p->nby;
+    sj.map0 = p->map;
+    sj.map1 = p->map + nb;
+    TRY(launch_scatter(sj, s));
+    if (p->jnbx > 0) {
+        ScatterJob jj = sj;
+        jj.size = (const float2*)p->jsize;
+        jj.ratio = p->jratio;
+        jj.num_nodes = p->num_mov;
+        jj.inv_bx = 1.f / p->jbx;
+        jj.inv_by = 1.f / p->jby;
+        jj.nbx = p->jnbx;
+        jj.nby = p->jnby;
+        jj.map0 = p->jmap;
+        jj.map1 = nullptr;
+        TRY(launch_scatter(jj, s));
+    }
+    const FieldLayout L = layout_of(p);
+    PostJob pj = {};
+    pj.map = p->map;
+    pj.fixed = p->fixed;
+    pj.target = p->target;
+    pj.nbx = p->nbx;
+    pj.nby = p->nby;
+    pj.with_fill = 1;
+    if (p->field_mode == GP103_FIELD_FP32) {
+        pj.dens = (float*)((char*)p->field_work + L.w_a);
+    } else {
+        __nv_bfloat16* t = (__nv_bfloat16*)((char*)p->field_work + L.w_a);
+        pj.t0 = t;
+        pj.t1 = t + nb;
+        pj.t2 = t + 2 * nb;
+        pj.terms = 3;
+    }
+    pj.red = reduce_slot(p->red, p->counters, R_OVF);
+    TRY(launch_post_plain(pj, s));
+    if (p->jnbx > 0) {
+        PostJob jp = {};
+        jp.map = p->jmap;
+        jp.fixed = p->jfixed;
+        jp.target = p->target;
+        jp.nbx = p->jnbx;
+        jp.nby = p->jnby;
+        jp.red = reduce_slot(p->red, p->counters, R_JOVF);
+        TRY(launch_post_plain(jp, s));
+    }
+    return run_field(p, nullptr, s);
+}
+
+static GatherJob gather_job(const gp103_plan* p) {
+    GatherJob g = {};
+    g.size = (const float2*)p->size;
+    g.ratio = p->ratio;
+    g.pins = p->pins;
+    g.area = p->area;
+    g.num_nodes = p->num_nodes;
+    g.num_mov = p->num_mov;
+    g.inv_bx = 1.f / p->bx;
+    g.inv_by = 1.f / p->by;
+    g.nbx = p->nbx;
+    g.nby = p->nby;
+    g.pin_grad = (const float2*)p->pin_grad;
+    g.cell_start = p->cell_start;
+    g.cell_pin = p->cell_pin;
+    g.red = reduce_slot(p->red, p->counters, R_GRAD);
+    return g;
+}
+
+static WaJob wa_job(const gp103_plan* p) {
+    WaJob w = {};
+    w.pin_cell = p->pin_cell;
+    w.pin_off = (const float2*)p->pin_off;
+    w.net_start = p->net_start;
+    w.num_nets = p->num_nets;
+    w.num_mov = p->num_mov;
+    w.gamma = p->kp;
+    w.pin_grad = (float2*)p->pin_grad;
+    w.red = reduce_slot(p->red, p->counters, R_WA);
+    return w;
+}
+
+extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    const gp103_plan* p = plan;
+    REQUIRE(phase == GP103_PHASE_START || phase == GP103_PHASE_DENSITY);
+    REQUIRE(p->u[0] && p->u[1] && p->v[0] && p->v[1] && p->g[0] && p->g[1] && p->cur && p->lo && p->hi);
+    REQUIRE(phase == GP103_PHASE_START ? p->T != nullptr : (p->S && p->c && p->best));
+    StepJob sj = {};
+    for (int k = 0; k < 2; k++) { sj.u[k] = p->u[k]; sj.v[k] = p->v[k]; sj.g[k] = p->g[k]; }
+    sj.cur = p->cur;
+    sj.lo = p->lo;
+    sj.hi = p->hi;
+    sj.kp = p->kp;
+    sj.S = phase == GP103_PHASE_DENSITY ? p->S : nullptr;
+    sj.best = phase == GP103_PHASE_DENSITY ? p->best : nullptr;
+    sj.n = p->num_nodes;
+    sj.red = reduce_slot(p->red, p->counters, R_MOVED);
+    TRY(launch_step(sj, stream));
+
+    WaJob w = wa_job(p);
+    w.pos_a = (const float2*)p->v[0];
+    w.pos_b = (const float2*)p->v[1];
+    w.sel = p->cur;
+    TRY(launch_wa_net(w, stream));
+
+    GatherJob g = gather_job(p);
+    g.pos_a = (const float2*)p->v[0];
+    g.pos_b = (const float2*)p->v[1];
+    g.sel = p->cur;
+    g.gout_a = (float2*)p->g[0];
+    g.gout_b = (float2*)p->g[1];
+    g.gref_a = (const float2*)p->g[0];
+    g.gref_b = (const float2*)p->g[1];
+    g.with_wl = 1;
+    double* r_moved = reduce_out(p->red, R_MOVED);
+    double* r_grad = reduce_out(p->red, R_GRAD);
+    double* r_wa = reduce_out(p->red, R_WA);
+    if (phase == GP103_PHASE_START) {
+        TRY(launch_gather(g, stream));
+        return launch_control_start(p->T, p->kp, r_moved, r_grad, r_wa, p->cur, stream);
+    }
+    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, stream));
+    g.ex = p->ex;
+    g.ey = p->ey;
+    g.weight_p = p->kp + 1;
+    g.precond_p = p->kp + 2;
+    TRY(launch_gather(g, stream));
+    const double* ovf = reduce_out(p->red, p->jnbx > 0 ? R_JOVF : R_OVF);
+    const double scale = p->jnbx > 0 ? p->jovf_scale : p->ovf_scale;
+    return launch_control_fused(p->S, p->kp, p->c, r_moved, r_grad, r_wa, ovf, scale, p->cur, stream);
+}
+
+extern "C" int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out, const float* g_ref, double weight,
+                          double precond, int with_wl, double* out5, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    const gp103_plan* p = plan;
+    REQUIRE(pos && g_out && out5);
+    if (with_wl) {
+        WaJob w = wa_job(p);
+        w.pos_a = w.pos_b = (const float2*)pos;
+        TRY(launch_wa_net(w, stream));
+    }
+    GatherJob g = gather_job(p);
+    g.pos_a = g.pos_b = (const float2*)pos;
+    g.gout_a = g.gout_b = (float2*)g_out;
+    g.gref_a = g.gref_b = (const float2*)g_ref;
+    g.with_wl = with_wl;
+    if (weight != 0.0) {
+        TRY(density_and_field(p, pos, pos, nullptr, stream));
+        g.ex = p->ex;
+        g.ey = p->ey;
+        g.weight = (float)weight;
+        g.precond = (float)precond;
+    }
+    TRY(launch_gather(g, stream));
+    const double* r_wa = reduce_out(p->red, R_WA);
+    const double* r_grad = reduce_out(p->red, R_GRAD);
+    const double* ovf = reduce_out(p->red, p->jnbx > 0 ? R_JOVF : R_OVF);
+    // out5 = (|g - g_ref|^2, WA, HPWL, overflow sum, L1 of g over the cells)
+    TRY(launch_gather_scalars(r_grad, 1, r_wa, 2, ovf, 1, out5, stream));
+    return launch_gather_scalars(r_grad + 1, 1, nullptr, 0, nullptr, 0, out5 + 4, stream);
+}
+
+extern "C" int gp103_probe(const gp103_plan* plan, const float* v, const float* g, double step, float* probe,
+                           double* out1, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    REQUIRE(v && g && probe && out1 && plan->lo && plan->hi);
+    Reduce r = reduce_slot(plan->red, plan->counters, R_MOVED);
+    TRY(launch_probe(v, g, plan->lo, plan->hi, (float)step, plan->num_nodes, probe, r, stream));
+    return launch_gather_scalars(r.out, 1, nullptr, 0, nullptr, 0, out1, stream);
+}
+
+extern "C" int gp103_finish(const gp103_plan* plan, cudaStream_t stream) {
+    REQUIRE(plan && plan->S && plan->cur && plan->v[0] && plan->v[1] && plan->best);
+    return launch_finish(plan->S, plan->cur, plan->v[0], plan->v[1], plan->best, 2 * plan->num_nodes, stream);
+}

@@ -1,0 +1,288 @@
+// Density: fixed-point charge scatter, map post-processing and the field gather (GB300, sm_103a).
+//
+// Reference: cpp_to_py/gp_cuda_kernel.cu:67-153 (density_map_kernel, density_post_kernel, density_grad_kernel) and
+// src/core/electronic_density_layer.py:96-149. The charge of a (node, bin) pair is the reference's float32 product
+// truncated to 2^-32 bin areas and summed as 64-bit integers: the map is the same integers in any summation order.
+// This file is built with -ftz=true, as the reference's kernels are (--use_fast_math), so that even denormal
+// intermediates round the same way.
+#include <cuda_bf16.h>
+
+#include "gp103.cuh"
+#include "kernels.cuh"
+
+namespace gp103 {
+
+// ----------------------------------------------------------------------------- scatter
+// A block takes a chunk of SCAT_CHUNK consecutive nodes, all movable or all fillers. If the bins its nodes touch fit
+// in shared memory (bounding box <= SCAT_SMEM_BINS), the block adds its charges there with shared 64-bit atomics and
+// then adds every non-zero bin to the global map once; otherwise it adds each charge to the global map directly.
+constexpr int SCAT_THREADS = 256;
+constexpr int SCAT_PER_THREAD = 4;
+constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;
+constexpr int SCAT_SMEM_BINS = 6144;      // 48 KB of 64-bit bins
+
+__global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(ScatterJob j) {
+    __shared__ unsigned long long tile[SCAT_SMEM_BINS];
+    __shared__ int box[4];
+    const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
+    const int cell_chunks = ceil_div(j.num_mov, SCAT_CHUNK);
+    int first, last;
+    unsigned long long* map;
+    if ((int)blockIdx.x < cell_chunks) {
+        first = blockIdx.x * SCAT_CHUNK;
+        last = min(first + SCAT_CHUNK, j.num_mov);
+        map = j.map0;
+    } else {
+        first = j.num_mov + (blockIdx.x - cell_chunks) * SCAT_CHUNK;
+        last = min(first + SCAT_CHUNK, j.num_nodes);
+        map = j.map1;
+    }
+    if (threadIdx.x == 0) { box[0] = INT_MAX; box[1] = INT_MIN; box[2] = INT_MAX; box[3] = INT_MIN; }
+    Span sx[SCAT_PER_THREAD], sy[SCAT_PER_THREAD];
+    float ratio[SCAT_PER_THREAD];
+    int x0 = INT_MAX, x1 = INT_MIN, y0 = INT_MAX, y1 = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < SCAT_PER_THREAD; k++) {
+        int i = first + k * SCAT_THREADS + threadIdx.x;
+        sx[k].b0 = 1; sx[k].b1 = 0; sy[k].b0 = 1; sy[k].b1 = 0; ratio[k] = 0.f;
+        if (i < last) {
+            float2 p = pos[i], s = j.size[i];
+            sx[k] = span(p.x, s.x, j.inv_bx, j.nbx);
+            sy[k] = span(p.y, s.y, j.inv_by, j.nby);
+            ratio[k] = j.ratio[i];
+            if (sx[k].b0 <= sx[k].b1 && sy[k].b0 <= sy[k].b1) {
+                x0 = min(x0, sx[k].b0); x1 = max(x1, sx[k].b1);
+                y0 = min(y0, sy[k].b0); y1 = max(y1, sy[k].b1);
+            }
+        }
+    }
+    x0 = __reduce_min_sync(0xffffffffu, x0); x1 = __reduce_max_sync(0xffffffffu, x1);
+    y0 = __reduce_min_sync(0xffffffffu, y0); y1 = __reduce_max_sync(0xffffffffu, y1);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && x0 <= x1) {
+        atomicMin(&box[0], x0); atomicMax(&box[1], x1); atomicMin(&box[2], y0); atomicMax(&box[3], y1);
+    }
+    __syncthreads();
+    const int bx0 = box[0], bx1 = box[1], by0 = box[2], by1 = box[3];
+    if (bx0 > bx1 || map == nullptr) return;                       // nothing to add (uniform over the block)
+    const long long w = (long long)(bx1 - bx0 + 1), h = (long long)(by1 - by0 + 1);
+    if (w * h <= SCAT_SMEM_BINS) {
+        const int H = (int)h, area = (int)(w * h);
+        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) tile[t] = 0ull;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAT_PER_THREAD; k++) {
+            for (int x = sx[k].b0; x <= sx[k].b1; x++) {
+                const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
+                for (int y = sy[k].b0; y <= sy[k].b1; y++) {
+                    unsigned long long q = charge(wx, overlap(sy[k], y));
+                    if (q) atomicAdd(&tile[(x - bx0) * H + (y - by0)], q);
+                }
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) {
+            unsigned long long q = tile[t];
+            if (q) atomicAdd(&map[(size_t)(bx0 + t / H) * j.nby + (by0 + t % H)], q);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAT_PER_THREAD; k++) {
+            for (int x = sx[k].b0; x <= sx[k].b1; x++) {
+                const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
+                for (int y = sy[k].b0; y <= sy[k].b1; y++) {
+                    unsigned long long q = charge(wx, overlap(sy[k], y));
+                    if (q) atomicAdd(&map[(size_t)x * j.nby + y], q);
+                }
+            }
+        }
+    }
+}
+
+int launch_scatter(const ScatterJob& j, cudaStream_t s) {
+    int blocks = ceil_div(j.num_mov, SCAT_CHUNK) + ceil_div(j.num_nodes - j.num_mov, SCAT_CHUNK);
+    if (blocks == 0) return GP103_OK;
+    scatter_kernel<<<blocks, SCAT_THREADS, 0, s>>>(j);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// ----------------------------------------------------------------------------- post
+// Reference layout: rho mirrored [2 nbx][2 nby] and over [nbx][nby] (density_post_kernel, gp_cuda_kernel.cu:130-139).
+__global__ void post_mirror_kernel(const unsigned long long* map, const float* fixed, float target, int nbx, int nby,
+                                   float* rho, float* over) {
+    const int nb = nbx * nby;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int bx = b / nby, by = b - bx * nby, w = 2 * nby, mx = 2 * nbx - 1 - bx, my = w - 1 - by;
+        const float mov = __fadd_rn((float)((double)map[b] / DENSITY_SCALE), fixed[b]);
+        const float r = __fadd_rn(mov, (float)((double)map[nb + b] / DENSITY_SCALE));
+        over[b] = fmaxf(__fsub_rn(mov, target), 0.f);
+        rho[(size_t)bx * w + by] = r;
+        rho[(size_t)bx * w + my] = r;
+        rho[(size_t)mx * w + by] = r;
+        rho[(size_t)mx * w + my] = r;
+    }
+}
+
+int launch_post_mirror(const unsigned long long* map, const float* fixed, float target, int nbx, int nby, float* rho,
+                       float* over, cudaStream_t s) {
+    const int nb = nbx * nby;
+    post_mirror_kernel<<<grid_for(nb, 256, 8), 256, 0, s>>>(map, fixed, target, nbx, nby, rho, over);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// Fused layout: the plain total density for the field (float32 plane, or the bf16 terms of its split) and the
+// float64 sum of the density above the target; the map is zeroed behind the read for the next pass.
+__device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0, __nv_bfloat16* t1,
+                                           __nv_bfloat16* t2, size_t at) {
+    __nv_bfloat16 a = __float2bfloat16_rn(r);
+    float rem = __fsub_rn(r, __bfloat162float(a));
+    __nv_bfloat16 b = __float2bfloat16_rn(rem);
+    t0[at] = a;
+    t1[at] = b;
+    if (terms > 2) t2[at] = __float2bfloat16_rn(__fsub_rn(rem, __bfloat162float(b)));
+}
+
+__global__ void post_plain_kernel(PostJob j) {
+    const int nb = j.nbx * j.nby;
+    double ov = 0.0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const unsigned long long m0 = j.map[b];
+        const float mov = __fadd_rn((float)((double)m0 / DENSITY_SCALE), j.fixed[b]);
+        ov += (double)fmaxf(__fsub_rn(mov, j.target), 0.f);
+        if (j.with_fill) {
+            const unsigned long long m1 = j.map[nb + b];
+            const float r = __fadd_rn(mov, (float)((double)m1 / DENSITY_SCALE));
+            if (j.dens) j.dens[b] = r;
+            if (j.t0) split_bf16(r, j.terms, j.t0, j.t1, j.t2, b);
+            j.map[nb + b] = 0ull;
+        }
+        j.map[b] = 0ull;
+    }
+    double v[1] = {ov};
+    grid_sum<1>(v, j.red);
+}
+
+int launch_post_plain(const PostJob& j, cudaStream_t s) {
+    post_plain_kernel<<<grid_for((long long)j.nbx * j.nby, 256, 4), 256, 0, s>>>(j);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// ----------------------------------------------------------------------------- gather
+// Reference semantics (density_grad_kernel): field = mirrored planes [2][2 nbx][2 nby], first quadrant read.
+__global__ void gather_mirror_kernel(const float2* pos, const float2* size, const float* ratio, const float* field,
+                                     const float2* wl_grad, const float* pins, const float* area, int num_nodes,
+                                     int num_wl, const float* weight_p, const float* precond_p, float inv_bx,
+                                     float inv_by, int nbx, int nby, float2* grad) {
+    const float weight = *weight_p, precond = *precond_p;
+    const float* fy = field + (size_t)4 * nbx * nby;
+    const int ld = 2 * nby;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
+        const float2 p = pos[i], sz = size[i];
+        const Span sx = span(p.x, sz.x, inv_bx, nbx), sy = span(p.y, sz.y, inv_by, nby);
+        const float r = ratio[i];
+        float gx = 0.f, gy = 0.f;
+        for (int x = sx.b0; x <= sx.b1; x++) {
+            const float wx = __fmul_rn(r, overlap(sx, x));
+            for (int y = sy.b0; y <= sy.b1; y++) {
+                const float w = __fmul_rn(wx, overlap(sy, y));
+                gx = fmaf(-w, field[(size_t)x * ld + y], gx);
+                gy = fmaf(-w, fy[(size_t)x * ld + y], gy);
+            }
+        }
+        gx *= weight;
+        gy *= weight;
+        if (i < num_wl) {
+            const float2 wl = wl_grad[i];
+            gx += wl.x;
+            gy += wl.y;
+        }
+        const float scale = precond < 0.f ? 1.f : 1.f / fmaxf(pins[i] + precond * area[i], 1.f);
+        grad[i] = make_float2(gx * scale, gy * scale);
+    }
+}
+
+int launch_gather_mirror(const float* pos, const float* size, const float* ratio, const float* field,
+                         const float* wl_grad, const float* pins, const float* area, int num_nodes, int num_wl,
+                         const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,
+                         cudaStream_t s) {
+    if (num_nodes == 0) return GP103_OK;
+    gather_mirror_kernel<<<grid_for(num_nodes, 256, 8), 256, 0, s>>>(
+        (const float2*)pos, (const float2*)size, ratio, field, (const float2*)wl_grad, pins, area, num_nodes, num_wl,
+        weight, precond, 1.f / bx, 1.f / by, nbx, nby, (float2*)grad);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// Fused gather: the field planes [nbx][nby]; the wirelength gradient of a cell summed here from the pins' gradients
+// (cell CSR, fixed order); the new gradient, its squared distance to the previous one and its L1 norm over the
+// cells reduced in float64.
+__global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
+    const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
+    float2* gout = pick_mut(j.gout_a, j.gout_b, j.sel);
+    const float2* gref = j.gref_a ? pick_ref(j.gref_a, j.gref_b, j.sel) : nullptr;
+    float weight = j.weight_p ? j.weight_p[0] : j.weight;
+    float precond = j.precond_p ? j.precond_p[0] : j.precond;
+    const bool density = j.ex != nullptr;
+    double d2 = 0.0, l1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.num_nodes; i += gridDim.x * blockDim.x) {
+        float gx = 0.f, gy = 0.f;
+        if (density) {
+            const float2 p = pos[i], sz = j.size[i];
+            const Span sx = span(p.x, sz.x, j.inv_bx, j.nbx), sy = span(p.y, sz.y, j.inv_by, j.nby);
+            const float r = j.ratio[i];
+            for (int x = sx.b0; x <= sx.b1; x++) {
+                const float wx = __fmul_rn(r, overlap(sx, x));
+                const float* ex = j.ex + (size_t)x * j.nby;
+                const float* ey = j.ey + (size_t)x * j.nby;
+                for (int y = sy.b0; y <= sy.b1; y++) {
+                    const float w = __fmul_rn(wx, overlap(sy, y));
+                    gx = fmaf(-w, ex[y], gx);
+                    gy = fmaf(-w, ey[y], gy);
+                }
+            }
+            gx *= weight;
+            gy *= weight;
+        }
+        float wx = 0.f, wy = 0.f;
+        if (j.with_wl && i < j.num_mov) {
+            const int k0 = j.cell_start[i], k1 = j.cell_start[i + 1];
+            for (int k = k0; k < k1; k++) {
+                const float2 q = j.pin_grad[j.cell_pin[k]];
+                wx += q.x;
+                wy += q.y;
+            }
+        }
+        float2 g;
+        if (density) {
+            gx += wx;
+            gy += wy;
+            const float scale = precond < 0.f ? 1.f : 1.f / fmaxf(j.pins[i] + precond * j.area[i], 1.f);
+            g = make_float2(gx * scale, gy * scale);
+        } else if (i < j.num_mov) {                     // wirelength only: wl_grad / max(1, pins)
+            const float pc = fmaxf(j.pins[i], 1.f);
+            g = make_float2(wx / pc, wy / pc);
+        } else {
+            g = make_float2(0.f, 0.f);
+        }
+        gout[i] = g;
+        if (gref) {
+            const float2 o = gref[i];
+            const double dx = (double)g.x - (double)o.x, dy = (double)g.y - (double)o.y;
+            d2 += dx * dx + dy * dy;
+        }
+        if (i < j.num_mov) l1 += fabs((double)g.x) + fabs((double)g.y);
+    }
+    double v[2] = {d2, l1};
+    grid_sum<2>(v, j.red);
+}
+
+int launch_gather(const GatherJob& j, cudaStream_t s) {
+    gather_kernel<<<grid_for(j.num_nodes, 256, 8), 256, 0, s>>>(j);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+}  // namespace gp103

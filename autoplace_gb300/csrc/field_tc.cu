@@ -1,0 +1,371 @@
+// Tensor-core form of the field's six GEMMs (GB300, sm_103a): tcgen05.mma (kind::f16, bf16 operands, float32
+// accumulation in tensor memory), operands staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) through an
+// mbarrier pipeline, one elected thread issuing the MMAs, four warps reading the accumulator back (tcgen05.ld) into
+// fused epilogues. Operands are float32 values split into bf16 terms, a = a0 + a1 + a2 (each term the bf16 rounding
+// of what the previous ones leave), stored as three planes; a product is a list of (A term, B term) pairs over the
+// same K, concatenated along K into one accumulation:
+//   bf16x3: (0,0) (0,1) (1,0)                          ~1e-5 of the max
+//   bf16x6: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)        ~1e-7 of the max (float32-level)
+// Shapes: M, N multiples of 128, K a multiple of 64 (force grids of 128 .. 2048 bins per side).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include "field.cuh"
+#include "gp103.cuh"
+
+namespace gp103 {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 6;
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;                  // 16 KB per operand tile
+constexpr int TC_STAGE_BYTES = 2 * TC_TILE_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+constexpr long long TC_WAIT_NS = 2000000000LL;                  // a wait that takes 2 s has failed
+
+struct TcProblem {
+    int M, N, K;
+    int epi;
+    __nv_bfloat16* o_terms;      // EPI_TRANS: [3][N][M]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
+    __nv_bfloat16* o2_terms;
+    float* out_f32;              // EPI_PLAIN: [M][N]
+    const float* w0; const float* w1;
+};
+
+struct TcArgs {
+    TcProblem p[2];
+    int nseg;
+    int seg_a[6], seg_b[6];
+    int* err;
+};
+
+// ----------------------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ long long gtime() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false (and the error flag set) if the phase did not complete within TC_WAIT_NS.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = gtime();
+    while (!mbar_try(bar, parity)) {
+        if (gtime() - t0 > TC_WAIT_NS || *(volatile int*)err != 0) {
+            atomicCAS(err, 0, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major tile of 128-byte rows, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
+    d |= (uint64_t)1 << 16;                         // leading byte offset (unused by swizzled K-major tiles)
+    d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                         // descriptor version of tcgen05
+    d |= (uint64_t)2 << 61;                         // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor: D float32, A and B bf16, both K-major, M = 128, N = TC_BN.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+                              ((uint32_t)(TC_BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem), "l"(a), "l"(b), "r"(TC_IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16& b, __nv_bfloat16& c) {
+    a = __float2bfloat16_rn(v);
+    const float r1 = __fsub_rn(v, __bfloat162float(a));
+    b = __float2bfloat16_rn(r1);
+    c = __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(b)));
+}
+
+// ----------------------------------------------------------------------------- the GEMM kernel
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
+                   const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1, TcArgs args) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);     // full[S], empty[S], done
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int z = blockIdx.z;
+    const TcProblem& P = args.p[z];
+    const CUtensorMap* ma = z ? &a1 : &a0;
+    const CUtensorMap* mb = z ? &b1 : &b0;
+    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+    const int kblocks = P.K / TC_BK, total = kblocks * args.nseg;
+    int* err = args.err;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(smem_u32(&bars[s]), 1);
+            mbar_init(smem_u32(&bars[TC_STAGES + s]), 1);
+        }
+        mbar_init(smem_u32(&bars[2 * TC_STAGES]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t done_bar = smem_u32(&bars[2 * TC_STAGES]);
+
+    if (warp == 0 && lane == 0) {                                // TMA producer
+        for (int it = 0; it < total; it++) {
+            const int s = it % TC_STAGES;
+            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+            if (!mbar_wait(smem_u32(&bars[TC_STAGES + s]), ph ^ 1u, err, 1)) break;
+            const int seg = it / kblocks, kb = it % kblocks;
+            const uint32_t full = smem_u32(&bars[s]);
+            mbar_expect_tx(full, TC_STAGE_BYTES);
+            uint8_t* st = smem + s * TC_STAGE_BYTES;
+            tma_load_3d(smem_u32(st), ma, full, kb * TC_BK, m0, args.seg_a[seg]);
+            tma_load_3d(smem_u32(st + TC_TILE_BYTES), mb, full, kb * TC_BK, n0, args.seg_b[seg]);
+        }
+    } else if (warp == 1 && lane == 0) {                         // MMA issuer
+        bool ok = true;
+        for (int it = 0; it < total && ok; it++) {
+            const int s = it % TC_STAGES;
+            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+            if (!mbar_wait(smem_u32(&bars[s]), ph, err, 2)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_TILE_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; kk++)
+                mma_bf16(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (it > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(smem_u32(&bars[TC_STAGES + s]));
+        }
+        mma_commit(done_bar);                                    // completes once every MMA above has
+    }
+    __syncwarp();
+
+    // epilogue: warp w owns accumulator rows 32 w .. 32 w + 31 (tensor-memory lanes)
+    const bool have = mbar_wait(done_bar, 0, err, 3) && *(volatile int*)err == 0;
+    tc_fence_after();
+    if (have) {
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            const int col = n0 + c0;
+            if (P.epi == EPI_PLAIN) {
+                float4* o = (float4*)(P.out_f32 + (size_t)row * P.N + col);
+#pragma unroll
+                for (int i = 0; i < 8; i++) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            } else if (P.epi == EPI_TRANS) {
+                const size_t plane = (size_t)P.M * P.N;
+#pragma unroll
+                for (int i = 0; i < 32; i++) {
+                    __nv_bfloat16 a, b, c;
+                    split3(v[i], a, b, c);
+                    const size_t at = (size_t)(col + i) * P.M + row;
+                    P.o_terms[at] = a;
+                    P.o_terms[plane + at] = b;
+                    P.o_terms[2 * plane + at] = c;
+                }
+            } else {
+                const size_t plane = (size_t)P.M * P.N;
+                const size_t base = (size_t)row * P.N + col;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const float* w = (h ? P.w1 : P.w0) + base;
+                    __nv_bfloat16* o = (h ? P.o2_terms : P.o_terms) + base;
+                    __align__(16) __nv_bfloat16 ta[32], tb[32], tcv[32];
+#pragma unroll
+                    for (int i = 0; i < 32; i++) split3(v[i] * __ldg(w + i), ta[i], tb[i], tcv[i]);
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        ((uint4*)o)[i] = ((uint4*)ta)[i];
+                        ((uint4*)(o + plane))[i] = ((uint4*)tb)[i];
+                        ((uint4*)(o + 2 * plane))[i] = ((uint4*)tcv)[i];
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+    }
+}
+
+// ----------------------------------------------------------------------------- host side
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// Three bf16 planes [3][rows][K] as a 3-D tensor (K, rows, term); box = 64 x 128 x 1.
+static bool make_map(CUtensorMap* m, const void* base, int rows, int K) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
+    cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
+    cuuint32_t box[3] = {TC_BK, TC_BM, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+bool field_tc_supported(int nbx, int nby) {
+    return nbx >= 128 && nby >= 128 && nbx % 128 == 0 && nby % 128 == 0 && nbx <= 4096 && nby <= 4096;
+}
+
+struct TcOp {
+    const void* a; int arows;
+    const void* b; int brows;
+    TcProblem p;
+};
+
+static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        attr = true;
+    }
+    CUtensorMap maps[4];
+    TcArgs args = {};
+    for (int z = 0; z < 2; z++) {
+        const TcOp& o = ops[z < nops ? z : 0];
+        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K) || !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K))
+            return GP103_ERR_CUDA;
+        args.p[z] = o.p;
+    }
+    static const int x3a[3] = {0, 0, 1}, x3b[3] = {0, 1, 0};
+    static const int x6a[6] = {2, 1, 0, 1, 0, 0}, x6b[6] = {0, 1, 2, 0, 1, 0};
+    args.nseg = mode == GP103_FIELD_BF16X3 ? 3 : 6;
+    for (int i = 0; i < args.nseg; i++) {
+        args.seg_a[i] = mode == GP103_FIELD_BF16X3 ? x3a[i] : x6a[i];
+        args.seg_b[i] = mode == GP103_FIELD_BF16X3 ? x3b[i] : x6b[i];
+    }
+    args.err = err;
+    const TcProblem& p = ops[0].p;
+    dim3 grid(p.N / TC_BN, p.M / TC_BM, nops);
+    tc_gemm_kernel<<<grid, 128, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+__global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        __nv_bfloat16 a, b, c;
+        split3(d[e], a, b, c);
+        t[e] = a;
+        t[n + e] = b;
+        t[2 * n + e] = c;
+    }
+}
+
+int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* density, float* ex, float* ey,
+             cudaStream_t s) {
+    if (!field_tc_supported(L.nbx, L.nby)) return GP103_ERR_SHAPE;
+    const char* c = (const char*)cbuf;
+    char* w = (char*)wbuf;
+    const int X = L.nbx, Y = L.nby;
+    auto B = [](const char* base, size_t off) { return (__nv_bfloat16*)(base + off); };
+    int* err = (int*)(w + L.w_err);
+    int st;
+    if (density) {
+        split_density_kernel<<<grid_for((size_t)X * Y, 256, 8), 256, 0, s>>>(density, (size_t)X * Y, B(w, L.w_a));
+        GP103_CHECK_LAUNCH();
+    }
+    auto prob = [](int M, int N, int K, int epi) {
+        TcProblem p = {};
+        p.M = M; p.N = N; p.K = K; p.epi = epi;
+        return p;
+    };
+    // 1: Tt = (A Cy^T)^T
+    TcOp o1 = {B(w, L.w_a), X, B(c, L.c_cy), Y, prob(X, Y, Y, EPI_TRANS)};
+    o1.p.o_terms = B(w, L.w_tt);
+    if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
+    // 2: K = Cx T -> Kx, Ky
+    TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
+    o2.p.o_terms = B(w, L.w_kx);
+    o2.p.o2_terms = B(w, L.w_ky);
+    o2.p.w0 = (const float*)(c + L.c_wx);
+    o2.p.w1 = (const float*)(c + L.c_wy);
+    if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
+    // 3a / 4a: Pt = (Kx Cy)^T, Qt = (Ky Sy)^T
+    TcOp o3[2] = {{B(w, L.w_kx), X, B(c, L.c_cyt), Y, prob(X, Y, Y, EPI_TRANS)},
+                  {B(w, L.w_ky), X, B(c, L.c_syt), Y, prob(X, Y, Y, EPI_TRANS)}};
+    o3[0].p.o_terms = B(w, L.w_pt);
+    o3[1].p.o_terms = B(w, L.w_qt);
+    if ((st = launch_tc(o3, 2, L.mode, err, s))) return st;
+    // 3b / 4b: Ex = Sx^T P, Ey = Cx^T Q
+    TcOp o4[2] = {{B(c, L.c_sxt), X, B(w, L.w_pt), Y, prob(X, Y, X, EPI_PLAIN)},
+                  {B(c, L.c_cxt), X, B(w, L.w_qt), Y, prob(X, Y, X, EPI_PLAIN)}};
+    o4[0].p.out_f32 = ex;
+    o4[1].p.out_f32 = ey;
+    return launch_tc(o4, 2, L.mode, err, s);
+}
+
+}  // namespace gp103

@@ -1,0 +1,99 @@
+// Job descriptions and launchers shared by the gp103 translation units.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "gp103.cuh"
+
+namespace gp103 {
+
+// Ping-pong selection: with sel = the device index of the current buffers, the evaluated point of a pass lives in
+// the other buffer: pick(a, b, sel) = *sel ? a : b; pick_ref is the current one. sel == nullptr -> a.
+template <typename T>
+__device__ __forceinline__ const T* pick(const T* a, const T* b, const int* sel) {
+    return sel == nullptr ? a : (*sel ? a : b);
+}
+template <typename T>
+__device__ __forceinline__ T* pick_mut(T* a, T* b, const int* sel) {
+    return sel == nullptr ? a : (*sel ? a : b);
+}
+template <typename T>
+__device__ __forceinline__ const T* pick_ref(const T* a, const T* b, const int* sel) {
+    return sel == nullptr ? a : (*sel ? b : a);
+}
+
+// Reduction slots of a plan's `red` buffer (float64): each has K <= 4 values, MAX_BLOCKS partials per value.
+constexpr int MAX_BLOCKS = 2048;
+enum { R_WA = 0, R_OVF, R_JOVF, R_MOVED, R_GRAD, R_COUNT };
+inline Reduce reduce_slot(double* red, unsigned int* counters, int slot) {
+    Reduce r;
+    r.partials = red + (size_t)slot * 4 * MAX_BLOCKS;
+    r.counter = counters + slot;
+    r.out = red + (size_t)R_COUNT * 4 * MAX_BLOCKS + slot * 4;
+    return r;
+}
+inline double* reduce_out(double* red, int slot) { return red + (size_t)R_COUNT * 4 * MAX_BLOCKS + slot * 4; }
+constexpr size_t RED_DOUBLES = (size_t)R_COUNT * 4 * MAX_BLOCKS + R_COUNT * 4;
+
+struct WaJob {
+    const float2* pos_a; const float2* pos_b; const int* sel;
+    const int* pin_cell; const float2* pin_off; const int* net_start;
+    int num_nets, num_mov;
+    const float* gamma;
+    float2* pin_grad;
+    float2* out;            // per-net (WA, HPWL), may be null
+    Reduce red;             // (WA, HPWL) totals; red.out == nullptr: none
+};
+
+struct ScatterJob {
+    const float2* pos_a; const float2* pos_b; const int* sel;
+    const float2* size; const float* ratio;
+    int num_nodes, num_mov;
+    float inv_bx, inv_by;
+    int nbx, nby;
+    unsigned long long* map0;   // nodes < num_mov
+    unsigned long long* map1;   // the rest (null: not added)
+};
+
+struct PostJob {
+    unsigned long long* map;    // [1 or 2][nbx][nby], zeroed behind the read
+    const float* fixed;
+    float target;
+    int nbx, nby;
+    int with_fill;              // map has the filler plane
+    float* dens;                // plain density, may be null
+    __nv_bfloat16 *t0, *t1, *t2;  // bf16 split terms of the density, may be null
+    int terms;
+    Reduce red;                 // sum of the density above the target
+};
+
+struct GatherJob {
+    const float2* pos_a; const float2* pos_b; const int* sel;
+    const float2* size; const float* ratio; const float* pins; const float* area;
+    int num_nodes, num_mov;
+    float inv_bx, inv_by;
+    int nbx, nby;
+    const float* ex; const float* ey;      // null: no density term (wirelength-only gradient)
+    const float* weight_p; const float* precond_p;   // device scalars, or null: the host values below
+    float weight, precond;
+    int with_wl;
+    const float2* pin_grad; const int* cell_start; const int* cell_pin;
+    float2* gout_a; float2* gout_b;
+    const float2* gref_a; const float2* gref_b;     // null: no distance
+    Reduce red;                 // (|g - gref|^2, L1 of g over the cells)
+};
+
+int launch_wa_net(const WaJob& j, cudaStream_t s);
+int launch_wa_cell(const float2* pin_grad, const int* cell_start, const int* cell_pin, int num_mov, float2* grad,
+                   cudaStream_t s);
+int launch_scatter(const ScatterJob& j, cudaStream_t s);
+int launch_post_mirror(const unsigned long long* map, const float* fixed, float target, int nbx, int nby, float* rho,
+                       float* over, cudaStream_t s);
+int launch_post_plain(const PostJob& j, cudaStream_t s);
+int launch_gather_mirror(const float* pos, const float* size, const float* ratio, const float* field,
+                         const float* wl_grad, const float* pins, const float* area, int num_nodes, int num_wl,
+                         const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,
+                         cudaStream_t s);
+int launch_gather(const GatherJob& j, cudaStream_t s);
+
+}  // namespace gp103

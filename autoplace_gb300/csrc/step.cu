@@ -1,0 +1,281 @@
+// Nesterov / Barzilai-Borwein step, the run's control and the accepted-step selection (GB300, sm_103a).
+//
+// Reference: cpp_to_py/gp_cuda_kernel.cu:155-259 (nesterov_step_kernel, control_kernel, select_kernel) with the
+// host rules they replay: src/nesterov_optimizer.py:34-53, src/param_scheduler.py:63-116, src/resolution.py:33-56.
+// The fused path keeps two copies of (u, v, g) and an index of the current one in device memory: an accepted step
+// flips the index instead of copying three arrays (select_kernel's copies).
+#include <math.h>
+
+#include "gp103.cuh"
+#include "kernels.cuh"
+#include "step.cuh"
+
+namespace gp103 {
+
+// ----------------------------------------------------------------------------- reference-layout kernels
+__global__ void nesterov_step_kernel(const float* u, const float* v, const float* g, const float* lo, const float* hi,
+                                     const float* alpha_p, const float* coef_p, int n, float* u_next, float* v_next) {
+    const float alpha = *alpha_p, coef = *coef_p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float un = fmaf(-alpha, g[i], v[i]);
+        u_next[i] = un;
+        v_next[i] = fminf(fmaxf(fmaf(coef, un - u[i], un), lo[i]), hi[i]);
+    }
+}
+
+int launch_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,
+                         const float* alpha, const float* coef, int n, float* u_next, float* v_next, cudaStream_t s) {
+    if (n == 0) return GP103_OK;
+    nesterov_step_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(u, v, g, lo, hi, alpha, coef, n, u_next, v_next);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// One pass of the control, float64, in the order of control_kernel (gp_cuda_kernel.cu:183-240). -> accepted.
+__device__ bool control_body(double* S, float* kp, const double* c, double moved, double turned, double hpwl,
+                             double ovf, double wa) {
+    S[S_ACCEPT] = 0;
+    S[S_IS_BEST] = 0;
+    if (S[S_STOP] != 0) return false;
+    if (!(isfinite(moved) && isfinite(turned) && isfinite(hpwl) && isfinite(ovf))) {
+        S[S_STOP] = 3;
+        return false;
+    }
+    const double alpha_next = turned > 0 ? moved / turned : S[S_ALPHA];
+    S[S_ALPHA] = alpha_next;
+    S[S_EVALS] += 1;
+    S[S_ACCEPT] = 1;
+    S[S_A] = (1 + sqrt(4 * S[S_A] * S[S_A] + 1)) / 2;
+    double iter = S[S_ITER];
+    S[S_MOTION] = moved / c[C_MOTION_UNIT];
+    const double part = S[S_LAM] * c[C_TOTAL_AREA];
+    S[S_WW] = part / (c[C_TOTAL_PINS] + part);
+    const double mu = hpwl < S[S_HPWL_PREV] ? 1.05 * 0.98
+                                             : 1.05 * fmax(pow(1.05, -S[S_MOTION] * c[C_PITCH] / S[S_GAM]), 0.95);
+    S[S_HPWL_PREV] = hpwl;
+    S[S_MU] = mu;
+    S[S_LAM] *= mu;
+    if (c[C_ACCURACY] != 0) {
+        const double err = fmax(1e-6, 1 - wa / fmax(hpwl, 1e-12)), m = fmax(mu, 1 / mu);
+        const double g = S[S_GAM] * fmin(m, fmax(1 / m, sqrt(fmax(ovf, 1e-3) / c[C_REFINE] / err)));
+        S[S_GAM] = fmin(100 * c[C_BASE_GAMMA], fmax(0.01 * c[C_BASE_GAMMA], g));
+    } else {
+        S[S_GAM] = c[C_BASE_GAMMA] * pow(10.0, (ovf - 0.1) * 20 / 9 - 1);
+    }
+    S[S_ITER] = iter = iter + 1;
+    double stop = 0, is_best = 0;
+    if (!(hpwl < 1e30 && ovf < 1e30)) {
+        stop = 3;
+    } else {
+        if (iter >= c[C_MIN_ITER] && ovf < c[C_STOP_OVF]) {
+            S[S_SETTLED] += 1;
+            is_best = hpwl < S[S_BEST_HPWL];
+            S[S_BEST_HPWL] = fmin(hpwl, S[S_BEST_HPWL]);
+            if (S[S_SETTLED] > c[C_SETTLE]) stop = 1;
+        } else if (S[S_SETTLED] == 0) {
+            is_best = ovf < S[S_BEST_OVF];
+            if (ovf < S[S_BEST_OVF] * 0.999) S[S_IMPROVED] = iter;
+            S[S_BEST_OVF] = fmin(ovf, S[S_BEST_OVF]);
+        }
+        if (stop == 0) {
+            if ((is_best != 0 && S[S_SETTLED] > 0) || S[S_WW] < 0.95) S[S_IMPROVED] = iter;
+            if (iter - S[S_IMPROVED] > c[C_STALL]) stop = 2;
+        }
+        if (stop == 0 && c[C_HANDOVER] > 0 && S[S_LAM] > 0 && S[S_GAM] <= c[C_HANDOVER]) stop = 5;
+    }
+    S[S_IS_BEST] = is_best;
+    if (is_best != 0) {
+        S[S_RES_HPWL] = hpwl;
+        S[S_RES_OVF] = ovf;
+        S[S_HAS_BEST] = 1;
+    }
+    S[S_LOOP_IT] += 1;
+    if (stop == 0 && S[S_LOOP_IT] >= c[C_INNER]) stop = 4;
+    S[S_STOP] = stop;
+    if (S[S_HAS_BEST] == 0) {
+        S[S_RES_HPWL] = hpwl;
+        S[S_RES_OVF] = ovf;
+    }
+    const double a_next = (1 + sqrt(4 * S[S_A] * S[S_A] + 1)) / 2;
+    kp[0] = (float)S[S_GAM];
+    kp[1] = (float)S[S_LAM];
+    kp[2] = (float)S[S_LAM];
+    kp[3] = (float)alpha_next;
+    kp[4] = (float)((S[S_A] - 1) / a_next);
+    return true;
+}
+
+__global__ void control_kernel(double* S, float* kp, const double* c, const float* moved, const float* turned,
+                               const float* hpwl, const float* ovf, const float* wa) {
+    control_body(S, kp, c, *moved, *turned, *hpwl, *ovf, *wa);
+}
+
+int launch_control(double* S, float* kp, const double* c, const float* moved, const float* turned, const float* hpwl,
+                   const float* ovf, const float* wa, cudaStream_t s) {
+    control_kernel<<<1, 1, 0, s>>>(S, kp, c, moved, turned, hpwl, ovf, wa);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+__global__ void select_kernel(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
+                              const float* g_next, float* best, int n) {
+    if (S[S_ACCEPT] == 0) return;
+    const bool is_best = S[S_IS_BEST] != 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        u[i] = u_next[i];
+        v[i] = v_next[i];
+        g[i] = g_next[i];
+        if (is_best) best[i] = v_next[i];
+    }
+}
+
+int launch_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
+                  const float* g_next, float* best, int n, cudaStream_t s) {
+    if (n == 0) return GP103_OK;
+    select_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(S, u, v, g, u_next, v_next, g_next, best, n);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// ----------------------------------------------------------------------------- fused path
+// u' = v - alpha g, v' = clamp(u' + coef (u' - u)) from the current buffers into the other ones, |v' - v|^2 in
+// float64; the best placement of the previous pass (S[is_best]) is copied on the way.
+__global__ void __launch_bounds__(256) step_kernel(StepJob j) {
+    const int c = j.cur ? *j.cur : 0;
+    const float2 *u = (const float2*)j.u[c], *v = (const float2*)j.v[c], *g = (const float2*)j.g[c];
+    float2 *un_out = (float2*)j.u[1 - c], *vn_out = (float2*)j.v[1 - c];
+    const float alpha = j.kp[3], coef = j.kp[4];
+    const bool copy_best = j.best && j.S && j.S[S_IS_BEST] != 0;
+    const float2 *lo = (const float2*)j.lo, *hi = (const float2*)j.hi;
+    double d2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.n; i += gridDim.x * blockDim.x) {
+        const float2 vi = v[i], gi = g[i], ui = u[i], l = lo[i], h = hi[i];
+        const float ux = fmaf(-alpha, gi.x, vi.x), uy = fmaf(-alpha, gi.y, vi.y);
+        const float vx = fminf(fmaxf(fmaf(coef, ux - ui.x, ux), l.x), h.x);
+        const float vy = fminf(fmaxf(fmaf(coef, uy - ui.y, uy), l.y), h.y);
+        un_out[i] = make_float2(ux, uy);
+        vn_out[i] = make_float2(vx, vy);
+        if (copy_best) ((float2*)j.best)[i] = vi;
+        const double dx = (double)vx - (double)vi.x, dy = (double)vy - (double)vi.y;
+        d2 += dx * dx + dy * dy;
+    }
+    double r[1] = {d2};
+    grid_sum<1>(r, j.red);
+}
+
+int launch_step(const StepJob& j, cudaStream_t s) {
+    step_kernel<<<grid_for(j.n, 256, 8), 256, 0, s>>>(j);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// probe = clamp(v - step g, lo, hi); |probe - v|^2
+__global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step, int n,
+                             float2* probe, Reduce red) {
+    double d2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float2 vi = v[i], gi = g[i], l = lo[i], h = hi[i];
+        const float px = fminf(fmaxf(fmaf(-step, gi.x, vi.x), l.x), h.x);
+        const float py = fminf(fmaxf(fmaf(-step, gi.y, vi.y), l.y), h.y);
+        probe[i] = make_float2(px, py);
+        const double dx = (double)px - vi.x, dy = (double)py - vi.y;
+        d2 += dx * dx + dy * dy;
+    }
+    double r[1] = {d2};
+    grid_sum<1>(r, red);
+}
+
+int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
+                 Reduce red, cudaStream_t s) {
+    probe_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>((const float2*)v, (const float2*)g, (const float2*)lo,
+                                                      (const float2*)hi, step, n, (float2*)probe, red);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// The density phase's control from the pass's float64 reductions; an accepted step flips the current buffers.
+__global__ void control_fused_kernel(double* S, float* kp, const double* c, const double* moved2,
+                                     const double* turned2, const double* wa_hpwl, const double* ovf_sum,
+                                     double ovf_scale, int* cur) {
+    const double ovf = ovf_sum[0] * ovf_scale;
+    if (control_body(S, kp, c, sqrt(moved2[0]), sqrt(turned2[0]), wa_hpwl[1], ovf, wa_hpwl[0])) *cur = 1 - *cur;
+}
+
+int launch_control_fused(double* S, float* kp, const double* c, const double* moved2, const double* turned2,
+                         const double* wa_hpwl, const double* ovf_sum, double ovf_scale, int* cur, cudaStream_t s) {
+    control_fused_kernel<<<1, 1, 0, s>>>(S, kp, c, moved2, turned2, wa_hpwl, ovf_sum, ovf_scale, cur);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// The wirelength-only start: NesterovOptimizer.step's step length and acceptance, ParamScheduler.start_step's end
+// test (the WA fell by less than start_tol per iteration over the last 5), in float64.
+__global__ void control_start_kernel(double* T, float* kp, const double* moved2, const double* turned2,
+                                     const double* wa_hpwl, int* cur) {
+    T[GP103_T_ACCEPT] = 0;
+    if (T[GP103_T_STOP] != 0 || T[GP103_T_DONE] != 0) return;
+    const double moved = sqrt(moved2[0]), turned = sqrt(turned2[0]), wa = wa_hpwl[0], hpwl = wa_hpwl[1];
+    if (!(isfinite(moved) && isfinite(turned) && isfinite(hpwl))) {
+        T[GP103_T_STOP] = 3;
+        return;
+    }
+    if (turned > 0) T[GP103_T_ALPHA] = moved / turned;
+    const double a = T[GP103_T_A];
+    T[GP103_T_A] = (1 + sqrt(4 * a * a + 1)) / 2;
+    T[GP103_T_ACCEPT] = 1;
+    *cur = 1 - *cur;
+    T[GP103_T_EVALS] += 1;
+    T[GP103_T_HPWL] = hpwl;
+    T[GP103_T_WA] = wa;
+    T[GP103_T_ITER] += 1;
+    T[GP103_T_LOOP_IT] += 1;
+    const int n = (int)T[GP103_T_NWA];
+    T[GP103_T_RING + n % 6] = wa;
+    T[GP103_T_NWA] = n + 1;
+    const int window = 5;
+    const bool done = (n + 1) > window && !(T[GP103_T_RING + (n + 1) % 6] - wa > T[GP103_T_START_TOL] * window * wa);
+    if (done) T[GP103_T_DONE] = 1;
+    else if (T[GP103_T_LOOP_IT] >= T[GP103_T_INNER]) T[GP103_T_STOP] = 4;
+    const double an = T[GP103_T_A];
+    kp[3] = (float)T[GP103_T_ALPHA];
+    kp[4] = (float)((an - 1) / ((1 + sqrt(4 * an * an + 1)) / 2));
+}
+
+int launch_control_start(double* T, float* kp, const double* moved2, const double* turned2, const double* wa_hpwl,
+                         int* cur, cudaStream_t s) {
+    control_start_kernel<<<1, 1, 0, s>>>(T, kp, moved2, turned2, wa_hpwl, cur);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+__global__ void finish_kernel(const double* S, const int* cur, float* const* v_unused, const float* v0, const float* v1,
+                              float* best, int n) {
+    if (S[S_IS_BEST] == 0) return;
+    const float* v = *cur ? v1 : v0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) best[i] = v[i];
+}
+
+int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
+                  cudaStream_t s) {
+    if (n == 0) return GP103_OK;
+    finish_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(S, cur, nullptr, v0, v1, best, n);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+__global__ void copy_doubles_kernel(const double* a, int na, const double* b, int nb, const double* c, int nc,
+                                    double* out) {
+    int k = 0;
+    for (int i = 0; i < na; i++) out[k++] = a[i];
+    for (int i = 0; i < nb; i++) out[k++] = b[i];
+    for (int i = 0; i < nc; i++) out[k++] = c[i];
+}
+
+int launch_gather_scalars(const double* a, int na, const double* b, int nb, const double* c, int nc, double* out,
+                          cudaStream_t s) {
+    copy_doubles_kernel<<<1, 1, 0, s>>>(a, na, b, nb, c, nc, out);
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+}  // namespace gp103

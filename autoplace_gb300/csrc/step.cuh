@@ -1,0 +1,47 @@
+// Step / control declarations (state layout of the reference's control kernel).
+#pragma once
+#include "gp103.cuh"
+
+namespace gp103 {
+
+// State S [21]: the order of FIELDS in src/gpu_loop.py:19-22 (and of the enum of control_kernel).
+enum {
+    S_LAM, S_GAM, S_ALPHA, S_A, S_ITER, S_HPWL_PREV, S_MOTION, S_WW, S_MU, S_SETTLED, S_BEST_HPWL, S_BEST_OVF,
+    S_IS_BEST, S_IMPROVED, S_STOP, S_ACCEPT, S_LOOP_IT, S_EVALS, S_RES_HPWL, S_RES_OVF, S_HAS_BEST, S_SIZE
+};
+// Constants c [13]: the order of src/gpu_loop.py:50-53.
+enum {
+    C_BASE_GAMMA, C_MOTION_UNIT, C_TOTAL_PINS, C_TOTAL_AREA, C_PITCH, C_MIN_ITER, C_STOP_OVF, C_SETTLE, C_STALL,
+    C_INNER, C_REFINE, C_ACCURACY, C_HANDOVER, C_SIZE
+};
+
+struct StepJob {
+    float* u[2]; float* v[2]; float* g[2];
+    const int* cur;             // null: buffers 0 are current
+    const float* lo; const float* hi;
+    const float* kp;            // kp[3] = alpha, kp[4] = coef
+    const double* S;            // S[is_best] of the previous pass: copy v[cur] to best (null: never)
+    float* best;
+    int n;                      // nodes
+    Reduce red;                 // |v' - v|^2
+};
+
+int launch_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,
+                         const float* alpha, const float* coef, int n, float* u_next, float* v_next, cudaStream_t s);
+int launch_control(double* S, float* kp, const double* c, const float* moved, const float* turned, const float* hpwl,
+                   const float* ovf, const float* wa, cudaStream_t s);
+int launch_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
+                  const float* g_next, float* best, int n, cudaStream_t s);
+int launch_step(const StepJob& j, cudaStream_t s);
+int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
+                 Reduce red, cudaStream_t s);
+int launch_control_fused(double* S, float* kp, const double* c, const double* moved2, const double* turned2,
+                         const double* wa_hpwl, const double* ovf_sum, double ovf_scale, int* cur, cudaStream_t s);
+int launch_control_start(double* T, float* kp, const double* moved2, const double* turned2, const double* wa_hpwl,
+                         int* cur, cudaStream_t s);
+int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
+                  cudaStream_t s);
+int launch_gather_scalars(const double* a, int na, const double* b, int nb, const double* c, int nc, double* out,
+                          cudaStream_t s);
+
+}  // namespace gp103

@@ -1,0 +1,254 @@
+"""The placement loop on the GPU: one level of AutoPlace's global placement run by libgp103's fused passes.
+
+Mirrors `_place_level` + `run_level_on_gpu` (src/run_placement.py:41-76, src/gpu_loop.py:35-81):
+  1. first step length from a probe step (estimate_initial_learning_rate, src/nesterov_optimizer.py:56-61) and the
+     optimiser's own probe (NesterovOptimizer.__init__, :15-32): four gradient evaluations, four scalars read back;
+  2. the wirelength-only start (density weight 0) until the WA wirelength settles (ParamScheduler.start_step),
+     control on the device, the host polling every `check_every` passes;
+  3. the first density weight in tension units (Objective.tension_unit, src/calculator.py:20-24);
+  4. the density phase: `check_every` passes per CUDA-graph replay until the control kernel stops the run.
+Device buffers come from torch's caching allocator (plumbing only); every kernel is libgp103's, launched on one
+stream. A pass runs on the positions in the ping-pong buffers selected by a device index, so the passes of a
+graph never need the host.
+"""
+import ctypes
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import native
+from .native import Plan, Sizes, T as TI, T_SIZE
+
+S_FIELDS = ("lam gam alpha a iter hpwl_prev motion ww mu settled best_hpwl best_ovf is_best improved stop accept "
+            "loop_it evals res_hpwl res_ovf has_best").split()
+SK = {n: i for i, n in enumerate(S_FIELDS)}
+REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handover"}
+
+
+def degree_order(net_start, cell_pin):
+    """Nets sorted by degree (stable), their pins moved along; cell_pin renumbered so that every cell still sums
+    its pins in the original order. -> (pin permutation, new net_start, new cell_pin)."""
+    ns = np.asarray(net_start, np.int64)
+    deg = np.diff(ns)
+    order = np.argsort(deg, kind="stable")
+    lens = deg[order]
+    new_start = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    perm = np.repeat(ns[:-1][order] - new_start[:-1], lens) + np.arange(int(new_start[-1]))
+    newpos = np.empty_like(perm)
+    newpos[perm] = np.arange(len(perm))
+    return perm, new_start.astype(np.int32), newpos[np.asarray(cell_pin, np.int64)].astype(np.int32)
+
+
+class Placer(object):
+    def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None):
+        self.p = prob
+        self.dev = torch.device(device or "cuda")
+        self.mode = native.FIELD_MODES[field] if isinstance(field, str) else int(field)
+        self.check_every = check_every
+        self.use_graphs = use_graphs
+        self.stream = stream or torch.cuda.Stream(self.dev)
+        self._graphs = {}
+        self._keep = []
+        dev = self.dev
+        t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev))
+        z = lambda shape, dt: self._hold(torch.zeros(shape, dtype=dt, device=dev))
+        cs = prob.csr
+        perm, net_start, cell_pin = degree_order(cs.net_start, cs.cell_pin)
+        n, f, judge = prob.num_nodes, prob.force, prob.judge
+        P = len(perm)
+        sz = Sizes()
+        native.call("gp103_plan_sizes", f.nbx, f.nby, self.mode, ctypes.byref(sz))
+        pl = Plan()
+        pl.num_nodes, pl.num_mov, pl.num_nets, pl.num_pins = n, prob.num_mov, cs.num_nets, P
+        pl.nbx, pl.nby = f.nbx, f.nby
+        pl.field_mode = self.mode
+        self.pin_cell = t(cs.cell32[perm], torch.int32)
+        self.pin_off = t(cs.off[perm], torch.float32)
+        self.net_start = t(net_start, torch.int32)
+        self.cell_start = t(cs.cell_start, torch.int32)
+        self.cell_pin = t(cell_pin, torch.int32)
+        pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
+        pl.cell_start, pl.cell_pin = self._p(self.cell_start), self._p(self.cell_pin)
+        self.size, self.ratio = t(f.size, torch.float32), t(f.ratio, torch.float32)
+        self.pins, self.area = t(prob.pins, torch.float32), t(prob.area, torch.float32)
+        self.lo, self.hi = t(f.pos_lo, torch.float32), t(f.pos_hi, torch.float32)
+        for k in ("size", "ratio", "pins", "area", "lo", "hi"):
+            setattr(pl, k, self._p(getattr(self, k)))
+        pl.bx, pl.by, pl.target = f.bx, f.by, prob.target
+        self.fixed = t(f.fixed_map, torch.float32)
+        pl.fixed = self._p(self.fixed)
+        pl.ovf_scale = f.bin_area / f.mov_area
+        if judge is not None:
+            pl.jnbx, pl.jnby = judge.nbx, judge.nby
+            self.jsize, self.jratio = t(judge.size, torch.float32), t(judge.ratio, torch.float32)
+            self.jfixed = t(judge.fixed_map, torch.float32)
+            pl.jsize, pl.jratio, pl.jfixed = self._p(self.jsize), self._p(self.jratio), self._p(self.jfixed)
+            pl.jbx, pl.jby = judge.bx, judge.by
+            pl.jovf_scale = judge.bin_area / judge.mov_area
+            self.jmap = z((judge.nbx, judge.nby), torch.int64)
+            pl.jmap = self._p(self.jmap)
+        self.field_const = z((sz.field_const,), torch.uint8)
+        self.field_work = z((sz.field_work,), torch.uint8)
+        self.ex, self.ey = z((f.nbx, f.nby), torch.float32), z((f.nbx, f.nby), torch.float32)
+        pl.field_const, pl.field_work, pl.ex, pl.ey = (self._p(x) for x in (self.field_const, self.field_work,
+                                                                             self.ex, self.ey))
+        self.U = [z((n, 2), torch.float32) for _ in range(2)]
+        self.V = [z((n, 2), torch.float32) for _ in range(2)]
+        self.G = [z((n, 2), torch.float32) for _ in range(2)]
+        for k in range(2):
+            pl.u[k], pl.v[k], pl.g[k] = self._p(self.U[k]), self._p(self.V[k]), self._p(self.G[k])
+        self.best = z((n, 2), torch.float32)
+        self.cur = z((1,), torch.int32)
+        self.S = z((len(S_FIELDS),), torch.float64)
+        self.T = z((T_SIZE,), torch.float64)
+        self.kp = z((5,), torch.float32)
+        self.c = t(prob.constants(), torch.float64)
+        self.pin_grad = z((max(P, 1), 2), torch.float32)
+        self.map = z((2, f.nbx, f.nby), torch.int64)
+        self.red = z((sz.red,), torch.float64)
+        self.counters = z((16,), torch.int32)
+        self.scal = z((8,), torch.float64)
+        self.tmp = [z((n, 2), torch.float32) for _ in range(2)]
+        for k in ("best", "cur", "S", "T", "kp", "c", "pin_grad", "map", "red", "counters"):
+            setattr(pl, k, self._p(getattr(self, k)))
+        self.plan = pl
+        self._ref = ctypes.byref(pl)
+        native.call("gp103_field_constants", self._ref, self.stream.cuda_stream)
+
+    # ------------------------------------------------------------------ helpers
+    def _hold(self, x):
+        self._keep.append(x)
+        return x
+
+    @staticmethod
+    def _p(x):
+        return ctypes.c_void_p(x.data_ptr())
+
+    def sync(self):
+        self.stream.synchronize()
+
+    def eval(self, pos, g_out, g_ref=None, weight=0.0, precond=-1.0, with_wl=True):
+        """-> (|g - g_ref|^2, WA, HPWL, overflow sum, L1 of g over the cells), after a host sync."""
+        native.call("gp103_eval", self._ref, self._p(pos), self._p(g_out),
+                    None if g_ref is None else self._p(g_ref), float(weight), float(precond), int(bool(with_wl)),
+                    self._p(self.scal), self.stream.cuda_stream)
+        self.sync()
+        return self.scal[:5].cpu().numpy()
+
+    def probe(self, v, g, step, out):
+        native.call("gp103_probe", self._ref, self._p(v), self._p(g), float(step), self._p(out), self._p(self.scal),
+                    self.stream.cuda_stream)
+        self.sync()
+        return float(self.scal[0].cpu())
+
+    def _passes(self, phase, k):
+        s = self.stream.cuda_stream
+        for _ in range(k):
+            native.call("gp103_pass", self._ref, phase, s)
+
+    def _replay(self, phase):
+        if not self.use_graphs:
+            self._passes(phase, self.check_every)
+            return
+        g = self._graphs.get(phase)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream):
+                self._passes(phase, self.check_every)
+            self._graphs[phase] = g
+        with torch.cuda.stream(self.stream):
+            g.replay()
+
+    def overflow_scale(self):
+        return self.plan.jovf_scale if self.plan.jnbx > 0 else self.plan.ovf_scale
+
+    # ------------------------------------------------------------------ one level
+    def run(self, pos0, log=None):
+        """Place from pos0 ([num_nodes, 2], host or device) to the stop. -> dict (reason, iters, start_iters, hpwl,
+        overflow, evals, seconds, pos = final positions on the device)."""
+        p, o = self.p, self.p.opts
+        t0 = time.time()
+        with torch.cuda.stream(self.stream):
+            v = self.V[0]
+            v.copy_(torch.as_tensor(pos0, dtype=torch.float32).to(self.dev, non_blocking=True))
+            torch.max(torch.min(v, self.hi), self.lo, out=v)
+            gam = 10 * p.base_gamma
+            self.kp.copy_(torch.tensor([gam, 0, 0, 0, 0], dtype=torch.float32))
+            self.cur.zero_()
+        g, probe, g2 = self.G[0], self.tmp[0], self.tmp[1]
+        evals = 0
+        # estimate_initial_learning_rate
+        self.eval(v, g)
+        d1 = self.probe(v, g, o.lr, probe)
+        d2 = self.eval(probe, g2, g_ref=g)[0]
+        lr = math.sqrt(d1) / math.sqrt(d2)
+        # NesterovOptimizer.__init__: the gradient again (same point, same bits), then the optimiser's own probe
+        self.eval(v, g)
+        with torch.cuda.stream(self.stream):
+            self.U[0].copy_(v)
+        d1 = self.probe(v, g, lr, probe)
+        d2 = self.eval(probe, g2, g_ref=g)[0]
+        alpha = math.sqrt(d1) / math.sqrt(d2)
+        evals += 4
+        # the wirelength-only start
+        Th = np.zeros(T_SIZE)
+        Th[TI["alpha"]], Th[TI["a"]] = alpha, 1.0
+        Th[TI["start_tol"]], Th[TI["inner"]] = o.start_tol, o.inner_iter
+        with torch.cuda.stream(self.stream):
+            self.T.copy_(torch.as_tensor(Th))
+            self.kp.copy_(torch.tensor([gam, 0, 0, alpha, 0.0], dtype=torch.float32))
+        while True:
+            self._replay(native.PHASE_START)
+            self.sync()
+            Th = self.T.cpu().numpy()
+            if Th[TI["done"]] or Th[TI["stop"]]:
+                break
+        evals += int(Th[TI["evals"]])
+        start_iters = int(Th[TI["loop_it"]])
+        if Th[TI["stop"]]:
+            reason = REASON[int(Th[TI["stop"]])]
+            cur = int(self.cur.cpu())
+            return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
+                        overflow=float("nan"), evals=evals, seconds=time.time() - t0, pos=self.V[cur])
+        cur = int(self.cur.cpu())
+        # first density weight: density_weight x tension unit (Objective.tension_unit)
+        out = self.eval(self.V[cur], self.tmp[0], weight=1.0, precond=-1.0, with_wl=False)
+        lam = o.density_weight * float(p.pins.astype(np.float64).sum()) / float(out[4])
+        if log:
+            log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
+                % (start_iters, Th[TI["hpwl"]], lam))
+        S = np.zeros(len(S_FIELDS))
+        S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, gam, Th[TI["alpha"]], Th[TI["a"]]
+        S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = Th[TI["iter"]], Th[TI["hpwl"]], 1.0
+        S[SK["best_hpwl"]] = S[SK["best_ovf"]] = math.inf
+        S[SK["loop_it"]] = start_iters
+        a = Th[TI["a"]]
+        coef = (a - 1) / ((1 + math.sqrt(4 * a * a + 1)) / 2)
+        with torch.cuda.stream(self.stream):
+            self.S.copy_(torch.as_tensor(S))
+            self.kp.copy_(torch.tensor([gam, lam, lam, Th[TI["alpha"]], coef], dtype=torch.float32))
+            self.best.copy_(self.V[cur])
+        logged = start_iters // o.log_freq
+        while True:
+            self._replay(native.PHASE_DENSITY)
+            self.sync()
+            Sh = self.S.cpu().numpy()
+            it = int(Sh[SK["loop_it"]])
+            if log and it // o.log_freq > logged:
+                logged = it // o.log_freq
+                log("iter: %d | hpwl: %.4E overflow: %.4f density_weight: %.4E wa_coeff: %.4E"
+                    % (it, Sh[SK["res_hpwl"]], Sh[SK["res_ovf"]], Sh[SK["lam"]], Sh[SK["gam"]]))
+            if Sh[SK["stop"]]:
+                break
+        native.call("gp103_finish", self._ref, self.stream.cuda_stream)
+        self.sync()
+        Sh = self.S.cpu().numpy()
+        cur = int(self.cur.cpu())
+        pos = self.best if Sh[SK["has_best"]] else self.V[cur]
+        return dict(reason=REASON[int(Sh[SK["stop"]])], iters=int(Sh[SK["loop_it"]]), start_iters=start_iters,
+                    hpwl=float(Sh[SK["res_hpwl"]]), overflow=float(Sh[SK["res_ovf"]]),
+                    evals=evals + int(Sh[SK["evals"]]), seconds=time.time() - t0, pos=pos,
+                    density_iters=int(Sh[SK["loop_it"]]) - start_iters, lam=float(Sh[SK["lam"]]),
+                    gam=float(Sh[SK["gam"]]))

@@ -1,0 +1,96 @@
+"""ctypes binding of libgp103.so (include/gp103.h). No fallback: if the library is missing or fails to load, every
+entry point raises. Streams are passed as raw cudaStream_t handles (torch.cuda.Stream.cuda_stream)."""
+import ctypes
+import os
+
+from . import build as _build
+
+_LIB = None
+
+OK, ERR_ARG, ERR_CUDA, ERR_SHAPE = 0, 1, 2, 3
+FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6 = 0, 1, 2
+FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6}
+PHASE_START, PHASE_DENSITY = 0, 1
+T = dict(alpha=0, a=1, iter=2, loop_it=3, done=4, stop=5, accept=6, hpwl=7, wa=8, evals=9, nwa=10, start_tol=11,
+         inner=12, ring=16)
+T_SIZE = 32
+
+_vp, _i, _f, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
+
+
+class Plan(ctypes.Structure):
+    """gp103_plan, field for field."""
+    _fields_ = [
+        ("num_nodes", _i), ("num_mov", _i), ("num_nets", _i), ("num_pins", _i),
+        ("nbx", _i), ("nby", _i), ("jnbx", _i), ("jnby", _i), ("field_mode", _i),
+        ("pin_cell", _vp), ("pin_off", _vp), ("net_start", _vp), ("cell_start", _vp), ("cell_pin", _vp),
+        ("size", _vp), ("ratio", _vp), ("pins", _vp), ("area", _vp), ("lo", _vp), ("hi", _vp),
+        ("bx", _f), ("by", _f), ("target", _f),
+        ("fixed", _vp),
+        ("ovf_scale", _d),
+        ("jsize", _vp), ("jratio", _vp), ("jfixed", _vp), ("jbx", _f), ("jby", _f), ("jovf_scale", _d),
+        ("field_const", _vp), ("field_work", _vp), ("ex", _vp), ("ey", _vp),
+        ("u", _vp * 2), ("v", _vp * 2), ("g", _vp * 2), ("best", _vp), ("cur", _vp),
+        ("S", _vp), ("T", _vp), ("kp", _vp), ("c", _vp),
+        ("pin_grad", _vp), ("map", _vp), ("jmap", _vp), ("red", _vp), ("counters", _vp),
+    ]
+
+
+class Sizes(ctypes.Structure):
+    _fields_ = [("field_const", ctypes.c_size_t), ("field_work", ctypes.c_size_t), ("red", ctypes.c_size_t)]
+
+
+_SIGS = {
+    "gp103_version": ([], _i),
+    "gp103_status_string": ([_i], ctypes.c_char_p),
+    "gp103_wa": ([_vp] * 6 + [_i, _i] + [_vp] * 4 + [_vp], _i),
+    "gp103_density_map": ([_vp, _vp, _vp, _i, _i, _f, _f, _i, _i, _vp, _vp, _f, _vp, _vp, _vp], _i),
+    "gp103_nesterov_step": ([_vp] * 7 + [_i, _vp, _vp, _vp], _i),
+    "gp103_density_grad": ([_vp] * 7 + [_i, _i, _vp, _vp, _f, _f, _i, _i, _vp, _vp], _i),
+    "gp103_control": ([_vp] * 8 + [_vp], _i),
+    "gp103_select": ([_vp] * 8 + [_i, _vp], _i),
+    "gp103_plan_offsets": ([ctypes.POINTER(ctypes.c_size_t), _i], _i),
+    "gp103_plan_sizes": ([_i, _i, _i, ctypes.POINTER(Sizes)], _i),
+    "gp103_field_constants": ([ctypes.POINTER(Plan), _vp], _i),
+    "gp103_pass": ([ctypes.POINTER(Plan), _i, _vp], _i),
+    "gp103_eval": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _d, _d, _i, _vp, _vp], _i),
+    "gp103_probe": ([ctypes.POINTER(Plan), _vp, _vp, _d, _vp, _vp, _vp], _i),
+    "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
+    "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
+}
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load libgp103.so (building it first if it is missing or older than its sources)."""
+    global _LIB
+    if _LIB is None:
+        if not _build.up_to_date():
+            _build.build()
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError("libgp103.so is not built (python -m autoplace_gb300.build)")
+        L = ctypes.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def check(status, what):
+    if status != OK:
+        msg = lib().gp103_status_string(status).decode()
+        raise RuntimeError("%s failed: %s (status %d)" % (what, msg, status))
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args), name)
+
+
+def exported_symbols():
+    return list(_SIGS)

@@ -1,0 +1,179 @@
+/* gp103: GB300-native (sm_103a) electrostatic global-placement iteration behind a C ABI.
+ *
+ * Drop-in boundary for AutoPlace's `gp_cuda` operator module. Every entry point takes raw device pointers, sizes
+ * and a CUDA stream, launches on that stream only (never the legacy default stream), allocates nothing, and returns
+ * a status: 0 = ok, > 0 = GP103_ERR_* (bad argument, or the CUDA error of a launch). Float arrays of shape [n, 2]
+ * are row-major (x, y) pairs, as in the reference. Device scalars (gamma, weights, step sizes) are read inside the
+ * kernels: no host synchronisation.
+ *
+ * Part 1 mirrors the six host launchers of the reference (cpp_to_py/gp_cuda_kernel.cu) that its pybind11 module
+ * (cpp_to_py/gp_cuda.cpp:78-85) exposes to Python; part 2 is the fused iteration this library runs itself.
+ */
+#ifndef GP103_H
+#define GP103_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GP103_OK = 0,
+    GP103_ERR_ARG = 1,       /* a size or pointer the kernels cannot take */
+    GP103_ERR_CUDA = 2,      /* a launch failed (cudaGetLastError) */
+    GP103_ERR_SHAPE = 3      /* a grid the tensor-core field does not support */
+};
+
+/* Library version and the status text of an error code. */
+int gp103_version(void);
+const char* gp103_status_string(int status);
+
+/* ------------------------------------------------------------------------------------------------ part 1
+ * gp_cuda.wa (cpp_to_py/gp_cuda.cpp:31-38; launcher wa_wirelength, gp_cuda_kernel.cu:59-65).
+ * Weighted-average wirelength of the nets [0, num_nets) grouped by net_start, gamma read from device memory.
+ * pin_grad [P, 2] is scratch (P = net_start[num_nets]); out [num_nets, 2] = per-net (WA, HPWL); grad [num_mov, 2] =
+ * per-cell sum of its pins' gradients in cell_pin order (cell_start [num_mov + 1]). A pin whose cell is >= num_mov
+ * is fixed: its offset is its position. */
+int gp103_wa(const float* pos, const int* pin_cell, const float* pin_off, const int* net_start, const int* cell_start,
+             const int* cell_pin, int num_nets, int num_mov, const float* gamma, float* pin_grad, float* out,
+             float* grad, cudaStream_t stream);
+
+/* gp_cuda.density_map (gp_cuda.cpp:41-48; launcher density_map, gp_cuda_kernel.cu:141-146).
+ * Fixed-point (2^32 per bin area) charge of nodes [0, num_nodes) into map [2, nbx, nby] (map 0: nodes < num_mov,
+ * map 1: the rest; zeroed here first, it is scratch), then rho [2 nbx, 2 nby] = total density mirrored in both
+ * axes and over [nbx, nby] = max(movable + fixed - target, 0). The map is the reference's integer map, bit for bit. */
+int gp103_density_map(const float* pos, const float* size, const float* ratio, int num_nodes, int num_mov, float bx,
+                      float by, int nbx, int nby, unsigned long long* map, const float* fixed, float target,
+                      float* rho, float* over, cudaStream_t stream);
+
+/* gp_cuda.nesterov_step (gp_cuda.cpp:51-56; launcher nesterov_step, gp_cuda_kernel.cu:167-170).
+ * n floats: u_next = v - alpha g; v_next = clamp(u_next + coef (u_next - u), lo, hi); alpha, coef on the device. */
+int gp103_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,
+                        const float* alpha, const float* coef, int n, float* u_next, float* v_next,
+                        cudaStream_t stream);
+
+/* gp_cuda.density_grad (gp_cuda.cpp:59-65; launcher density_grad, gp_cuda_kernel.cu:148-153).
+ * grad[i] = (wl_grad[i] (i < num_wl) + weight * -(charge x field)) / max(1, pins[i] + precond area[i]) (precond < 0:
+ * no division). field = two planes (x, y) of the mirrored map, each [2 nbx, 2 nby]; weight, precond on the device. */
+int gp103_density_grad(const float* pos, const float* size, const float* ratio, const float* field,
+                       const float* wl_grad, const float* pins, const float* area, int num_nodes, int num_wl,
+                       const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,
+                       cudaStream_t stream);
+
+/* gp_cuda.control (gp_cuda.cpp:69-71; launcher control, gp_cuda_kernel.cu:251-254).
+ * One pass of the run's control in float64: S [21] (layout FIELDS of src/gpu_loop.py:19-22) and kp [5] (gamma,
+ * density weight, density weight of the preconditioner, alpha, coef) updated in place; c [13] constants (order of
+ * src/gpu_loop.py:50-53); moved / turned / hpwl / ovf / wa are float32 device scalars of the pass. */
+int gp103_control(double* S, float* kp, const double* c, const float* moved, const float* turned, const float* hpwl,
+                  const float* ovf, const float* wa, cudaStream_t stream);
+
+/* gp_cuda.select (gp_cuda.cpp:74-76; launcher select_step, gp_cuda_kernel.cu:256-259).
+ * n floats: if S[accept]: u, v, g <- next; if S[is_best]: best <- v_next. */
+int gp103_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
+                 const float* g_next, float* best, int n, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------------------------------ part 2
+ * The fused iteration. The caller owns all memory: it fills a gp103_plan with device pointers (sizes from
+ * gp103_plan_sizes) and captures gp103_pass calls in a CUDA graph if it wants one. */
+
+/* Field precision of the Poisson solve. */
+enum {
+    GP103_FIELD_FP32 = 0,     /* cosine / sine transforms as float32 CUDA-core GEMMs (any grid) */
+    GP103_FIELD_BF16X3 = 1,   /* tensor cores (tcgen05), bf16 operands split in 2 terms, 3 products, fp32 accumulation */
+    GP103_FIELD_BF16X6 = 2    /* tensor cores, bf16 operands split in 3 terms, 6 products (error ~1e-7 of the max) */
+};
+
+/* Phases of gp103_pass. */
+enum {
+    GP103_PHASE_START = 0,    /* wirelength-only start (density weight 0), src/run_placement.py:60-65 */
+    GP103_PHASE_DENSITY = 1   /* the device loop of src/gpu_loop.py:58-68 */
+};
+
+/* Layout of the start-phase state T [32] (float64): what NesterovOptimizer (alpha, a) and
+ * ParamScheduler.start_step (src/param_scheduler.py:42-48) keep during the wirelength-only start. */
+enum {
+    GP103_T_ALPHA = 0, GP103_T_A = 1, GP103_T_ITER = 2, GP103_T_LOOP_IT = 3, GP103_T_DONE = 4, GP103_T_STOP = 5,
+    GP103_T_ACCEPT = 6, GP103_T_HPWL = 7, GP103_T_WA = 8, GP103_T_EVALS = 9, GP103_T_NWA = 10,
+    GP103_T_START_TOL = 11, GP103_T_INNER = 12, GP103_T_RING = 16 /* 6 slots: the last WA values */,
+    GP103_T_SIZE = 32
+};
+
+typedef struct {
+    /* sizes */
+    int num_nodes, num_mov, num_nets, num_pins;
+    int nbx, nby;             /* force grid */
+    int jnbx, jnby;           /* overflow grid; 0 = the force grid measures the overflow */
+    int field_mode;           /* GP103_FIELD_* */
+    /* netlist, grouped by net (nets in any order) and by cell (cell_pin = positions in the pin arrays) */
+    const int* pin_cell; const float* pin_off; const int* net_start; const int* cell_start; const int* cell_pin;
+    /* nodes */
+    const float* size; const float* ratio; const float* pins; const float* area; const float* lo; const float* hi;
+    float bx, by, target;
+    const float* fixed;       /* [nbx, nby] */
+    double ovf_scale;         /* bin area / movable area of the overflow grid */
+    /* overflow grid (when jnbx > 0): smoothed sizes of the cells on it */
+    const float* jsize; const float* jratio; const float* jfixed; float jbx, jby; double jovf_scale;
+    /* field constants (gp103_field_constants fills them) and the field planes */
+    void* field_const;        /* gp103_plan_sizes(...).field_const bytes */
+    void* field_work;         /* gp103_plan_sizes(...).field_work bytes */
+    float* ex; float* ey;     /* [nbx, nby] */
+    /* optimiser state: ping-pong buffers, *cur = the current one; best placement */
+    float* u[2]; float* v[2]; float* g[2]; float* best; int* cur;
+    double* S;                /* [21] density phase (layout of the reference) */
+    double* T;                /* [GP103_T_SIZE] start phase */
+    float* kp;                /* [5] */
+    const double* c;          /* [13] constants of the density phase */
+    /* scratch */
+    float* pin_grad;          /* [num_pins, 2] */
+    unsigned long long* map;  /* [2, nbx, nby], zero between passes */
+    unsigned long long* jmap; /* [jnbx, jnby], zero between passes */
+    double* red;              /* gp103_plan_sizes(...).red doubles */
+    unsigned int* counters;   /* 16, zero */
+} gp103_plan;
+
+typedef struct {
+    size_t field_const;       /* bytes */
+    size_t field_work;        /* bytes */
+    size_t red;               /* doubles */
+} gp103_sizes;
+
+/* Byte offsets of gp103_plan's fields in declaration order (arrays count once), for bindings that lay the struct
+ * out themselves; returns the number of fields, writes at most n offsets and then sizeof(gp103_plan) if room. */
+int gp103_plan_offsets(size_t* out, int n);
+
+/* Sizes of the plan's buffers for a force grid nbx x nby and a field mode; GP103_ERR_SHAPE if the mode does not
+ * support the grid (tensor-core modes: nbx and nby multiples of 128). */
+int gp103_plan_sizes(int nbx, int nby, int field_mode, gp103_sizes* out);
+
+/* Fill plan->field_const (cosine / sine matrices, in the operand layout of the mode). Once per grid. */
+int gp103_field_constants(const gp103_plan* plan, cudaStream_t stream);
+
+/* One iteration of the phase (all kernels, on `stream`). The scalar results of the pass stay on the device; the
+ * reductions behind them are float64 and bit-reproducible. */
+int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream);
+
+/* The gradient of the objective at pos ([num_nodes, 2]) into g_out, with the density weight `weight` (0: the
+ * wirelength-only gradient, the density map and field are not computed) and preconditioner weight `precond`
+ * (< 0: none), both host values; -1 for wl_scale skips the wirelength term (the plain density gradient of
+ * tension_unit). Writes out3 = (sum of squares of g_out - g_ref or 0 if g_ref is NULL, WA, HPWL, overflow,
+ * L1 norm of g_out over the cells) as 5 doubles. gamma is read from plan->kp[0]. */
+int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out, const float* g_ref, double weight,
+               double precond, int with_wl, double* out5, cudaStream_t stream);
+
+/* probe = clamp(v - step * g, lo, hi) for the whole node set; out[0] = sum of squares of probe - v. */
+int gp103_probe(const gp103_plan* plan, const float* v, const float* g, double step, float* probe, double* out1,
+                cudaStream_t stream);
+
+/* The field of a plain density map a [nbx, nby] (float32) into ex, ey [nbx, nby] with the plan's field mode. */
+int gp103_field(const gp103_plan* plan, const float* density, float* ex, float* ey, cudaStream_t stream);
+
+/* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
+int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

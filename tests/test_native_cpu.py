@@ -1,0 +1,75 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports what include/gp103.h declares, the
+ctypes plan matches the C struct, and the host logic of the engine (net reordering) is exact."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from autoplace_gb300 import native, problem, synth
+from autoplace_gb300.engine import degree_order
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "gp103.h")).read()
+    return sorted(set(re.findall(r"\b(gp103_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = native.lib()
+    declared = header_functions()
+    assert declared, "no function declared"
+    for name in declared:
+        assert hasattr(L, name), name
+    assert set(declared) == set(native.exported_symbols())
+    assert L.gp103_version() >= 1
+    assert L.gp103_status_string(1).decode().startswith("invalid argument")
+
+
+def test_plan_layout_matches_c_struct():
+    n = len(native.Plan._fields_)
+    out = (ctypes.c_size_t * (n + 1))()
+    count = native.lib().gp103_plan_offsets(out, n + 1)
+    assert count == n
+    for k, (name, _) in enumerate(native.Plan._fields_):
+        assert getattr(native.Plan, name).offset == out[k], name
+    assert ctypes.sizeof(native.Plan) == out[n]
+
+
+def test_plan_sizes_and_shape_errors():
+    s = native.Sizes()
+    native.call("gp103_plan_sizes", 256, 256, native.FIELD_BF16X6, ctypes.byref(s))
+    assert s.field_const > 6 * 256 * 256 * 6 and s.field_work > 0 and s.red > 0
+    assert native.lib().gp103_plan_sizes(96, 96, native.FIELD_BF16X6, ctypes.byref(s)) == native.ERR_SHAPE
+    native.call("gp103_plan_sizes", 96, 96, native.FIELD_FP32, ctypes.byref(s))
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        native.call("gp103_plan_sizes", 0, 96, native.FIELD_FP32, ctypes.byref(s))
+
+
+def test_argument_errors_without_gpu():
+    """Bad sizes are rejected before any launch (no GPU needed)."""
+    L = native.lib()
+    assert L.gp103_wa(None, None, None, None, None, None, -1, 0, None, None, None, None, None) == native.ERR_ARG
+    assert L.gp103_density_map(None, None, None, 0, 0, 1.0, 1.0, 0, 4, None, None, 1.0, None, None,
+                               None) == native.ERR_ARG
+    assert L.gp103_select(None, None, None, None, None, None, None, None, 0, None) == native.ERR_ARG
+
+
+def test_degree_order_keeps_nets_and_cell_sums():
+    nl = synth.make_netlist(3000, 3100, window=60, macros=3, cover=0.1, fixed_pin_share=0.05, seed=4)
+    cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
+    perm, ns, cp = degree_order(cs.net_start, cs.cell_pin)
+    deg = np.diff(ns)
+    assert np.all(np.diff(deg) >= 0)                       # nets by degree
+    assert sorted(perm.tolist()) == list(range(len(perm)))  # a permutation of the pins
+    # every net keeps its pins, in order
+    old = np.diff(cs.net_start)
+    order = np.argsort(old, kind="stable")
+    for k in range(0, len(order), 97):
+        i = order[k]
+        assert np.array_equal(perm[ns[k]:ns[k + 1]], np.arange(cs.net_start[i], cs.net_start[i + 1]))
+    # a cell sums the same pins in the same order
+    assert np.array_equal(perm[cp], cs.cell_pin)
