@@ -18,6 +18,49 @@ using namespace gp103;
         if (st_) return st_;             \
     } while (0)
 
+// ------------------------------------------------------------------------------------------------ launch accounting
+static unsigned long long g_launches = 0;
+static struct {
+    cudaEvent_t ev[GP103_PROFILE_MAX + 1];
+    const char* name[GP103_PROFILE_MAX + 1];
+    int n, open;
+} g_prof;
+
+int gp103::after_launch(cudaStream_t s, const char* name) {
+    if (cudaGetLastError() != cudaSuccess) return GP103_ERR_CUDA;
+    __atomic_add_fetch(&g_launches, 1ull, __ATOMIC_RELAXED);
+    if (g_prof.open && g_prof.n <= GP103_PROFILE_MAX) {
+        if (cudaEventRecord(g_prof.ev[g_prof.n], s) != cudaSuccess) return GP103_ERR_CUDA;
+        g_prof.name[g_prof.n++] = name;
+    }
+    return GP103_OK;
+}
+
+extern "C" unsigned long long gp103_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+extern "C" int gp103_profile_begin(cudaStream_t s) {
+    REQUIRE(!g_prof.open);
+    for (int i = 0; i <= GP103_PROFILE_MAX; i++)
+        if (!g_prof.ev[i] && cudaEventCreate(&g_prof.ev[i]) != cudaSuccess) return GP103_ERR_CUDA;
+    if (cudaEventRecord(g_prof.ev[0], s) != cudaSuccess) return GP103_ERR_CUDA;
+    g_prof.name[0] = "begin";
+    g_prof.n = 1;
+    g_prof.open = 1;
+    return GP103_OK;
+}
+
+extern "C" int gp103_profile_end(float* ms, const char** names, int max) {
+    REQUIRE(g_prof.open);
+    g_prof.open = 0;
+    if (cudaEventSynchronize(g_prof.ev[g_prof.n - 1]) != cudaSuccess) return -GP103_ERR_CUDA;
+    int k = 0;
+    for (int i = 1; i < g_prof.n && k < max; i++, k++) {
+        if (cudaEventElapsedTime(&ms[k], g_prof.ev[i - 1], g_prof.ev[i]) != cudaSuccess) return -GP103_ERR_CUDA;
+        names[k] = g_prof.name[i];
+    }
+    return k;
+}
+
 extern "C" int gp103_version(void) { return 1; }
 
 extern "C" const char* gp103_status_string(int status) {
@@ -35,8 +78,9 @@ extern "C" int gp103_wa(const float* pos, const int* pin_cell, const float* pin_
                         const int* cell_start, const int* cell_pin, int num_nets, int num_mov, const float* gamma,
                         float* pin_grad, float* out, float* grad, cudaStream_t stream) {
     REQUIRE(num_nets >= 0 && num_mov >= 0 && net_start && gamma && cell_start);
-    REQUIRE(num_nets == 0 || (pin_cell && pin_off && pin_grad && out && pos));
-    REQUIRE(num_mov == 0 || (grad && cell_pin));
+    // an optimised net has >= 2 pins: no nets <=> no pins (the pin arrays may then be empty / null)
+    REQUIRE(num_nets == 0 || (pin_cell && pin_off && pin_grad && out && pos && cell_pin));
+    REQUIRE(num_mov == 0 || grad);
     if (num_nets > 0) {
         WaJob j = {};
         j.pos_a = j.pos_b = (const float2*)pos;

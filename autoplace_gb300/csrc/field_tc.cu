@@ -1,7 +1,7 @@
 // Tensor-core form of the field's six GEMMs (GB300, sm_103a): tcgen05.mma (kind::f16, bf16 operands, float32
 // accumulation in tensor memory), operands staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) through an
 // mbarrier pipeline, one elected thread issuing the MMAs, four warps reading the accumulator back (tcgen05.ld) into
-// fused epilogues. Operands are float32 values split into bf16 terms, a = a0 + a1 + a2 (each term the bf16 rounding
+// fused epilogues, with the accumulation promoted to float32 registers after every k-block (below). Operands are float32 values split into bf16 terms, a = a0 + a1 + a2 (each term the bf16 rounding
 // of what the previous ones leave), stored as three planes; a product is a list of (A term, B term) pairs over the
 // same K, concatenated along K into one accumulation:
 //   bf16x3: (0,0) (0,1) (1,0)                          ~1e-5 of the max
@@ -131,13 +131,23 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16&
 }
 
 // ----------------------------------------------------------------------------- the GEMM kernel
-__global__ void __launch_bounds__(128, 1)
+// Warp roles (192 threads): warp 0 = TMA producer (and tensor-memory owner), warp 1 = MMA issuer, warps 2..5 =
+// accumulator readers / epilogue (warp w reads tensor-memory lanes 32 (w % 4) .. + 31, i.e. output rows).
+// The tensor cores accumulate in float32 with truncation, so a long accumulation drifts (about 2e-6 of the max
+// after four chained GEMMs of K = 256). Each k-block (64 of K) therefore goes into a fresh tensor-memory
+// accumulator (two, alternating) and the readers add it into float32 registers with round-to-nearest; the error
+// then stays at float32 level (~2e-7) at every grid size.
+constexpr int TC_THREADS = 192;
+constexpr int TC_TMEM_COLS = 2 * TC_BN;
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
                    const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1, TcArgs args) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);     // full[S], empty[S], done
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 1);
+    // barriers: full[S], empty[S], acc_full[2], acc_empty[2]
+    uint64_t* bars = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int z = blockIdx.z;
     const TcProblem& P = args.p[z];
@@ -146,77 +156,101 @@ __global__ void __launch_bounds__(128, 1)
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
     const int kblocks = P.K / TC_BK, total = kblocks * args.nseg;
     int* err = args.err;
+    auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
+    auto empty_bar = [&](int s) { return smem_u32(&bars[TC_STAGES + s]); };
+    auto accf_bar = [&](int b) { return smem_u32(&bars[2 * TC_STAGES + b]); };
+    auto acce_bar = [&](int b) { return smem_u32(&bars[2 * TC_STAGES + 2 + b]); };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
-            mbar_init(smem_u32(&bars[s]), 1);
-            mbar_init(smem_u32(&bars[TC_STAGES + s]), 1);
+            mbar_init(full_bar(s), 1);
+            mbar_init(empty_bar(s), 1);
         }
-        mbar_init(smem_u32(&bars[2 * TC_STAGES]), 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(accf_bar(b), 1);
+            mbar_init(acce_bar(b), 4);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(TC_BN));
+                     "r"(TC_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t done_bar = smem_u32(&bars[2 * TC_STAGES]);
 
-    if (warp == 0 && lane == 0) {                                // TMA producer
-        for (int it = 0; it < total; it++) {
-            const int s = it % TC_STAGES;
-            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-            if (!mbar_wait(smem_u32(&bars[TC_STAGES + s]), ph ^ 1u, err, 1)) break;
-            const int seg = it / kblocks, kb = it % kblocks;
-            const uint32_t full = smem_u32(&bars[s]);
-            mbar_expect_tx(full, TC_STAGE_BYTES);
-            uint8_t* st = smem + s * TC_STAGE_BYTES;
-            tma_load_3d(smem_u32(st), ma, full, kb * TC_BK, m0, args.seg_a[seg]);
-            tma_load_3d(smem_u32(st + TC_TILE_BYTES), mb, full, kb * TC_BK, n0, args.seg_b[seg]);
+    if (warp == 0) {
+        if (lane == 0) {                                         // TMA producer
+            for (int it = 0; it < total; it++) {
+                const int s = it % TC_STAGES;
+                const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+                if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1)) break;
+                const int seg = it / kblocks, kb = it % kblocks;
+                mbar_expect_tx(full_bar(s), TC_STAGE_BYTES);
+                uint8_t* st = smem + s * TC_STAGE_BYTES;
+                tma_load_3d(smem_u32(st), ma, full_bar(s), kb * TC_BK, m0, args.seg_a[seg]);
+                tma_load_3d(smem_u32(st + TC_TILE_BYTES), mb, full_bar(s), kb * TC_BK, n0, args.seg_b[seg]);
+            }
         }
-    } else if (warp == 1 && lane == 0) {                         // MMA issuer
+    } else if (warp == 1) {
+        if (lane == 0) {                                         // MMA issuer: one k-block per accumulator
+            for (int it = 0; it < total; it++) {
+                const int s = it % TC_STAGES, b = it & 1;
+                const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u, use = (uint32_t)(it >> 1) & 1u;
+                if (!mbar_wait(acce_bar(b), use ^ 1u, err, 2)) break;
+                if (!mbar_wait(full_bar(s), ph, err, 3)) break;
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_TILE_BYTES;
+                const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / 16; kk++)
+                    mma_bf16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), kk > 0 ? 1u : 0u);
+                mma_commit(empty_bar(s));
+                mma_commit(accf_bar(b));
+            }
+        }
+    } else {                                                     // readers + epilogue
+        const int q = warp & 3;                                  // tensor-memory lane quarter
+        const int row = m0 + q * 32 + lane;
+        float r[TC_BN];
+#pragma unroll
+        for (int i = 0; i < TC_BN; i++) r[i] = 0.f;
         bool ok = true;
         for (int it = 0; it < total && ok; it++) {
-            const int s = it % TC_STAGES;
-            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-            if (!mbar_wait(smem_u32(&bars[s]), ph, err, 2)) { ok = false; break; }
+            const int b = it & 1;
+            if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_TILE_BYTES;
+            const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN);
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; kk++)
-                mma_bf16(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (it > 0 || kk > 0) ? 1u : 0u);
-            mma_commit(smem_u32(&bars[TC_STAGES + s]));
+            for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(base + (uint32_t)c0, v);
+#pragma unroll
+                for (int i = 0; i < 32; i++) r[c0 + i] = __fadd_rn(r[c0 + i], v[i]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce_bar(b)) : "memory");
         }
-        mma_commit(done_bar);                                    // completes once every MMA above has
-    }
-    __syncwarp();
-
-    // epilogue: warp w owns accumulator rows 32 w .. 32 w + 31 (tensor-memory lanes)
-    const bool have = mbar_wait(done_bar, 0, err, 3) && *(volatile int*)err == 0;
-    tc_fence_after();
-    if (have) {
-        const int row = m0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            const int col = n0 + c0;
+        ok = ok && *(volatile int*)err == 0;
+        if (ok) {
+            const int col = n0;
             if (P.epi == EPI_PLAIN) {
                 float4* o = (float4*)(P.out_f32 + (size_t)row * P.N + col);
 #pragma unroll
-                for (int i = 0; i < 8; i++) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+                for (int i = 0; i < TC_BN / 4; i++) o[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
             } else if (P.epi == EPI_TRANS) {
                 const size_t plane = (size_t)P.M * P.N;
 #pragma unroll
-                for (int i = 0; i < 32; i++) {
-                    __nv_bfloat16 a, b, c;
-                    split3(v[i], a, b, c);
+                for (int i = 0; i < TC_BN; i++) {
+                    __nv_bfloat16 a, bb, c;
+                    split3(r[i], a, bb, c);
                     const size_t at = (size_t)(col + i) * P.M + row;
                     P.o_terms[at] = a;
-                    P.o_terms[plane + at] = b;
+                    P.o_terms[plane + at] = bb;
                     P.o_terms[2 * plane + at] = c;
                 }
             } else {
@@ -226,14 +260,17 @@ __global__ void __launch_bounds__(128, 1)
                 for (int h = 0; h < 2; h++) {
                     const float* w = (h ? P.w1 : P.w0) + base;
                     __nv_bfloat16* o = (h ? P.o2_terms : P.o_terms) + base;
-                    __align__(16) __nv_bfloat16 ta[32], tb[32], tcv[32];
 #pragma unroll
-                    for (int i = 0; i < 32; i++) split3(v[i] * __ldg(w + i), ta[i], tb[i], tcv[i]);
+                    for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+                        __align__(16) __nv_bfloat16 ta[32], tb[32], tcv[32];
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        ((uint4*)o)[i] = ((uint4*)ta)[i];
-                        ((uint4*)(o + plane))[i] = ((uint4*)tb)[i];
-                        ((uint4*)(o + 2 * plane))[i] = ((uint4*)tcv)[i];
+                        for (int i = 0; i < 32; i++) split3(r[c0 + i] * __ldg(w + c0 + i), ta[i], tb[i], tcv[i]);
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            ((uint4*)(o + c0))[i] = ((uint4*)ta)[i];
+                            ((uint4*)(o + plane + c0))[i] = ((uint4*)tb)[i];
+                            ((uint4*)(o + 2 * plane + c0))[i] = ((uint4*)tcv)[i];
+                        }
                     }
                 }
             }
@@ -243,7 +280,7 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
     }
 }
 
@@ -310,7 +347,7 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     args.err = err;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / TC_BN, p.M / TC_BM, nops);
-    tc_gemm_kernel<<<grid, 128, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
+    tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -5,13 +5,17 @@
 
 #include "../../include/gp103.h"
 
+// After every kernel launch (stream `s` in scope): the launch status, the library's launch count and, while a
+// profile is open, an event on the stream named after the launching function.
 #define GP103_CHECK_LAUNCH()                                   \
     do {                                                       \
-        cudaError_t e_ = cudaGetLastError();                   \
-        if (e_ != cudaSuccess) return GP103_ERR_CUDA;          \
+        int e_ = gp103::after_launch(s, __func__);             \
+        if (e_) return e_;                                     \
     } while (0)
 
 namespace gp103 {
+
+int after_launch(cudaStream_t s, const char* name);
 
 constexpr double DENSITY_SCALE = 4294967296.0;     // fixed point of the density map: 2^32 per bin area
 constexpr int SMS = 152;                           // GB300: 2 dies x 76 SMs

@@ -50,6 +50,7 @@ class Placer(object):
         self.use_graphs = use_graphs
         self.stream = stream or torch.cuda.Stream(self.dev)
         self._graphs = {}
+        self._captured = self._replayed = 0
         self._keep = []
         dev = self.dev
         t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev))
@@ -155,11 +156,20 @@ class Placer(object):
         g = self._graphs.get(phase)
         if g is None:
             g = torch.cuda.CUDAGraph()
+            before = native.launch_count()
             with torch.cuda.graph(g, stream=self.stream):
                 self._passes(phase, self.check_every)
-            self._graphs[phase] = g
+            per = native.launch_count() - before
+            self._captured += per
+            self._graphs[phase] = (g, per)
+        g, per = self._graphs[phase]
         with torch.cuda.stream(self.stream):
             g.replay()
+        self._replayed += per
+
+    def launches(self):
+        """Kernels of libgp103 executed so far by this process (graph replays counted launch by launch)."""
+        return native.launch_count() - self._captured + self._replayed
 
     def overflow_scale(self):
         return self.plan.jovf_scale if self.plan.jnbx > 0 else self.plan.ovf_scale

@@ -43,6 +43,9 @@ class Sizes(ctypes.Structure):
 _SIGS = {
     "gp103_version": ([], _i),
     "gp103_status_string": ([_i], ctypes.c_char_p),
+    "gp103_launch_count": ([], ctypes.c_ulonglong),
+    "gp103_profile_begin": ([_vp], _i),
+    "gp103_profile_end": ([ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), _i], _i),
     "gp103_wa": ([_vp] * 6 + [_i, _i] + [_vp] * 4 + [_vp], _i),
     "gp103_density_map": ([_vp, _vp, _vp, _i, _i, _f, _f, _i, _i, _vp, _vp, _f, _vp, _vp, _vp], _i),
     "gp103_nesterov_step": ([_vp] * 7 + [_i, _vp, _vp, _vp], _i),
@@ -94,3 +97,21 @@ def call(name, *args):
 
 def exported_symbols():
     return list(_SIGS)
+
+
+def launch_count():
+    return int(lib().gp103_launch_count())
+
+
+def profile(stream_handle, fn):
+    """Run fn() with the launch profile open: -> [(launcher name, ms)] in launch order."""
+    call("gp103_profile_begin", stream_handle)
+    try:
+        fn()
+    finally:
+        ms = (ctypes.c_float * 512)()
+        names = (ctypes.c_char_p * 512)()
+        k = lib().gp103_profile_end(ms, names, 512)
+    if k < 0:
+        raise RuntimeError("gp103_profile_end failed")
+    return [(names[i].decode(), float(ms[i])) for i in range(k)]

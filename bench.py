@@ -1,0 +1,403 @@
+"""Benchmark: time to overflow 0.07 of one global-placement level of the 1.2M-cell synthetic netlist on a GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2] [--field bf16x6]
+
+Workload (config "c2"): 1,200,000 cells, 1,250,000 nets (5.2M pins, degree mix 2/3/4-10/11-100), 40 macros over 20 %
+of the region, target density 0.8, force grid 1024 x 1024, overflow grid 512 x 512; seeded synthetic data (the
+ISPD suites are not available). One step = one whole level from the seeded start to the stop (wirelength-only start,
+first density weight, density phase until overflow < 0.07 + the settle iterations), inputs resident in HBM. The
+working set (pins, nodes, maps, field planes) is larger than the 129 MB L2, so no flush is needed between steps.
+
+Reported on one JSON line (rank 0): value = seconds per placement (lower is better), e2e = the same through the
+public API from host arrays (upload, run, download of the placement), the roofline of the dominant kernel (CUDA
+events on its stream), a CPU baseline (the oracle's restatement of the reference's CPU iteration timed on a bounded
+sample of iterations of the same netlist, scaled by the iterations the GPU run needed), SM clocks during the timed
+region, and the number of libgp103 kernels launched.
+
+--impl reference: the reference's CPU path restated by the oracle (the reference's own code is Python + torch and
+cannot run on the GPU machine), on the host cores, same metric and config; the iterations to the stop come from the
+GB300 run recorded in profiles/bench_iterations.json.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-overflow 0.07 (s) at 1.2M cells, learned+TC vs plain, HPWL within 1%"
+ITER_FILE = os.path.join(ROOT, "profiles", "bench_iterations.json")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--config", default="c2")
+    p.add_argument("--field", default="bf16x6", choices=["bf16x6", "bf16x3", "fp32"])
+    p.add_argument("--cpu-iters", type=int, default=4, help="density-phase iterations of the CPU sample")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------------------------------------ ranks
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x, world):
+    """Max over ranks of a float (the slowest replica decides the step time)."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x, world):
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------------ clocks
+class Clocks(object):
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.proc, self.path = index, None, None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------ workload
+def workload(cfg, seed):
+    from autoplace_gb300 import problem, synth
+    nl, o = synth.preset(cfg, seed=seed)
+    prob = problem.Problem(nl, problem.options(**o))
+    pos0 = synth.init_positions(nl, prob.num_nodes, seed=seed)
+    return prob, pos0
+
+
+def config_dict(prob, args, world):
+    nl = prob.nl
+    return {"workload": "synthetic %s: %d cells, %d nets, %d pins, %d macros, %d fillers; force grid %d, overflow grid %d"
+                        % (args.config, nl.num_mov, nl.num_nets, nl.num_pins, len(nl.macros),
+                           prob.num_nodes - prob.num_mov, prob.force_bin, prob.num_bin),
+            "cells": nl.num_mov, "nets": nl.num_nets, "pins": nl.num_pins, "nodes": prob.num_nodes,
+            "force_grid": prob.force_bin, "overflow_grid": prob.num_bin, "target_density": prob.target,
+            "field": args.field, "levels": 1, "start": "plain (wirelength-only)",
+            "l2": "working set > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world}
+
+
+# ------------------------------------------------------------------------------------------------ CPU baseline
+def cpu_sample(prob, pos0, iters, gpu_iters):
+    """Time `iters` density-phase iterations of the oracle's CPU iteration (gradient at the density phase: WA,
+    density map, overflow grid, field by FFT of the mirrored map, gather; Nesterov step; control), after one
+    untimed warm-up iteration. -> (seconds per iteration, threads)."""
+    import numpy as np
+    import torch
+    from oracle import gp_oracle as O
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    lvl = O.CpuLevel(prob, dtype=np.float32, field="fft")
+    gr = prob.force
+    v = np.clip(np.asarray(pos0, np.float64), gr.pos_lo, gr.pos_hi)
+    gam, lam = 10 * prob.base_gamma, 1e-4
+    g = lvl.grad(v, lam, gam)[0]
+    u = v.copy()
+    S = np.zeros(len(O.FIELDS))
+    S[O.K["lam"]], S[O.K["gam"]], S[O.K["alpha"]], S[O.K["a"]], S[O.K["mu"]] = lam, gam, 1.0, 1.0, 1.0
+    S[O.K["best_hpwl"]] = S[O.K["best_ovf"]] = math.inf
+    kp = np.array([gam, lam, lam, 1.0, 0.0], np.float32)
+    c = prob.constants()
+    t0 = None
+    for k in range(iters + 1):
+        if k == 1:
+            t0 = time.time()
+        un, vn = O.nesterov_step(u, v, g, gr.pos_lo, gr.pos_hi, kp[3], kp[4])
+        gn, wa, hpwl, ovf = lvl.grad(vn, float(kp[1]), float(kp[0]))
+        O.control(S, kp, c, np.linalg.norm(vn - v), np.linalg.norm(gn - g), hpwl, ovf, wa)
+        u, v, g = un, vn, gn
+    per = (time.time() - t0) / iters
+    return per, threads
+
+
+def cpu_baseline_dict(per, threads, iters, gpu_iters, source):
+    return {"value": per * gpu_iters, "unit": "s", "cores": threads, "kind": "port",
+            "sample": "%d density-phase iterations of the oracle CPU iteration (restating the reference's --gpu -1 "
+                      "path, FFT field) on the full netlist: %.3f s/iter x %d iterations to the stop (%s)"
+                      % (iters, per, gpu_iters, source)}
+
+
+# ------------------------------------------------------------------------------------------------ roofline
+def kernel_bytes(prob):
+    """Algorithmic bytes (or flops) per launch of each kernel, by launcher name."""
+    cs, n, c = prob.csr, prob.num_nodes, prob.num_mov
+    P, N = len(cs.cell32), cs.num_nets
+    nb = prob.force_bin * prob.force_bin
+    jn = prob.num_bin * prob.num_bin if prob.judge is not None else 0
+    return {
+        "launch_wa_net": 20 * P + 8 * c + 4 * N,                       # pins (cell, offset) in, pin gradient out
+        "launch_gather": 44 * n + 12 * P + 4 * c + 8 * nb,             # node data, cell CSR gather, field planes
+        "launch_scatter": 20 * n + 16 * nb,                            # node data in, map out (force grid); judge below
+        "launch_post_plain": 42 * nb,                                   # map in + zeroed, fixed in, bf16 terms out
+        "launch_step": 56 * n,                                          # u, v, g, lo, hi in; u', v' out
+    }
+
+
+def tc_flops(prob, field):
+    nb = prob.force_bin
+    terms = {"bf16x6": 6, "bf16x3": 3}.get(field, 0)
+    return 2.0 * nb ** 3 * terms        # per GEMM
+
+
+def profile_pass(placer):
+    """Per-launch durations of one density pass (eager, CUDA events on the engine's stream), averaged over 8."""
+    from autoplace_gb300 import native
+    rec = native.profile(placer.stream.cuda_stream, lambda: placer._passes(native.PHASE_DENSITY, 8))
+    agg = {}
+    for name, ms in rec:
+        a = agg.setdefault(name, [0, 0.0])
+        a[0] += 1
+        a[1] += ms
+    return {k: {"launches_per_pass": v[0] / 8.0, "ms_per_pass": v[1] / 8.0} for k, v in agg.items()}, rec
+
+
+def roofline(prob, field, prof, peaks):
+    hbm = peaks.get("hbm_gbs")
+    tc = peaks.get("bf16_tflops")
+    by = kernel_bytes(prob)
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms_per_pass"])
+    name, d = dom
+    ms_launch = d["ms_per_pass"] / max(d["launches_per_pass"], 1e-9)
+    table = {}
+    for k, v in prof.items():
+        ml = v["ms_per_pass"] / max(v["launches_per_pass"], 1e-9)
+        row = {"ms_per_pass": round(v["ms_per_pass"], 4), "launches_per_pass": v["launches_per_pass"],
+               "ms_per_launch": round(ml, 4)}
+        if k in by:
+            row["gbs"] = round(by[k] / (ml * 1e-3) / 1e9, 1)
+        if k == "launch_tc":
+            f = tc_flops(prob, field) * (6.0 / v["launches_per_pass"])
+            row["tflops"] = round(f / (ml * 1e-3) / 1e12, 1)
+        table[k] = row
+    if name == "launch_tc":
+        f = tc_flops(prob, field) * (6.0 / d["launches_per_pass"])
+        ach = f / (ms_launch * 1e-3) / 1e12
+        r = {"kernel": "tc_gemm_kernel", "bound": "tensor", "achieved": round(ach, 1), "peak": tc,
+             "unit": "TFLOP/s", "frac": round(ach / tc, 4) if tc else None, "traffic": None,
+             "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops)"}
+    else:
+        b = by.get(name)
+        ach = b / (ms_launch * 1e-3) / 1e9 if b else None
+        r = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1) if ach else None, "peak": hbm, "unit": "GB/s",
+             "frac": round(ach / hbm, 4) if ach and hbm else None, "traffic": None,
+             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+    return r, table
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+# ------------------------------------------------------------------------------------------------ arms
+def run_gb300(args):
+    import numpy as np
+    import torch
+    from autoplace_gb300.engine import Placer
+    rank, world, local = dist_setup()
+    prob, pos0 = workload(args.config, seed=rank)
+    placer = Placer(prob, field=args.field)
+    dpos = torch.tensor(pos0, device="cuda")
+    r = None
+    for _ in range(max(args.warmup, 0)):
+        r = placer.run(dpos)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = placer.launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(placer.stream)
+    t0 = time.time()
+    runs = []
+    for _ in range(args.steps):
+        runs.append(placer.run(dpos))
+    ev1.record(placer.stream)
+    torch.cuda.synchronize()
+    wall = time.time() - t0
+    barrier(world)
+    clk = clocks.stop()
+    launches = placer.launches() - l0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    step_s = reduce_max(ms / 1000.0, world)
+    last = runs[-1]
+    iters = last["iters"]
+    from oracle import gp_oracle as O
+    pos = last["pos"].cpu().numpy()
+    hpwl_exact = O.hpwl_all(pos, prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
+
+    # e2e: from host arrays through the public API (upload, run, download)
+    e2e_s, h2d, d2h = [], 0, 0
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t = time.time()
+        pl2 = Placer(prob, field=args.field, stream=placer.stream)
+        rr = pl2.run(pos0)
+        out = rr["pos"].cpu().numpy()
+        torch.cuda.synchronize()
+        e2e_s.append(time.time() - t)
+        h2d = sum(x.numel() * x.element_size() for x in pl2._keep if x.dtype != torch.uint8) - \
+            sum(x.numel() * x.element_size() for x in (pl2.U + pl2.V + pl2.G + pl2.tmp))
+        d2h = out.nbytes
+        del pl2
+    e2e = reduce_max(statistics.median(e2e_s), world)
+
+    prof, _ = profile_pass(placer)
+    peaks = load_peaks()
+    roof, table = roofline(prob, args.field, prof, peaks)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        per, threads = cpu_sample(prob, pos0, args.cpu_iters, iters)
+        cpu = cpu_baseline_dict(per, threads, args.cpu_iters, iters, "iterations of this GB300 run")
+    if rank == 0:
+        os.makedirs(os.path.dirname(ITER_FILE), exist_ok=True)
+        try:
+            with open(ITER_FILE, "w") as f:
+                json.dump({"config": args.config, "iterations": iters, "start_iters": last["start_iters"],
+                           "reason": last["reason"], "field": args.field}, f)
+        except OSError:
+            pass
+    line = {"metric": METRIC, "value": round(step_s, 4), "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(step_s * 1000, 2), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (field: %s tensor cores; f64 reductions)" % args.field,
+            "data": "synthetic (seeded generator standing in for ISPD 2015/2019)",
+            "config": config_dict(prob, args, world),
+            "result": {"stop": last["reason"], "iterations": iters, "start_iterations": last["start_iters"],
+                       "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "ms_per_iteration":
+                       round(step_s * 1000 / max(iters, 1), 4), "wall_s_per_step": round(wall / args.steps, 4)},
+            "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": roof, "kernels": table, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": int(launches)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference(args):
+    rank, world, _ = dist_setup()
+    if rank != 0:
+        return
+    prob, pos0 = workload(args.config, seed=0)
+    iters, source = None, None
+    try:
+        with open(ITER_FILE) as f:
+            rec = json.load(f)
+        if rec.get("config") == args.config:
+            iters, source = int(rec["iterations"]), "iterations of the GB300 run in profiles/bench_iterations.json"
+    except (OSError, ValueError, KeyError):
+        pass
+    if iters is None:
+        print(json.dumps({"impl": "reference", "unavailable": "no recorded iteration count for %s" % args.config}))
+        return
+    samples = []
+    for _ in range(max(args.warmup, 0)):
+        pass
+    for _ in range(max(args.steps, 1)):
+        per, threads = cpu_sample(prob, pos0, args.cpu_iters, iters)
+        samples.append(per)
+    per = statistics.median(samples)
+    value = per * iters
+    cpu = cpu_baseline_dict(per, threads, args.cpu_iters, iters, source)
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1000, 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (CPU)",
+            "data": "synthetic (seeded generator standing in for ISPD 2015/2019)", "config": config_dict(prob, args, world),
+            "cpu_baseline": cpu, "e2e": {"value": round(value, 3), "unit": "s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

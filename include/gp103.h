@@ -31,6 +31,17 @@ enum {
 int gp103_version(void);
 const char* gp103_status_string(int status);
 
+/* Kernel launches issued through this library so far (a launch captured into a CUDA graph counts once). */
+unsigned long long gp103_launch_count(void);
+
+/* Launch profile (single host thread): after gp103_profile_begin(stream), every launch records an event on its
+ * stream; gp103_profile_end waits for the last one and writes each launch's duration (ms, event to event, so a
+ * launch's time includes any gap before it) and the name of its launcher. Returns the number of launches profiled
+ * (at most GP103_PROFILE_MAX), negative on a CUDA error. */
+#define GP103_PROFILE_MAX 512
+int gp103_profile_begin(cudaStream_t stream);
+int gp103_profile_end(float* ms, const char** names, int max);
+
 /* ------------------------------------------------------------------------------------------------ part 1
  * gp_cuda.wa (cpp_to_py/gp_cuda.cpp:31-38; launcher wa_wirelength, gp_cuda_kernel.cu:59-65).
  * Weighted-average wirelength of the nets [0, num_nets) grouped by net_start, gamma read from device memory.

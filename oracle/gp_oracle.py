@@ -139,10 +139,13 @@ def spectral_operator(nbx, nby, bin_np, dtype=np.float64):
     return np.stack([-1j * kx * inv, -1j * ky * inv])
 
 
-def field_fft(rho_mirrored, nbx, nby, bin_np):
-    """Field of the mirrored map in float64 -> [2, 2 nbx, 2 nby] (x plane, y plane)."""
+def field_fft(rho_mirrored, nbx, nby, bin_np, dtype=np.float64):
+    """Field of the mirrored map -> [2, 2 nbx, 2 nby] (x plane, y plane); float64, or float32 / complex64 as the
+    reference's CPU path computes it."""
     op = spectral_operator(nbx, nby, bin_np)
-    spec = np.fft.rfft2(np.asarray(rho_mirrored, np.float64))
+    if dtype == np.float32:
+        op = op.astype(np.complex64)
+    spec = np.fft.rfft2(np.asarray(rho_mirrored, dtype))
     return np.fft.irfft2(spec[None] * op, s=(2 * nbx, 2 * nby))
 
 
@@ -314,10 +317,11 @@ def select(S, u, v, g, u_next, v_next, g_next, best):
 class CpuLevel(object):
     """One level of global placement on the CPU with the oracle operators (the reference's `--gpu -1` iteration,
     restated): a wirelength-only start, the first density weight in tension units, then the density phase with
-    the control rules above. `dtype` is the float type of the field and gradient arithmetic."""
+    the control rules above. `dtype` is the float type of the wirelength and field arithmetic; `field` = "dct"
+    (cosine / sine transforms of the plain map) or "fft" (FFT of the mirrored map, as the reference)."""
 
-    def __init__(self, prob, dtype=np.float64):
-        self.p, self.dtype = prob, dtype
+    def __init__(self, prob, dtype=np.float64, field="dct"):
+        self.p, self.dtype, self.field = prob, dtype, field
         self.evals = 0
 
     def wirelength(self, pos, gamma):
@@ -329,14 +333,17 @@ class CpuLevel(object):
         """-> (gradient [n, 2], overflow on the overflow grid)."""
         p, gr = self.p, self.p.force
         m = density_map(pos, gr.size, gr.ratio, p.num_mov, gr.bx, gr.by, gr.nbx, gr.nby)
-        _, _, ovsum = density_post(m, gr.fixed_map, gr.target, gr.nbx, gr.nby, mirrored=False)
+        rho, _, ovsum = density_post(m, gr.fixed_map, gr.target, gr.nbx, gr.nby, mirrored=self.field == "fft")
         overflow = ovsum * gr.bin_area / gr.mov_area
         if p.judge is not None:
             j = p.judge
             mj = density_map(pos[:p.num_mov], j.size, j.ratio, p.num_mov, j.bx, j.by, j.nbx, j.nby)
             _, _, js = density_post(mj, j.fixed_map, j.target, j.nbx, j.nby, mirrored=False)
             overflow = js * j.bin_area / j.mov_area
-        ex, ey = field_dct(plain_density(m, gr.fixed_map), gr.bin_np)
+        if self.field == "fft":
+            ex, ey = field_fft(rho, gr.nbx, gr.nby, gr.bin_np, self.dtype)
+        else:
+            ex, ey = field_dct(plain_density(m, gr.fixed_map), gr.bin_np)
         g = density_grad(pos, gr.size, gr.ratio, ex, ey, wl_grad, p.pins, p.area, weight, precond, gr.bx, gr.by,
                          gr.nbx, gr.nby)
         return g, overflow
