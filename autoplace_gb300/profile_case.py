@@ -1,9 +1,9 @@
-"""A fixed profiling case: place one synthetic netlist, then run extra density passes inside an NVTX range
-"gp103_profile" (so a profiler can be limited to them with --nvtx --nvtx-include "gp103_profile/").
+"""A fixed profiling case: place one synthetic netlist, then run extra density passes (from the placed state)
+inside an NVTX range "gp103_profile", so that a profiler can be limited to them with
+--nvtx --nvtx-include "gp103_profile/".
 
-    python -m autoplace_gb300.profile_case --config c2 --passes 8 [--field bf16x6] [--no-run]
-
---no-run skips the placement (the passes then run from the seeded start positions, a clumped state)."""
+    python -m autoplace_gb300.profile_case --config c2 --passes 8 [--field bf16x6]
+"""
 import argparse
 import time
 
@@ -18,18 +18,14 @@ def main(argv=None):
     ap.add_argument("--config", default="c2")
     ap.add_argument("--field", default="bf16x6")
     ap.add_argument("--passes", type=int, default=8)
-    ap.add_argument("--no-run", action="store_true")
     a = ap.parse_args(argv)
     nl, o = synth.preset(a.config)
     prob = problem.Problem(nl, problem.options(**o))
     pl = Placer(prob, field=a.field)
     pos0 = synth.init_positions(nl, prob.num_nodes)
     t = time.time()
-    if not a.no_run:
-        r = pl.run(pos0)
-        print("placed: %s after %d iterations, %.3f s" % (r["reason"], r["iters"], time.time() - t))
-    else:
-        pl.run_setup_only = True
+    r = pl.run(pos0)
+    print("placed: %s after %d iterations, %.3f s" % (r["reason"], r["iters"], time.time() - t))
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("gp103_profile")
     pl._passes(native.PHASE_DENSITY, a.passes)
