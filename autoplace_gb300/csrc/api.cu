@@ -89,6 +89,7 @@ extern "C" int gp103_wa(const float* pos, const int* pin_cell, const float* pin_
         j.net_start = net_start;
         j.num_nets = num_nets;
         j.num_mov = num_mov;
+        j.split = num_nets;
         j.gamma = gamma;
         j.pin_grad = (float2*)pin_grad;
         j.out = (float2*)out;
@@ -118,7 +119,7 @@ extern "C" int gp103_density_map(const float* pos, const float* size, const floa
     j.nby = nby;
     j.map0 = map;
     j.map1 = map + (size_t)nbx * nby;
-    TRY(launch_scatter(j, stream));
+    TRY(launch_scatter(&j, 1, stream));
     return launch_post_mirror(map, fixed, target, nbx, nby, rho, over, stream);
 }
 
@@ -170,7 +171,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(ratio), OFF(pins), OFF(area), OFF(lo), OFF(hi), OFF(bx), OFF(by), OFF(target), OFF(fixed),
         OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
-        OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters)};
+        OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -194,6 +195,8 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->nbx > 0 && p->nby > 0 && p->bx > 0.f && p->by > 0.f);
     REQUIRE(p->field_const && p->field_work && p->ex && p->ey && p->red && p->counters && p->map && p->kp);
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
+    REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
+    REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
     if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
     return GP103_OK;
 }
@@ -237,9 +240,9 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
     sj.nby = p->nby;
     sj.map0 = p->map;
     sj.map1 = p->map + nb;
-    TRY(launch_scatter(sj, s));
+    ScatterJob jobs[2] = {sj, sj};
     if (p->jnbx > 0) {
-        ScatterJob jj = sj;
+        ScatterJob& jj = jobs[1];
         jj.size = (const float2*)p->jsize;
         jj.ratio = p->jratio;
         jj.num_nodes = p->num_mov;
@@ -249,8 +252,8 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
         jj.nby = p->jnby;
         jj.map0 = p->jmap;
         jj.map1 = nullptr;
-        TRY(launch_scatter(jj, s));
     }
+    TRY(launch_scatter(jobs, p->jnbx > 0 ? 2 : 1, s));
     const FieldLayout L = layout_of(p);
     PostJob pj = {};
     pj.map = p->map;
@@ -269,17 +272,18 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
         pj.terms = 3;
     }
     pj.red = reduce_slot(p->red, p->counters, R_OVF);
-    TRY(launch_post_plain(pj, s));
+    PostJob posts[2] = {pj, pj};
     if (p->jnbx > 0) {
-        PostJob jp = {};
+        PostJob& jp = posts[1];
+        jp = PostJob{};
         jp.map = p->jmap;
         jp.fixed = p->jfixed;
         jp.target = p->target;
         jp.nbx = p->jnbx;
         jp.nby = p->jnby;
         jp.red = reduce_slot(p->red, p->counters, R_JOVF);
-        TRY(launch_post_plain(jp, s));
     }
+    TRY(launch_post_plain(posts, p->jnbx > 0 ? 2 : 1, s));
     return run_field(p, nullptr, s);
 }
 
@@ -297,7 +301,7 @@ static GatherJob gather_job(const gp103_plan* p) {
     g.nby = p->nby;
     g.pin_grad = (const float2*)p->pin_grad;
     g.cell_start = p->cell_start;
-    g.cell_pin = p->cell_pin;
+    g.cell_pin = p->pin_slot ? nullptr : p->cell_pin;
     g.red = reduce_slot(p->red, p->counters, R_GRAD);
     return g;
 }
@@ -309,6 +313,8 @@ static WaJob wa_job(const gp103_plan* p) {
     w.net_start = p->net_start;
     w.num_nets = p->num_nets;
     w.num_mov = p->num_mov;
+    w.split = p->net_split;
+    w.slot = p->pin_slot;
     w.gamma = p->kp;
     w.pin_grad = (float2*)p->pin_grad;
     w.red = reduce_slot(p->red, p->counters, R_WA);

@@ -14,26 +14,40 @@ namespace gp103 {
 
 // ----------------------------------------------------------------------------- scatter
 // A block takes a chunk of SCAT_CHUNK consecutive nodes, all movable or all fillers. If the bins its nodes touch fit
-// in shared memory (bounding box <= SCAT_SMEM_BINS), the block adds its charges there with shared 64-bit atomics and
-// then adds every non-zero bin to the global map once; otherwise it adds each charge to the global map directly.
+// in shared memory (bounding box <= SCAT_SMEM_BINS), the block sums its charges there and then adds every non-zero
+// bin to the global map once; otherwise it adds each charge to the global map directly (64-bit atomics in L2).
+// In shared memory a 64-bit sum is kept as two 32-bit words: a charge (at most 2^32) adds its low word to `lo` with
+// a 32-bit atomic whose old value tells whether the word wrapped; the wrap and the charge's high bit go to `hi`.
+// Exact (integer) in any order, with a single 32-bit atomic for most charges.
 constexpr int SCAT_THREADS = 256;
 constexpr int SCAT_PER_THREAD = 4;
 constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;
-constexpr int SCAT_SMEM_BINS = 6144;      // 48 KB of 64-bit bins
+constexpr int SCAT_SMEM_BINS = 6144;      // 2 x 24 KB of 32-bit words
 
-__global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(ScatterJob j) {
-    __shared__ unsigned long long tile[SCAT_SMEM_BINS];
+__device__ __forceinline__ void add_shared(unsigned int* lo, unsigned int* hi, int b, unsigned long long q) {
+    const unsigned int ql = (unsigned int)q;
+    unsigned int qh = (unsigned int)(q >> 32);
+    const unsigned int old = atomicAdd(lo + b, ql);
+    if (old + ql < old) qh += 1u;
+    if (qh) atomicAdd(hi + b, qh);
+}
+
+__global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_constant__ ScatterPair pair) {
+    __shared__ unsigned int tlo[SCAT_SMEM_BINS], thi[SCAT_SMEM_BINS];
     __shared__ int box[4];
+    const bool second = (int)blockIdx.x >= pair.blocks0;
+    const ScatterJob& j = second ? pair.j[1] : pair.j[0];
+    const int bid = second ? (int)blockIdx.x - pair.blocks0 : (int)blockIdx.x;
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const int cell_chunks = ceil_div(j.num_mov, SCAT_CHUNK);
     int first, last;
     unsigned long long* map;
-    if ((int)blockIdx.x < cell_chunks) {
-        first = blockIdx.x * SCAT_CHUNK;
+    if (bid < cell_chunks) {
+        first = bid * SCAT_CHUNK;
         last = min(first + SCAT_CHUNK, j.num_mov);
         map = j.map0;
     } else {
-        first = j.num_mov + (blockIdx.x - cell_chunks) * SCAT_CHUNK;
+        first = j.num_mov + (bid - cell_chunks) * SCAT_CHUNK;
         last = min(first + SCAT_CHUNK, j.num_nodes);
         map = j.map1;
     }
@@ -68,21 +82,22 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(ScatterJob j) {
     const long long w = (long long)(bx1 - bx0 + 1), h = (long long)(by1 - by0 + 1);
     if (w * h <= SCAT_SMEM_BINS) {
         const int H = (int)h, area = (int)(w * h);
-        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) tile[t] = 0ull;
+        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) { tlo[t] = 0u; thi[t] = 0u; }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < SCAT_PER_THREAD; k++) {
             for (int x = sx[k].b0; x <= sx[k].b1; x++) {
                 const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
+                const int row = (x - bx0) * H - by0;
                 for (int y = sy[k].b0; y <= sy[k].b1; y++) {
-                    unsigned long long q = charge(wx, overlap(sy[k], y));
-                    if (q) atomicAdd(&tile[(x - bx0) * H + (y - by0)], q);
+                    const unsigned long long q = charge(wx, overlap(sy[k], y));
+                    if (q) add_shared(tlo, thi, row + y, q);
                 }
             }
         }
         __syncthreads();
         for (int t = threadIdx.x; t < area; t += SCAT_THREADS) {
-            unsigned long long q = tile[t];
+            const unsigned long long q = ((unsigned long long)thi[t] << 32) | tlo[t];
             if (q) atomicAdd(&map[(size_t)(bx0 + t / H) * j.nby + (by0 + t % H)], q);
         }
     } else {
@@ -91,7 +106,7 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(ScatterJob j) {
             for (int x = sx[k].b0; x <= sx[k].b1; x++) {
                 const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
                 for (int y = sy[k].b0; y <= sy[k].b1; y++) {
-                    unsigned long long q = charge(wx, overlap(sy[k], y));
+                    const unsigned long long q = charge(wx, overlap(sy[k], y));
                     if (q) atomicAdd(&map[(size_t)x * j.nby + y], q);
                 }
             }
@@ -99,10 +114,19 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(ScatterJob j) {
     }
 }
 
-int launch_scatter(const ScatterJob& j, cudaStream_t s) {
-    int blocks = ceil_div(j.num_mov, SCAT_CHUNK) + ceil_div(j.num_nodes - j.num_mov, SCAT_CHUNK);
+static int scatter_blocks(const ScatterJob& j) {
+    return ceil_div(j.num_mov, SCAT_CHUNK) + ceil_div(j.num_nodes - j.num_mov, SCAT_CHUNK);
+}
+
+int launch_scatter(const ScatterJob* jobs, int njobs, cudaStream_t s) {
+    ScatterPair p = {};
+    p.j[0] = jobs[0];
+    p.j[1] = njobs > 1 ? jobs[1] : jobs[0];
+    p.njobs = njobs;
+    p.blocks0 = scatter_blocks(jobs[0]);
+    const int blocks = p.blocks0 + (njobs > 1 ? scatter_blocks(jobs[1]) : 0);
     if (blocks == 0) return GP103_OK;
-    scatter_kernel<<<blocks, SCAT_THREADS, 0, s>>>(j);
+    scatter_kernel<<<blocks, SCAT_THREADS, 0, s>>>(p);
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -133,7 +157,8 @@ int launch_post_mirror(const unsigned long long* map, const float* fixed, float 
 }
 
 // Fused layout: the plain total density for the field (float32 plane, or the bf16 terms of its split) and the
-// float64 sum of the density above the target; the map is zeroed behind the read for the next pass.
+// float64 sum of the density above the target; the map is zeroed behind the read for the next pass. Up to two
+// grids per launch (force grid, overflow grid), each with its own reduction.
 __device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0, __nv_bfloat16* t1,
                                            __nv_bfloat16* t2, size_t at) {
     __nv_bfloat16 a = __float2bfloat16_rn(r);
@@ -144,10 +169,14 @@ __device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0
     if (terms > 2) t2[at] = __float2bfloat16_rn(__fsub_rn(rem, __bfloat162float(b)));
 }
 
-__global__ void post_plain_kernel(PostJob j) {
+__global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
+    const bool second = (int)blockIdx.x >= pair.blocks0;
+    const PostJob& j = second ? pair.j[1] : pair.j[0];
+    const int bid = second ? (int)blockIdx.x - pair.blocks0 : (int)blockIdx.x;
+    const int nblk = second ? (int)gridDim.x - pair.blocks0 : pair.blocks0;
     const int nb = j.nbx * j.nby;
     double ov = 0.0;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    for (int b = bid * blockDim.x + threadIdx.x; b < nb; b += nblk * blockDim.x) {
         const unsigned long long m0 = j.map[b];
         const float mov = __fadd_rn((float)((double)m0 / DENSITY_SCALE), j.fixed[b]);
         ov += (double)fmaxf(__fsub_rn(mov, j.target), 0.f);
@@ -161,11 +190,17 @@ __global__ void post_plain_kernel(PostJob j) {
         j.map[b] = 0ull;
     }
     double v[1] = {ov};
-    grid_sum<1>(v, j.red);
+    grid_sum<1>(v, j.red, nblk, bid);
 }
 
-int launch_post_plain(const PostJob& j, cudaStream_t s) {
-    post_plain_kernel<<<grid_for((long long)j.nbx * j.nby, 256, 4), 256, 0, s>>>(j);
+int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s) {
+    PostPair p = {};
+    p.j[0] = jobs[0];
+    p.j[1] = njobs > 1 ? jobs[1] : jobs[0];
+    p.njobs = njobs;
+    p.blocks0 = grid_for((long long)jobs[0].nbx * jobs[0].nby, 256, 4);
+    const int blocks = p.blocks0 + (njobs > 1 ? grid_for((long long)jobs[1].nbx * jobs[1].nby, 256, 4) : 0);
+    post_plain_kernel<<<blocks, 256, 0, s>>>(p);
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -216,9 +251,10 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
     return GP103_OK;
 }
 
-// Fused gather: the field planes [nbx][nby]; the wirelength gradient of a cell summed here from the pins' gradients
-// (cell CSR, fixed order); the new gradient, its squared distance to the previous one and its L1 norm over the
-// cells reduced in float64.
+// Fused gather: the field planes [nbx][nby]; the wirelength gradient of a cell summed here from its pins'
+// gradients in the reference's order (cell CSR: contiguous when the pin gradients are stored in cell order, else
+// through cell_pin); the new gradient, its squared distance to the previous one and its L1 norm over the cells
+// reduced in float64.
 __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     float2* gout = pick_mut(j.gout_a, j.gout_b, j.sel);
@@ -250,7 +286,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
         if (j.with_wl && i < j.num_mov) {
             const int k0 = j.cell_start[i], k1 = j.cell_start[i + 1];
             for (int k = k0; k < k1; k++) {
-                const float2 q = j.pin_grad[j.cell_pin[k]];
+                const float2 q = j.pin_grad[j.cell_pin ? j.cell_pin[k] : k];
                 wx += q.x;
                 wy += q.y;
             }

@@ -1,11 +1,12 @@
 // Tensor-core form of the field's six GEMMs (GB300, sm_103a): tcgen05.mma (kind::f16, bf16 operands, float32
 // accumulation in tensor memory), operands staged by TMA (cp.async.bulk.tensor, 128-byte swizzle) through an
 // mbarrier pipeline, one elected thread issuing the MMAs, four warps reading the accumulator back (tcgen05.ld) into
-// fused epilogues, with the accumulation promoted to float32 registers after every k-block (below). Operands are float32 values split into bf16 terms, a = a0 + a1 + a2 (each term the bf16 rounding
-// of what the previous ones leave), stored as three planes; a product is a list of (A term, B term) pairs over the
-// same K, concatenated along K into one accumulation:
-//   bf16x3: (0,0) (0,1) (1,0)                          ~1e-5 of the max
-//   bf16x6: (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)        ~1e-7 of the max (float32-level)
+// fused epilogues, with the accumulation promoted to float32 registers after every k-block (below). Operands are
+// float32 values split into bf16 terms, a = a0 + a1 + a2 (each term the bf16 rounding of what the previous ones
+// leave), stored as three planes; a product is a list of (A term, B term) pairs over the same K, all issued on the
+// same staged k-block (each term's tile is loaded once per k-block) into one accumulator:
+//   bf16x3: (1,0) (0,1) (0,0)                          ~1e-5 of the max
+//   bf16x6: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)        ~2e-7 of the max (float32-level)
 // Shapes: M, N multiples of 128, K a multiple of 64 (force grids of 128 .. 2048 bins per side).
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -16,10 +17,11 @@
 
 namespace gp103 {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 6;
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;                  // 16 KB per operand tile
-constexpr int TC_STAGE_BYTES = 2 * TC_TILE_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+constexpr int TC_STAGE_SPACE = 12 * TC_TILE_BYTES;               // 192 KB of stages
+constexpr int TC_MAX_STAGES = 3;
+constexpr int TC_SMEM = TC_STAGE_SPACE + 1024 + 256;
 constexpr long long TC_WAIT_NS = 2000000000LL;                  // a wait that takes 2 s has failed
 
 struct TcProblem {
@@ -31,10 +33,13 @@ struct TcProblem {
     const float* w0; const float* w1;
 };
 
+// A stage holds the k-block (64 of K) of every term of A and of B that the products read: na A tiles, then nb B
+// tiles. Each of the nprod products (ia, ib) is four MMAs over that k-block, all into one accumulator, in the order
+// given (smallest first, so the truncating accumulation adds small terms while the sum is small).
 struct TcArgs {
     TcProblem p[2];
-    int nseg;
-    int seg_a[6], seg_b[6];
+    int na, nb, nprod, stages;
+    int prod_a[6], prod_b[6];
     int* err;
 };
 
@@ -146,23 +151,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     // barriers: full[S], empty[S], acc_full[2], acc_empty[2]
-    uint64_t* bars = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);
-    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_STAGES + 4);
+    uint64_t* bars = (uint64_t*)(smem + TC_STAGE_SPACE);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_MAX_STAGES + 4);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int z = blockIdx.z;
     const TcProblem& P = args.p[z];
     const CUtensorMap* ma = z ? &a1 : &a0;
     const CUtensorMap* mb = z ? &b1 : &b0;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
-    const int kblocks = P.K / TC_BK, total = kblocks * args.nseg;
+    const int total = P.K / TC_BK, stages = args.stages;
+    const int stage_bytes = (args.na + args.nb) * TC_TILE_BYTES;
     int* err = args.err;
     auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
-    auto empty_bar = [&](int s) { return smem_u32(&bars[TC_STAGES + s]); };
-    auto accf_bar = [&](int b) { return smem_u32(&bars[2 * TC_STAGES + b]); };
-    auto acce_bar = [&](int b) { return smem_u32(&bars[2 * TC_STAGES + 2 + b]); };
+    auto empty_bar = [&](int s) { return smem_u32(&bars[TC_MAX_STAGES + s]); };
+    auto accf_bar = [&](int b) { return smem_u32(&bars[2 * TC_MAX_STAGES + b]); };
+    auto acce_bar = [&](int b) { return smem_u32(&bars[2 * TC_MAX_STAGES + 2 + b]); };
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; s++) {
+        for (int s = 0; s < stages; s++) {
             mbar_init(full_bar(s), 1);
             mbar_init(empty_bar(s), 1);
         }
@@ -185,29 +191,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {                                         // TMA producer
             for (int it = 0; it < total; it++) {
-                const int s = it % TC_STAGES;
-                const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+                const int s = it % stages;
+                const uint32_t ph = (uint32_t)(it / stages) & 1u;
                 if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1)) break;
-                const int seg = it / kblocks, kb = it % kblocks;
-                mbar_expect_tx(full_bar(s), TC_STAGE_BYTES);
-                uint8_t* st = smem + s * TC_STAGE_BYTES;
-                tma_load_3d(smem_u32(st), ma, full_bar(s), kb * TC_BK, m0, args.seg_a[seg]);
-                tma_load_3d(smem_u32(st + TC_TILE_BYTES), mb, full_bar(s), kb * TC_BK, n0, args.seg_b[seg]);
+                mbar_expect_tx(full_bar(s), stage_bytes);
+                uint8_t* st = smem + s * stage_bytes;
+                for (int t = 0; t < args.na; t++)
+                    tma_load_3d(smem_u32(st + t * TC_TILE_BYTES), ma, full_bar(s), it * TC_BK, m0, t);
+                for (int t = 0; t < args.nb; t++)
+                    tma_load_3d(smem_u32(st + (args.na + t) * TC_TILE_BYTES), mb, full_bar(s), it * TC_BK, n0, t);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {                                         // MMA issuer: one k-block per accumulator
             for (int it = 0; it < total; it++) {
-                const int s = it % TC_STAGES, b = it & 1;
-                const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u, use = (uint32_t)(it >> 1) & 1u;
+                const int s = it % stages, b = it & 1;
+                const uint32_t ph = (uint32_t)(it / stages) & 1u, use = (uint32_t)(it >> 1) & 1u;
                 if (!mbar_wait(acce_bar(b), use ^ 1u, err, 2)) break;
                 if (!mbar_wait(full_bar(s), ph, err, 3)) break;
                 tc_fence_after();
-                const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES), sb = sa + TC_TILE_BYTES;
+                const uint32_t st = smem_u32(smem + s * stage_bytes);
                 const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+                for (int q = 0; q < args.nprod; q++) {
+                    const uint32_t sa = st + args.prod_a[q] * TC_TILE_BYTES;
+                    const uint32_t sb = st + (args.na + args.prod_b[q]) * TC_TILE_BYTES;
 #pragma unroll
-                for (int kk = 0; kk < TC_BK / 16; kk++)
-                    mma_bf16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), kk > 0 ? 1u : 0u);
+                    for (int kk = 0; kk < TC_BK / 16; kk++)
+                        mma_bf16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (q > 0 || kk > 0) ? 1u : 0u);
+                }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
             }
@@ -337,12 +348,16 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
             return GP103_ERR_CUDA;
         args.p[z] = o.p;
     }
-    static const int x3a[3] = {0, 0, 1}, x3b[3] = {0, 1, 0};
+    static const int x3a[3] = {1, 0, 0}, x3b[3] = {0, 1, 0};
     static const int x6a[6] = {2, 1, 0, 1, 0, 0}, x6b[6] = {0, 1, 2, 0, 1, 0};
-    args.nseg = mode == GP103_FIELD_BF16X3 ? 3 : 6;
-    for (int i = 0; i < args.nseg; i++) {
-        args.seg_a[i] = mode == GP103_FIELD_BF16X3 ? x3a[i] : x6a[i];
-        args.seg_b[i] = mode == GP103_FIELD_BF16X3 ? x3b[i] : x6b[i];
+    const bool x3 = mode == GP103_FIELD_BF16X3;
+    args.na = args.nb = x3 ? 2 : 3;
+    args.nprod = x3 ? 3 : 6;
+    args.stages = TC_STAGE_SPACE / ((args.na + args.nb) * TC_TILE_BYTES);
+    if (args.stages > TC_MAX_STAGES) args.stages = TC_MAX_STAGES;
+    for (int i = 0; i < args.nprod; i++) {
+        args.prod_a[i] = x3 ? x3a[i] : x6a[i];
+        args.prod_b[i] = x3 ? x3b[i] : x6b[i];
     }
     args.err = err;
     const TcProblem& p = ops[0].p;

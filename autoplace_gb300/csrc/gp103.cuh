@@ -65,17 +65,18 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sh) {
     }
 }
 
+// The blocks taking part are numbered bid = 0 .. nblk - 1 (a launch may hold several independent reductions).
 template <int K>
-__device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
+__device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r, int nblk, int bid) {
     __shared__ double sh[K * 32];
     __shared__ bool last;
     block_sum<K>(v, sh);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; k++) r.partials[(size_t)k * gridDim.x + blockIdx.x] = v[k];
+        for (int k = 0; k < K; k++) r.partials[(size_t)k * nblk + bid] = v[k];
         __threadfence();
         unsigned int t = atomicAdd(r.counter, 1u);
-        last = (t == gridDim.x - 1);
+        last = (t == (unsigned int)nblk - 1);
     }
     __syncthreads();
     if (last) {
@@ -83,9 +84,9 @@ __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
         double s[K];
 #pragma unroll
         for (int k = 0; k < K; k++) s[k] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x)
 #pragma unroll
-            for (int k = 0; k < K; k++) s[k] += __ldcg(r.partials + (size_t)k * gridDim.x + b);
+            for (int k = 0; k < K; k++) s[k] += __ldcg(r.partials + (size_t)k * nblk + b);
         block_sum<K>(s, sh);
         if (threadIdx.x == 0) {
 #pragma unroll
@@ -93,6 +94,11 @@ __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
             *r.counter = 0;
         }
     }
+}
+
+template <int K>
+__device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
+    grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
 }
 
 // ----------------------------------------------------------------------------- node span on a bin grid

@@ -39,6 +39,8 @@ struct WaJob {
     const float2* pos_a; const float2* pos_b; const int* sel;
     const int* pin_cell; const float2* pin_off; const int* net_start;
     int num_nets, num_mov;
+    int split;              // nets [split, num_nets): one warp each; below: 32 per warp (num_nets: any order)
+    const int* slot;        // pin p's gradient goes to pin_grad[slot[p]] (null: pin_grad[p])
     const float* gamma;
     float2* pin_grad;
     float2* out;            // per-net (WA, HPWL), may be null
@@ -55,6 +57,13 @@ struct ScatterJob {
     unsigned long long* map1;   // the rest (null: not added)
 };
 
+// One launch for up to two scatters (the force grid and the overflow grid read the same positions).
+struct ScatterPair {
+    ScatterJob j[2];
+    int njobs;
+    int blocks0;                // blocks of job 0; the rest are job 1's
+};
+
 struct PostJob {
     unsigned long long* map;    // [1 or 2][nbx][nby], zeroed behind the read
     const float* fixed;
@@ -67,6 +76,12 @@ struct PostJob {
     Reduce red;                 // sum of the density above the target
 };
 
+struct PostPair {
+    PostJob j[2];
+    int njobs;
+    int blocks0;
+};
+
 struct GatherJob {
     const float2* pos_a; const float2* pos_b; const int* sel;
     const float2* size; const float* ratio; const float* pins; const float* area;
@@ -77,7 +92,7 @@ struct GatherJob {
     const float* weight_p; const float* precond_p;   // device scalars, or null: the host values below
     float weight, precond;
     int with_wl;
-    const float2* pin_grad; const int* cell_start; const int* cell_pin;
+    const float2* pin_grad; const int* cell_start; const int* cell_pin;   // cell_pin null: pin_grad in cell order
     float2* gout_a; float2* gout_b;
     const float2* gref_a; const float2* gref_b;     // null: no distance
     Reduce red;                 // (|g - gref|^2, L1 of g over the cells)
@@ -86,10 +101,10 @@ struct GatherJob {
 int launch_wa_net(const WaJob& j, cudaStream_t s);
 int launch_wa_cell(const float2* pin_grad, const int* cell_start, const int* cell_pin, int num_mov, float2* grad,
                    cudaStream_t s);
-int launch_scatter(const ScatterJob& j, cudaStream_t s);
+int launch_scatter(const ScatterJob* jobs, int njobs, cudaStream_t s);
 int launch_post_mirror(const unsigned long long* map, const float* fixed, float target, int nbx, int nby, float* rho,
                        float* over, cudaStream_t s);
-int launch_post_plain(const PostJob& j, cudaStream_t s);
+int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s);
 int launch_gather_mirror(const float* pos, const float* size, const float* ratio, const float* field,
                          const float* wl_grad, const float* pins, const float* area, int num_nodes, int num_wl,
                          const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,

@@ -5,9 +5,14 @@
 // sp = sum e^{(x - hi)/g}, xp = sum x e^{(x - hi)/g} / sp (and sn, xn with lo), WA = xp - xn, HPWL = hi - lo,
 // pin gradient ep (1 + (x - xp)/g)/sp - en (1 - (x - xn)/g)/sn.
 //
-// A thread per net up to WA_REG pins, a warp per longer net, pins held in registers (one pass over memory). With
-// nets ordered by degree (what the fused path does at set-up) a warp's nets have equal degree and its loads are
-// contiguous. Exponentials use the hardware exp2 path (__expf), as the reference does under --use_fast_math.
+// Work items: a warp takes either 32 consecutive nets, one per lane (nets of up to WA_REG pins; a longer one met
+// there is done by the whole warp in turn), or, for nets from `split` on, one long net with the whole warp (lane l
+// takes pins l, l + 32, ...; max / min and sums by butterfly reductions). Pins stay in registers: one pass over
+// memory. The fused path orders the nets at set-up (short ones by their first cell, long ones after `split`), so
+// that warps do equal work and their gathers stay local; any order gives the same numbers. The pin gradient can go
+// to a slot in cell order (the gather then reads each cell's pins contiguously). Exponentials use the hardware exp2
+// path (__expf), as the reference does under --use_fast_math; the per-pin divisions by the sums are multiplications
+// by their reciprocals (within an ulp of the reference's form).
 #include "gp103.cuh"
 #include "kernels.cuh"
 
@@ -21,6 +26,10 @@ __device__ __forceinline__ float2 pin_xy(const WaJob& j, const float2* pos, int 
     const float2 o = __ldg(j.pin_off + p);
     const float2 q = c < j.num_mov ? pos[c] : make_float2(0.f, 0.f);
     return make_float2(q.x + o.x, q.y + o.y);
+}
+
+__device__ __forceinline__ void put(const WaJob& j, int p, float gx, float gy) {
+    j.pin_grad[j.slot ? __ldg(j.slot + p) : p] = make_float2(gx, gy);
 }
 
 __device__ __forceinline__ float wmax(float v) {
@@ -39,138 +48,147 @@ __device__ __forceinline__ float wsum(float v) {
     return v;
 }
 
-// Per-axis sums of a net: sp, sn, xp (sum x ep), xn (sum x en).
-struct Sums {
+// Running state of a net: per axis hi / lo and the sums sp, sn, xp, xn.
+struct Net {
+    float hx, lx, hy, ly;
     float spx, snx, xpx, xnx, spy, sny, xpy, xny;
+    __device__ __forceinline__ void init() {
+        hx = hy = -1e30f;
+        lx = ly = 1e30f;
+        spx = snx = xpx = xnx = spy = sny = xpy = xny = 0.f;
+    }
+    __device__ __forceinline__ void extent(float2 x) {
+        hx = fmaxf(hx, x.x); lx = fminf(lx, x.x);
+        hy = fmaxf(hy, x.y); ly = fminf(ly, x.y);
+    }
+    __device__ __forceinline__ void add(float2 x, float ig) {
+        const float epx = __expf((x.x - hx) * ig), enx = __expf((lx - x.x) * ig);
+        const float epy = __expf((x.y - hy) * ig), eny = __expf((ly - x.y) * ig);
+        spx += epx; snx += enx; xpx += x.x * epx; xnx += x.x * enx;
+        spy += epy; sny += eny; xpy += x.y * epy; xny += x.y * eny;
+    }
 };
 
-// A net of d <= WA_REG pins by one thread, pins in registers.
+// After the sums: the means and reciprocals the pin gradients need.
+struct Coef {
+    float xpx, xnx, xpy, xny, ipx, inx, ipy, iny;
+    __device__ __forceinline__ void from(const Net& n) {
+        xpx = n.xpx / n.spx; xnx = n.xnx / n.snx; xpy = n.xpy / n.spy; xny = n.xny / n.sny;
+        ipx = 1.f / n.spx; inx = 1.f / n.snx; ipy = 1.f / n.spy; iny = 1.f / n.sny;
+    }
+    __device__ __forceinline__ float2 grad(const Net& n, float2 x, float ig) const {
+        const float epx = __expf((x.x - n.hx) * ig), enx = __expf((n.lx - x.x) * ig);
+        const float epy = __expf((x.y - n.hy) * ig), eny = __expf((n.ly - x.y) * ig);
+        return make_float2(epx * (1.f + (x.x - xpx) * ig) * ipx - enx * (1.f - (x.x - xnx) * ig) * inx,
+                           epy * (1.f + (x.y - xpy) * ig) * ipy - eny * (1.f - (x.y - xny) * ig) * iny);
+    }
+};
+
+// A net of d <= WA_REG pins by one thread.
 __device__ __forceinline__ void net_thread(const WaJob& j, const float2* pos, float ig, int s, int d, float& wa,
                                            float& hp) {
-    float hx = -1e30f, lx = 1e30f, hy = -1e30f, ly = 1e30f;
+    Net n;
+    n.init();
     float2 x[WA_REG];
 #pragma unroll
     for (int k = 0; k < WA_REG; k++)
         if (k < d) {
             x[k] = pin_xy(j, pos, s + k);
-            hx = fmaxf(hx, x[k].x); lx = fminf(lx, x[k].x);
-            hy = fmaxf(hy, x[k].y); ly = fminf(ly, x[k].y);
+            n.extent(x[k]);
         }
-    float epx[WA_REG], enx[WA_REG], epy[WA_REG], eny[WA_REG];
-    Sums m = {};
+#pragma unroll
+    for (int k = 0; k < WA_REG; k++)
+        if (k < d) n.add(x[k], ig);
+    Coef c;
+    c.from(n);
 #pragma unroll
     for (int k = 0; k < WA_REG; k++)
         if (k < d) {
-            epx[k] = __expf((x[k].x - hx) * ig); enx[k] = __expf((lx - x[k].x) * ig);
-            epy[k] = __expf((x[k].y - hy) * ig); eny[k] = __expf((ly - x[k].y) * ig);
-            m.spx += epx[k]; m.snx += enx[k]; m.xpx += x[k].x * epx[k]; m.xnx += x[k].x * enx[k];
-            m.spy += epy[k]; m.sny += eny[k]; m.xpy += x[k].y * epy[k]; m.xny += x[k].y * eny[k];
+            const float2 g = c.grad(n, x[k], ig);
+            put(j, s + k, g.x, g.y);
         }
-    const float xpx = m.xpx / m.spx, xnx = m.xnx / m.snx, xpy = m.xpy / m.spy, xny = m.xny / m.sny;
-#pragma unroll
-    for (int k = 0; k < WA_REG; k++)
-        if (k < d) {
-            float gx = epx[k] * (1.f + (x[k].x - xpx) * ig) / m.spx - enx[k] * (1.f - (x[k].x - xnx) * ig) / m.snx;
-            float gy = epy[k] * (1.f + (x[k].y - xpy) * ig) / m.spy - eny[k] * (1.f - (x[k].y - xny) * ig) / m.sny;
-            j.pin_grad[s + k] = make_float2(gx, gy);
-        }
-    wa = (xpx - xnx) + (xpy - xny);
-    hp = (hx - lx) + (hy - ly);
+    wa = (c.xpx - c.xnx) + (c.xpy - c.xny);
+    hp = (n.hx - n.lx) + (n.hy - n.ly);
 }
 
-// A longer net by the whole warp: lane l takes pins l, l + 32, ...; max / min and sums by butterfly reductions
-// (every lane ends with the net's values).
+// A longer net by the whole warp (every lane ends with the net's values).
 __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, float ig, int s, int d, int lane,
                                          float& wa, float& hp) {
-    float hx = -1e30f, lx = 1e30f, hy = -1e30f, ly = 1e30f;
-    Sums m = {};
+    Net n;
+    n.init();
+    Coef c;
     if (d <= 32 * WA_WREG) {
         float2 x[WA_WREG];
 #pragma unroll
-        for (int t = 0; t < WA_WREG; t++) {
-            const int p = lane + 32 * t;
-            if (p < d) {
-                x[t] = pin_xy(j, pos, s + p);
-                hx = fmaxf(hx, x[t].x); lx = fminf(lx, x[t].x);
-                hy = fmaxf(hy, x[t].y); ly = fminf(ly, x[t].y);
+        for (int t = 0; t < WA_WREG; t++)
+            if (lane + 32 * t < d) {
+                x[t] = pin_xy(j, pos, s + lane + 32 * t);
+                n.extent(x[t]);
             }
+        n.hx = wmax(n.hx); n.lx = wmin(n.lx); n.hy = wmax(n.hy); n.ly = wmin(n.ly);
+#pragma unroll
+        for (int t = 0; t < WA_WREG; t++)
+            if (lane + 32 * t < d) n.add(x[t], ig);
+        n.spx = wsum(n.spx); n.snx = wsum(n.snx); n.xpx = wsum(n.xpx); n.xnx = wsum(n.xnx);
+        n.spy = wsum(n.spy); n.sny = wsum(n.sny); n.xpy = wsum(n.xpy); n.xny = wsum(n.xny);
+        c.from(n);
+#pragma unroll
+        for (int t = 0; t < WA_WREG; t++)
+            if (lane + 32 * t < d) {
+                const float2 g = c.grad(n, x[t], ig);
+                put(j, s + lane + 32 * t, g.x, g.y);
+            }
+    } else {                                             // very long nets: three passes, pins re-read (cached)
+        for (int p = lane; p < d; p += 32) n.extent(pin_xy(j, pos, s + p));
+        n.hx = wmax(n.hx); n.lx = wmin(n.lx); n.hy = wmax(n.hy); n.ly = wmin(n.ly);
+        for (int p = lane; p < d; p += 32) n.add(pin_xy(j, pos, s + p), ig);
+        n.spx = wsum(n.spx); n.snx = wsum(n.snx); n.xpx = wsum(n.xpx); n.xnx = wsum(n.xnx);
+        n.spy = wsum(n.spy); n.sny = wsum(n.sny); n.xpy = wsum(n.xpy); n.xny = wsum(n.xny);
+        c.from(n);
+        for (int p = lane; p < d; p += 32) {
+            const float2 g = c.grad(n, pin_xy(j, pos, s + p), ig);
+            put(j, s + p, g.x, g.y);
         }
-        hx = wmax(hx); lx = wmin(lx); hy = wmax(hy); ly = wmin(ly);
-        float epx[WA_WREG], enx[WA_WREG], epy[WA_WREG], eny[WA_WREG];
-#pragma unroll
-        for (int t = 0; t < WA_WREG; t++)
-            if (lane + 32 * t < d) {
-                epx[t] = __expf((x[t].x - hx) * ig); enx[t] = __expf((lx - x[t].x) * ig);
-                epy[t] = __expf((x[t].y - hy) * ig); eny[t] = __expf((ly - x[t].y) * ig);
-                m.spx += epx[t]; m.snx += enx[t]; m.xpx += x[t].x * epx[t]; m.xnx += x[t].x * enx[t];
-                m.spy += epy[t]; m.sny += eny[t]; m.xpy += x[t].y * epy[t]; m.xny += x[t].y * eny[t];
-            }
-        m.spx = wsum(m.spx); m.snx = wsum(m.snx); m.xpx = wsum(m.xpx); m.xnx = wsum(m.xnx);
-        m.spy = wsum(m.spy); m.sny = wsum(m.sny); m.xpy = wsum(m.xpy); m.xny = wsum(m.xny);
-        const float xpx = m.xpx / m.spx, xnx = m.xnx / m.snx, xpy = m.xpy / m.spy, xny = m.xny / m.sny;
-#pragma unroll
-        for (int t = 0; t < WA_WREG; t++)
-            if (lane + 32 * t < d) {
-                float gx = epx[t] * (1.f + (x[t].x - xpx) * ig) / m.spx - enx[t] * (1.f - (x[t].x - xnx) * ig) / m.snx;
-                float gy = epy[t] * (1.f + (x[t].y - xpy) * ig) / m.spy - eny[t] * (1.f - (x[t].y - xny) * ig) / m.sny;
-                j.pin_grad[s + lane + 32 * t] = make_float2(gx, gy);
-            }
-        wa = (xpx - xnx) + (xpy - xny);
-        hp = (hx - lx) + (hy - ly);
-        return;
     }
-    for (int p = lane; p < d; p += 32) {                 // very long nets: three passes, pins re-read (cached)
-        const float2 x = pin_xy(j, pos, s + p);
-        hx = fmaxf(hx, x.x); lx = fminf(lx, x.x);
-        hy = fmaxf(hy, x.y); ly = fminf(ly, x.y);
-    }
-    hx = wmax(hx); lx = wmin(lx); hy = wmax(hy); ly = wmin(ly);
-    for (int p = lane; p < d; p += 32) {
-        const float2 x = pin_xy(j, pos, s + p);
-        const float epx = __expf((x.x - hx) * ig), enx = __expf((lx - x.x) * ig);
-        const float epy = __expf((x.y - hy) * ig), eny = __expf((ly - x.y) * ig);
-        m.spx += epx; m.snx += enx; m.xpx += x.x * epx; m.xnx += x.x * enx;
-        m.spy += epy; m.sny += eny; m.xpy += x.y * epy; m.xny += x.y * eny;
-    }
-    m.spx = wsum(m.spx); m.snx = wsum(m.snx); m.xpx = wsum(m.xpx); m.xnx = wsum(m.xnx);
-    m.spy = wsum(m.spy); m.sny = wsum(m.sny); m.xpy = wsum(m.xpy); m.xny = wsum(m.xny);
-    const float xpx = m.xpx / m.spx, xnx = m.xnx / m.snx, xpy = m.xpy / m.spy, xny = m.xny / m.sny;
-    for (int p = lane; p < d; p += 32) {
-        const float2 x = pin_xy(j, pos, s + p);
-        const float epx = __expf((x.x - hx) * ig), enx = __expf((lx - x.x) * ig);
-        const float epy = __expf((x.y - hy) * ig), eny = __expf((ly - x.y) * ig);
-        float gx = epx * (1.f + (x.x - xpx) * ig) / m.spx - enx * (1.f - (x.x - xnx) * ig) / m.snx;
-        float gy = epy * (1.f + (x.y - xpy) * ig) / m.spy - eny * (1.f - (x.y - xny) * ig) / m.sny;
-        j.pin_grad[s + p] = make_float2(gx, gy);
-    }
-    wa = (xpx - xnx) + (xpy - xny);
-    hp = (hx - lx) + (hy - ly);
+    wa = (c.xpx - c.xnx) + (c.xpy - c.xny);
+    hp = (n.hx - n.lx) + (n.hy - n.ly);
 }
 
-// A warp takes 32 consecutive nets: nets of up to WA_REG pins one per lane, then every longer one by the whole
-// warp. Works for nets in any order; with nets sorted by degree (the fused path) the lanes of a warp do equal work.
 __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
     const int lane = threadIdx.x & 31;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long chunks = (j.split + 31) / 32, items = chunks + (j.num_nets - j.split);
     double wa_sum = 0.0, hp_sum = 0.0;
-    for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c * 32 < j.num_nets;
-         c += nwarps) {
-        const int i = (int)(c * 32) + lane;
+    for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
+        if (it >= chunks) {                              // one long net
+            const int i = j.split + (int)(it - chunks);
+            const int s = j.net_start[i], d = j.net_start[i + 1] - s;
+            float wa, hp;
+            net_warp(j, pos, ig, s, d, lane, wa, hp);
+            if (lane == 0) {
+                if (j.out) j.out[i] = make_float2(wa, hp);
+                wa_sum += (double)wa;
+                hp_sum += (double)hp;
+            }
+            continue;
+        }
+        const int i = (int)(it * 32) + lane;
+        const bool valid = i < j.split;
         int s = 0, d = 0;
-        if (i < j.num_nets) {
+        if (valid) {
             s = j.net_start[i];
             d = j.net_start[i + 1] - s;
         }
-        if (i < j.num_nets && d <= WA_REG) {
+        if (valid && d <= WA_REG) {
             float wa, hp;
             net_thread(j, pos, ig, s, d, wa, hp);
             if (j.out) j.out[i] = make_float2(wa, hp);
             wa_sum += (double)wa;
             hp_sum += (double)hp;
         }
-        unsigned big = __ballot_sync(0xffffffffu, i < j.num_nets && d > WA_REG);
+        unsigned big = __ballot_sync(0xffffffffu, valid && d > WA_REG);
         while (big) {
             const int src = __ffs(big) - 1;
             big &= big - 1;
@@ -191,7 +209,8 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
 }
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
-    wa_net_kernel<<<grid_for(j.num_nets, 256, 8), 256, 0, s>>>(j);
+    const long long items = (j.split + 31) / 32 + (j.num_nets - j.split);
+    wa_net_kernel<<<grid_for(items * 32, 256, 8), 256, 0, s>>>(j);
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -27,18 +27,31 @@ SK = {n: i for i, n in enumerate(S_FIELDS)}
 REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handover"}
 
 
-def degree_order(net_start, cell_pin):
-    """Nets sorted by degree (stable), their pins moved along; cell_pin renumbered so that every cell still sums
-    its pins in the original order. -> (pin permutation, new net_start, new cell_pin)."""
+SHORT_NET = 8          # nets of up to this many pins are done one per thread (WA_REG of the kernel)
+
+
+def net_order(net_start, cell32, cell_pin):
+    """The device order of the optimised nets: short nets (<= SHORT_NET pins) first, in classes of 2, 3 and 4..8
+    pins so that a warp's lanes do equal work, each class ordered by the net's lowest cell (nearby nets gather
+    nearby cells); the long nets after them (one warp each). Pins move with their nets.
+    -> (pin permutation: new position -> old pin, new net_start, slot: new pin position -> its position in cell
+    order (cell_pin order, which every cell sums in), index of the first long net)."""
     ns = np.asarray(net_start, np.int64)
     deg = np.diff(ns)
-    order = np.argsort(deg, kind="stable")
+    n = len(deg)
+    if n == 0:
+        return np.zeros(0, np.int64), np.zeros(1, np.int32), np.zeros(0, np.int32), 0
+    first = np.minimum.reduceat(np.asarray(cell32, np.int64), ns[:-1]) if len(cell32) else np.zeros(n, np.int64)
+    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, 3)))
+    order = np.lexsort((first, cls))
     lens = deg[order]
     new_start = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
     perm = np.repeat(ns[:-1][order] - new_start[:-1], lens) + np.arange(int(new_start[-1]))
     newpos = np.empty_like(perm)
     newpos[perm] = np.arange(len(perm))
-    return perm, new_start.astype(np.int32), newpos[np.asarray(cell_pin, np.int64)].astype(np.int32)
+    slot = np.empty(len(perm), np.int64)
+    slot[newpos[np.asarray(cell_pin, np.int64)]] = np.arange(len(perm))
+    return perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum())
 
 
 class Placer(object):
@@ -56,7 +69,7 @@ class Placer(object):
         t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev))
         z = lambda shape, dt: self._hold(torch.zeros(shape, dtype=dt, device=dev))
         cs = prob.csr
-        perm, net_start, cell_pin = degree_order(cs.net_start, cs.cell_pin)
+        perm, net_start, slot, split = net_order(cs.net_start, cs.cell32, cs.cell_pin)
         n, f, judge = prob.num_nodes, prob.force, prob.judge
         P = len(perm)
         sz = Sizes()
@@ -69,9 +82,9 @@ class Placer(object):
         self.pin_off = t(cs.off[perm], torch.float32)
         self.net_start = t(net_start, torch.int32)
         self.cell_start = t(cs.cell_start, torch.int32)
-        self.cell_pin = t(cell_pin, torch.int32)
+        self.pin_slot = t(slot, torch.int32)
         pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
-        pl.cell_start, pl.cell_pin = self._p(self.cell_start), self._p(self.cell_pin)
+        pl.cell_start, pl.pin_slot, pl.net_split = self._p(self.cell_start), self._p(self.pin_slot), split
         self.size, self.ratio = t(f.size, torch.float32), t(f.ratio, torch.float32)
         self.pins, self.area = t(prob.pins, torch.float32), t(prob.area, torch.float32)
         self.lo, self.hi = t(f.pos_lo, torch.float32), t(f.pos_hi, torch.float32)

@@ -33,6 +33,7 @@ class Plan(ctypes.Structure):
         ("u", _vp * 2), ("v", _vp * 2), ("g", _vp * 2), ("best", _vp), ("cur", _vp),
         ("S", _vp), ("T", _vp), ("kp", _vp), ("c", _vp),
         ("pin_grad", _vp), ("map", _vp), ("jmap", _vp), ("red", _vp), ("counters", _vp),
+        ("pin_slot", _vp), ("net_split", _i),
     ]
 
 

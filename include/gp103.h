@@ -143,6 +143,10 @@ typedef struct {
     unsigned long long* jmap; /* [jnbx, jnby], zero between passes */
     double* red;              /* gp103_plan_sizes(...).red doubles */
     unsigned int* counters;   /* 16, zero */
+    /* layout of the pin gradients: when pin_slot is given, the gradient of pin p is stored at pin_slot[p], the
+     * position of p in cell order (cell_start ranges), and cell_pin is not read */
+    const int* pin_slot;
+    int net_split;            /* nets [net_split, num_nets) are long: one warp each (num_nets: any order) */
 } gp103_plan;
 
 typedef struct {

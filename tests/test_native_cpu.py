@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from autoplace_gb300 import native, problem, synth
-from autoplace_gb300.engine import degree_order
+from autoplace_gb300.engine import SHORT_NET, net_order
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -58,18 +58,29 @@ def test_argument_errors_without_gpu():
     assert L.gp103_select(None, None, None, None, None, None, None, None, 0, None) == native.ERR_ARG
 
 
-def test_degree_order_keeps_nets_and_cell_sums():
+def test_net_order_keeps_nets_and_cell_sums():
     nl = synth.make_netlist(3000, 3100, window=60, macros=3, cover=0.1, fixed_pin_share=0.05, seed=4)
     cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
-    perm, ns, cp = degree_order(cs.net_start, cs.cell_pin)
+    perm, ns, slot, split = net_order(cs.net_start, cs.cell32, cs.cell_pin)
     deg = np.diff(ns)
-    assert np.all(np.diff(deg) >= 0)                       # nets by degree
+    assert np.all(deg[:split] <= SHORT_NET) and np.all(deg[split:] > SHORT_NET)
+    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, 3)))
+    assert np.all(np.diff(cls) >= 0)                       # classes in order
     assert sorted(perm.tolist()) == list(range(len(perm)))  # a permutation of the pins
-    # every net keeps its pins, in order
-    old = np.diff(cs.net_start)
-    order = np.argsort(old, kind="stable")
-    for k in range(0, len(order), 97):
-        i = order[k]
+    assert sorted(slot.tolist()) == list(range(len(slot)))
+    # every net keeps its pins, in order: the new nets are the old ones, each once
+    old_of_new = perm[ns[:-1]]
+    starts = set(cs.net_start[:-1].tolist())
+    assert set(old_of_new.tolist()) == starts
+    for k in range(0, len(deg), 97):
+        i = int(np.searchsorted(cs.net_start, perm[ns[k]]))
         assert np.array_equal(perm[ns[k]:ns[k + 1]], np.arange(cs.net_start[i], cs.net_start[i + 1]))
-    # a cell sums the same pins in the same order
-    assert np.array_equal(perm[cp], cs.cell_pin)
+    # the pin at new position q sits at slot[q] in cell order, which lists the old pins as cell_pin does
+    cell_order = np.empty(len(perm), np.int64)
+    cell_order[slot] = perm
+    assert np.array_equal(cell_order, cs.cell_pin)
+    # short nets of one class are ordered by their lowest cell
+    first = np.minimum.reduceat(cs.cell32[perm], ns[:-1])
+    for c in range(3):
+        f = first[cls == c]
+        assert np.all(np.diff(f) >= 0)
