@@ -138,8 +138,8 @@ __global__ void post_mirror_kernel(const unsigned long long* map, const float* f
     const int nb = nbx * nby;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int bx = b / nby, by = b - bx * nby, w = 2 * nby, mx = 2 * nbx - 1 - bx, my = w - 1 - by;
-        const float mov = __fadd_rn((float)((double)map[b] / DENSITY_SCALE), fixed[b]);
-        const float r = __fadd_rn(mov, (float)((double)map[nb + b] / DENSITY_SCALE));
+        const float mov = __fadd_rn(unfixed32(map[b]), fixed[b]);
+        const float r = __fadd_rn(mov, unfixed32(map[nb + b]));
         over[b] = fmaxf(__fsub_rn(mov, target), 0.f);
         rho[(size_t)bx * w + by] = r;
         rho[(size_t)bx * w + my] = r;
@@ -175,14 +175,14 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     const int bid = second ? (int)blockIdx.x - pair.blocks0 : (int)blockIdx.x;
     const int nblk = second ? (int)gridDim.x - pair.blocks0 : pair.blocks0;
     const int nb = j.nbx * j.nby;
-    double ov = 0.0;
+    float ov = 0.f;
     for (int b = bid * blockDim.x + threadIdx.x; b < nb; b += nblk * blockDim.x) {
         const unsigned long long m0 = j.map[b];
-        const float mov = __fadd_rn((float)((double)m0 / DENSITY_SCALE), j.fixed[b]);
-        ov += (double)fmaxf(__fsub_rn(mov, j.target), 0.f);
+        const float mov = __fadd_rn(unfixed32(m0), j.fixed[b]);
+        ov += fmaxf(__fsub_rn(mov, j.target), 0.f);
         if (j.with_fill) {
             const unsigned long long m1 = j.map[nb + b];
-            const float r = __fadd_rn(mov, (float)((double)m1 / DENSITY_SCALE));
+            const float r = __fadd_rn(mov, unfixed32(m1));
             if (j.dens) j.dens[b] = r;
             if (j.t0) split_bf16(r, j.terms, j.t0, j.t1, j.t2, b);
             j.map[nb + b] = 0ull;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     float weight = j.weight_p ? j.weight_p[0] : j.weight;
     float precond = j.precond_p ? j.precond_p[0] : j.precond;
     const bool density = j.ex != nullptr;
-    double d2 = 0.0, l1 = 0.0;
+    float d2 = 0.f, l1 = 0.f;                  // per-thread partials (a few nodes); float64 above
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.num_nodes; i += gridDim.x * blockDim.x) {
         float gx = 0.f, gy = 0.f;
         if (density) {
@@ -306,10 +306,10 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
         gout[i] = g;
         if (gref) {
             const float2 o = gref[i];
-            const double dx = (double)g.x - (double)o.x, dy = (double)g.y - (double)o.y;
+            const float dx = g.x - o.x, dy = g.y - o.y;
             d2 += dx * dx + dy * dy;
         }
-        if (i < j.num_mov) l1 += fabs((double)g.x) + fabs((double)g.y);
+        if (i < j.num_mov) l1 += fabsf(g.x) + fabsf(g.y);
     }
     double v[2] = {d2, l1};
     grid_sum<2>(v, j.red);

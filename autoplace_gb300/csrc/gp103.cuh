@@ -120,9 +120,29 @@ __device__ __forceinline__ Span span(float centre, float size, float inv_bin, in
 __device__ __forceinline__ float overlap(const Span& s, int b) {
     return fmaxf(__fsub_rn(fminf(s.hi, __fadd_rn((float)b, 1.f)), fmaxf(s.lo, (float)b)), 0.f);
 }
+// trunc(f * 2^32) as a 64-bit integer, exactly what (unsigned long long)((double)f * 2^32) gives (the double holds
+// f and the product exactly; the conversion truncates and saturates, NaN and negatives give 0), from the bits of f:
+// f = m 2^(e - 150) with a 24-bit m, so f 2^32 = m 2^(e - 118). Integer work only (GB300's float64 rate is 1/64 of
+// its float32 rate).
+__device__ __forceinline__ unsigned long long fixed32(float f) {
+    const unsigned int b = __float_as_uint(f);
+    if (b & 0x80000000u) return 0ull;                              // negative (or -0, -NaN)
+    const int e = (int)(b >> 23);
+    if (e == 0xff) return (b & 0x7fffffu) ? 0ull : ~0ull;          // NaN -> 0, +inf saturates
+    if (e == 0) return 0ull;                                       // zero / denormal: below 2^-32
+    const unsigned long long m = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+    const int sh = e - 118;
+    if (sh >= 0) return sh > 40 ? ~0ull : (m << sh);
+    return sh <= -24 ? 0ull : (m >> -sh);
+}
 // Fixed-point charge of one (node, bin) pair: trunc(float(wx * oy) * 2^32).
-__device__ __forceinline__ unsigned long long charge(float wx, float oy) {
-    return (unsigned long long)((double)__fmul_rn(wx, oy) * DENSITY_SCALE);
+__device__ __forceinline__ unsigned long long charge(float wx, float oy) { return fixed32(__fmul_rn(wx, oy)); }
+
+// (float)((double)q / 2^32) of a map entry, without float64 when q < 2^53 (then the double is exact and one
+// rounding to float is all there is).
+__device__ __forceinline__ float unfixed32(unsigned long long q) {
+    if (q < (1ull << 53)) return __ull2float_rn(q) * 2.3283064365386963e-10f;      // x 2^-32, exact
+    return (float)((double)q / DENSITY_SCALE);
 }
 
 }  // namespace gp103

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
     const float alpha = j.kp[3], coef = j.kp[4];
     const bool copy_best = j.best && j.S && j.S[S_IS_BEST] != 0;
     const float2 *lo = (const float2*)j.lo, *hi = (const float2*)j.hi;
-    double d2 = 0.0;
+    float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], ui = u[i], l = lo[i], h = hi[i];
         const float ux = fmaf(-alpha, gi.x, vi.x), uy = fmaf(-alpha, gi.y, vi.y);
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
         un_out[i] = make_float2(ux, uy);
         vn_out[i] = make_float2(vx, vy);
         if (copy_best) ((float2*)j.best)[i] = vi;
-        const double dx = (double)vx - (double)vi.x, dy = (double)vy - (double)vi.y;
+        const float dx = vx - vi.x, dy = vy - vi.y;
         d2 += dx * dx + dy * dy;
     }
     double r[1] = {d2};
@@ -172,13 +172,13 @@ int launch_step(const StepJob& j, cudaStream_t s) {
 // probe = clamp(v - step g, lo, hi); |probe - v|^2
 __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step, int n,
                              float2* probe, Reduce red) {
-    double d2 = 0.0;
+    float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], l = lo[i], h = hi[i];
         const float px = fminf(fmaxf(fmaf(-step, gi.x, vi.x), l.x), h.x);
         const float py = fminf(fmaxf(fmaf(-step, gi.y, vi.y), l.y), h.y);
         probe[i] = make_float2(px, py);
-        const double dx = (double)px - vi.x, dy = (double)py - vi.y;
+        const float dx = px - vi.x, dy = py - vi.y;
         d2 += dx * dx + dy * dy;
     }
     double r[1] = {d2};

@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
     const int lane = threadIdx.x & 31;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
     const long long chunks = (j.split + 31) / 32, items = chunks + (j.num_nets - j.split);
-    double wa_sum = 0.0, hp_sum = 0.0;
+    float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float64 above
     for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
         if (it >= chunks) {                              // one long net
             const int i = j.split + (int)(it - chunks);
@@ -169,8 +169,8 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
             net_warp(j, pos, ig, s, d, lane, wa, hp);
             if (lane == 0) {
                 if (j.out) j.out[i] = make_float2(wa, hp);
-                wa_sum += (double)wa;
-                hp_sum += (double)hp;
+                wa_sum += wa;
+                hp_sum += hp;
             }
             continue;
         }
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
             float wa, hp;
             net_thread(j, pos, ig, s, d, wa, hp);
             if (j.out) j.out[i] = make_float2(wa, hp);
-            wa_sum += (double)wa;
-            hp_sum += (double)hp;
+            wa_sum += wa;
+            hp_sum += hp;
         }
         unsigned big = __ballot_sync(0xffffffffu, valid && d > WA_REG);
         while (big) {
@@ -197,8 +197,8 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
             net_warp(j, pos, ig, bs, bd, lane, wa, hp);
             if (lane == src) {
                 if (j.out) j.out[i] = make_float2(wa, hp);
-                wa_sum += (double)wa;
-                hp_sum += (double)hp;
+                wa_sum += wa;
+                hp_sum += hp;
             }
         }
     }
