@@ -71,6 +71,16 @@ __global__ void weight_kernel(int nbx, int nby, double bx, double by, float* wx,
     }
 }
 
+// The separable parts of the weights, for epilogues that form them on the fly: per row p (kx^2, s kx / bin_x, w_p)
+// and per column q (ky^2, s ky / bin_x, w_q), s = 2 / (nbx nby); Wx = (s kx / bin_x) w_q / (kx^2 + ky^2).
+__global__ void weight_table_kernel(int n, int nbx, int nby, double bin, double bx, float4* tab) {
+    const double pi = 3.14159265358979323846;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const double k = pi * p / (n * bin), s = 2.0 / ((double)nbx * nby);
+        tab[p] = make_float4((float)(k * k), (float)(s * k / bx), p == 0 ? 1.f : 2.f, 0.f);
+    }
+}
+
 FieldLayout field_layout(int nbx, int nby, int mode) {
     FieldLayout L;
     L.nbx = nbx;
@@ -84,6 +94,7 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
     L.c_cx = take(xx * es); L.c_cy = take(yy * es); L.c_cyt = take(yy * es);
     L.c_sxt = take(xx * es); L.c_syt = take(yy * es); L.c_cxt = take(xx * es);
     L.c_wx = take(xy * 4); L.c_wy = take(xy * 4);
+    L.c_wrow = take((size_t)nbx * 16); L.c_wcol = take((size_t)nby * 16);
     L.const_bytes = o;
     o = 0;
     L.w_a = take(xy * es); L.w_tt = take(xy * es); L.w_kx = take(xy * es); L.w_ky = take(xy * es);
@@ -109,6 +120,12 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
     }
     weight_kernel<<<grid_for((size_t)L.nbx * L.nby, 256, 8), 256, 0, s>>>(L.nbx, L.nby, L.bx, L.by,
                                                                             (float*)(c + L.c_wx), (float*)(c + L.c_wy));
+    GP103_CHECK_LAUNCH();
+    weight_table_kernel<<<grid_for(L.nbx, 256, 8), 256, 0, s>>>(L.nbx, L.nbx, L.nby, L.bx, L.bx,
+                                                                 (float4*)(c + L.c_wrow));
+    GP103_CHECK_LAUNCH();
+    weight_table_kernel<<<grid_for(L.nby, 256, 8), 256, 0, s>>>(L.nby, L.nbx, L.nby, L.by, L.bx,
+                                                                 (float4*)(c + L.c_wcol));
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -10,7 +10,7 @@ namespace gp103 {
 struct FieldLayout {
     int nbx, nby, mode;
     double bx, by;
-    size_t c_cx, c_cy, c_cyt, c_sxt, c_syt, c_cxt, c_wx, c_wy, const_bytes;
+    size_t c_cx, c_cy, c_cyt, c_sxt, c_syt, c_cxt, c_wx, c_wy, c_wrow, c_wcol, const_bytes;
     size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err, work_bytes;
 };
 

@@ -7,7 +7,8 @@
 // same staged k-block (each term's tile is loaded once per k-block) into one accumulator:
 //   bf16x3: (1,0) (0,1) (0,0)                          ~1e-5 of the max
 //   bf16x6: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)        ~2e-7 of the max (float32-level)
-// Shapes: M, N multiples of 128, K a multiple of 64 (force grids of 128 .. 2048 bins per side).
+// Tiles are 128 rows x BN columns: BN = 64 when a launch has one GEMM (twice the blocks), 128 when it has two.
+// Shapes: M, N multiples of 128, K a multiple of 64 (force grids of 128 .. 4096 bins per side).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -17,10 +18,10 @@
 
 namespace gp103 {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
-constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;                  // 16 KB per operand tile
-constexpr int TC_STAGE_SPACE = 12 * TC_TILE_BYTES;               // 192 KB of stages
-constexpr int TC_MAX_STAGES = 3;
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                     // 16 KB per A term tile
+constexpr int TC_STAGE_SPACE = 216 * 1024;                       // room for the stages
+constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_SMEM = TC_STAGE_SPACE + 1024 + 256;
 constexpr long long TC_WAIT_NS = 2000000000LL;                  // a wait that takes 2 s has failed
 
@@ -30,7 +31,8 @@ struct TcProblem {
     __nv_bfloat16* o_terms;      // EPI_TRANS: [3][N][M]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
     __nv_bfloat16* o2_terms;
     float* out_f32;              // EPI_PLAIN: [M][N]
-    const float* w0; const float* w1;
+    const float4* wrow;          // EPI_WEIGHT2: per row p (kx^2, s kx / bin_x, w_p, 0)
+    const float4* wcol;          //              per column q (ky^2, s ky / bin_x, w_q, 0)
 };
 
 // A stage holds the k-block (64 of K) of every term of A and of B that the products read: na A tiles, then nb B
@@ -58,6 +60,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -67,7 +72,8 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false (and the error flag set) if the phase did not complete within TC_WAIT_NS.
+// Bounded wait: false (and the error flag set) if the phase did not complete within TC_WAIT_NS, or if another
+// thread already gave up.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = gtime();
@@ -98,14 +104,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor: D float32, A and B bf16, both K-major, M = 128, N = TC_BN.
-constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
-                              ((uint32_t)(TC_BM >> 4) << 24);
+// Instruction descriptor: D float32, A and B bf16, both K-major, M = 128, N = BN.
+template <int BN>
+__device__ __forceinline__ constexpr uint32_t idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
 
+template <int BN>
 __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem), "l"(a), "l"(b), "r"(TC_IDESC), "r"(accumulate));
+        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<BN>()), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -143,11 +152,13 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16&
 // accumulator (two, alternating) and the readers add it into float32 registers with round-to-nearest; the error
 // then stays at float32 level (~2e-7) at every grid size.
 constexpr int TC_THREADS = 192;
-constexpr int TC_TMEM_COLS = 2 * TC_BN;
 
+template <int BN, int EPI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
                    const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1, TcArgs args) {
+    constexpr int B_TILE = BN * TC_BK * 2;
+    constexpr uint32_t TMEM_COLS = 2 * BN;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     // barriers: full[S], empty[S], acc_full[2], acc_empty[2]
@@ -158,9 +169,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const TcProblem& P = args.p[z];
     const CUtensorMap* ma = z ? &a1 : &a0;
     const CUtensorMap* mb = z ? &b1 : &b0;
-    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
     const int total = P.K / TC_BK, stages = args.stages;
-    const int stage_bytes = (args.na + args.nb) * TC_TILE_BYTES;
+    const int stage_bytes = args.na * TC_A_TILE + args.nb * B_TILE;
     int* err = args.err;
     auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
     auto empty_bar = [&](int s) { return smem_u32(&bars[TC_MAX_STAGES + s]); };
@@ -180,7 +191,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(TC_TMEM_COLS));
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
@@ -197,9 +208,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mbar_expect_tx(full_bar(s), stage_bytes);
                 uint8_t* st = smem + s * stage_bytes;
                 for (int t = 0; t < args.na; t++)
-                    tma_load_3d(smem_u32(st + t * TC_TILE_BYTES), ma, full_bar(s), it * TC_BK, m0, t);
+                    tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
                 for (int t = 0; t < args.nb; t++)
-                    tma_load_3d(smem_u32(st + (args.na + t) * TC_TILE_BYTES), mb, full_bar(s), it * TC_BK, n0, t);
+                    tma_load_3d(smem_u32(st + args.na * TC_A_TILE + t * B_TILE), mb, full_bar(s), it * TC_BK, n0, t);
             }
         }
     } else if (warp == 1) {
@@ -211,32 +222,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (!mbar_wait(full_bar(s), ph, err, 3)) break;
                 tc_fence_after();
                 const uint32_t st = smem_u32(smem + s * stage_bytes);
-                const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+                const uint32_t acc = tmem + (uint32_t)(b * BN);
                 for (int q = 0; q < args.nprod; q++) {
-                    const uint32_t sa = st + args.prod_a[q] * TC_TILE_BYTES;
-                    const uint32_t sb = st + (args.na + args.prod_b[q]) * TC_TILE_BYTES;
+                    const uint32_t sa = st + args.prod_a[q] * TC_A_TILE;
+                    const uint32_t sb = st + args.na * TC_A_TILE + args.prod_b[q] * B_TILE;
 #pragma unroll
                     for (int kk = 0; kk < TC_BK / 16; kk++)
-                        mma_bf16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (q > 0 || kk > 0) ? 1u : 0u);
+                        mma_bf16<BN>(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (q > 0 || kk > 0) ? 1u : 0u);
                 }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
             }
         }
     } else {                                                     // readers + epilogue
-        const int q = warp & 3;                                  // tensor-memory lane quarter
-        const int row = m0 + q * 32 + lane;
-        float r[TC_BN];
+        const int q4 = warp & 3;                                 // tensor-memory lane quarter
+        const int row = m0 + q4 * 32 + lane;
+        float r[BN];
 #pragma unroll
-        for (int i = 0; i < TC_BN; i++) r[i] = 0.f;
+        for (int i = 0; i < BN; i++) r[i] = 0.f;
         bool ok = true;
         for (int it = 0; it < total && ok; it++) {
             const int b = it & 1;
             if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN);
+            const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll
-            for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+            for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
                 tmem_ld32(base + (uint32_t)c0, v);
 #pragma unroll
@@ -244,19 +255,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acce_bar(b)) : "memory");
+            if (lane == 0) mbar_arrive(acce_bar(b));
         }
         ok = ok && *(volatile int*)err == 0;
         if (ok) {
             const int col = n0;
-            if (P.epi == EPI_PLAIN) {
+            if (EPI == EPI_PLAIN) {
                 float4* o = (float4*)(P.out_f32 + (size_t)row * P.N + col);
 #pragma unroll
-                for (int i = 0; i < TC_BN / 4; i++) o[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
-            } else if (P.epi == EPI_TRANS) {
+                for (int i = 0; i < BN / 4; i++) o[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
+            } else if (EPI == EPI_TRANS) {
                 const size_t plane = (size_t)P.M * P.N;
 #pragma unroll
-                for (int i = 0; i < TC_BN; i++) {
+                for (int i = 0; i < BN; i++) {
                     __nv_bfloat16 a, bb, c;
                     split3(r[i], a, bb, c);
                     const size_t at = (size_t)(col + i) * P.M + row;
@@ -265,23 +276,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     P.o_terms[2 * plane + at] = c;
                 }
             } else {
+                // Kx = K Wx, Ky = K Wy with Wx = (s kx_p / bin_x) w_q r, Wy = (s ky_q / bin_x) w_p r,
+                // r = 1 / (kx_p^2 + ky_q^2) (0 at p = q = 0), from per-row and per-column tables
                 const size_t plane = (size_t)P.M * P.N;
                 const size_t base = (size_t)row * P.N + col;
+                const float4 wr = P.wrow[row];
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const float* w = (h ? P.w1 : P.w0) + base;
-                    __nv_bfloat16* o = (h ? P.o2_terms : P.o_terms) + base;
+                for (int c0 = 0; c0 < BN; c0 += 32) {
+                    __align__(16) __nv_bfloat16 xa[32], xb[32], xc[32], ya[32], yb[32], yc[32];
 #pragma unroll
-                    for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-                        __align__(16) __nv_bfloat16 ta[32], tb[32], tcv[32];
+                    for (int i = 0; i < 32; i++) {
+                        const float4 wc = P.wcol[col + c0 + i];
+                        const float t = wr.x + wc.x;
+                        const float rr = t > 0.f ? __frcp_rn(t) : 0.f;
+                        split3(r[c0 + i] * (wr.y * wc.z * rr), xa[i], xb[i], xc[i]);
+                        split3(r[c0 + i] * (wc.y * wr.z * rr), ya[i], yb[i], yc[i]);
+                    }
+                    __nv_bfloat16* ox = P.o_terms + base + c0;
+                    __nv_bfloat16* oy = P.o2_terms + base + c0;
 #pragma unroll
-                        for (int i = 0; i < 32; i++) split3(r[c0 + i] * __ldg(w + c0 + i), ta[i], tb[i], tcv[i]);
-#pragma unroll
-                        for (int i = 0; i < 4; i++) {
-                            ((uint4*)(o + c0))[i] = ((uint4*)ta)[i];
-                            ((uint4*)(o + plane + c0))[i] = ((uint4*)tb)[i];
-                            ((uint4*)(o + 2 * plane + c0))[i] = ((uint4*)tcv)[i];
-                        }
+                    for (int i = 0; i < 4; i++) {
+                        ((uint4*)ox)[i] = ((uint4*)xa)[i];
+                        ((uint4*)(ox + plane))[i] = ((uint4*)xb)[i];
+                        ((uint4*)(ox + 2 * plane))[i] = ((uint4*)xc)[i];
+                        ((uint4*)oy)[i] = ((uint4*)ya)[i];
+                        ((uint4*)(oy + plane))[i] = ((uint4*)yb)[i];
+                        ((uint4*)(oy + 2 * plane))[i] = ((uint4*)yc)[i];
                     }
                 }
             }
@@ -291,7 +311,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
     }
 }
 
@@ -309,13 +329,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// Three bf16 planes [3][rows][K] as a 3-D tensor (K, rows, term); box = 64 x 128 x 1.
-static bool make_map(CUtensorMap* m, const void* base, int rows, int K) {
+// Three bf16 planes [3][rows][K] as a 3-D tensor (K, rows, term); box = 64 x box_rows x 1.
+static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows) {
     auto fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
     cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
-    cuuint32_t box[3] = {TC_BK, TC_BM, 1};
+    cuuint32_t box[3] = {TC_BK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -333,10 +353,12 @@ struct TcOp {
     TcProblem p;
 };
 
-static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+template <int BN, int EPI>
+static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) != cudaSuccess)
+        if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
+            cudaSuccess)
             return GP103_ERR_CUDA;
         attr = true;
     }
@@ -344,7 +366,7 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     TcArgs args = {};
     for (int z = 0; z < 2; z++) {
         const TcOp& o = ops[z < nops ? z : 0];
-        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K) || !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K))
+        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM) || !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, BN))
             return GP103_ERR_CUDA;
         args.p[z] = o.p;
     }
@@ -353,7 +375,7 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     const bool x3 = mode == GP103_FIELD_BF16X3;
     args.na = args.nb = x3 ? 2 : 3;
     args.nprod = x3 ? 3 : 6;
-    args.stages = TC_STAGE_SPACE / ((args.na + args.nb) * TC_TILE_BYTES);
+    args.stages = TC_STAGE_SPACE / (args.na * TC_A_TILE + args.nb * BN * TC_BK * 2);
     if (args.stages > TC_MAX_STAGES) args.stages = TC_MAX_STAGES;
     for (int i = 0; i < args.nprod; i++) {
         args.prod_a[i] = x3 ? x3a[i] : x6a[i];
@@ -361,10 +383,21 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     }
     args.err = err;
     const TcProblem& p = ops[0].p;
-    dim3 grid(p.N / TC_BN, p.M / TC_BM, nops);
-    tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
+    dim3 grid(p.N / BN, p.M / TC_BM, nops);
+    tc_gemm_kernel<BN, EPI><<<grid, TC_THREADS, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
     GP103_CHECK_LAUNCH();
     return GP103_OK;
+}
+
+// One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles. The epilogue is a
+// template argument (every problem of a launch has the same one).
+static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+    const int epi = ops[0].p.epi;
+    if (nops == 1 && epi == EPI_TRANS) return launch_tc_bn<64, EPI_TRANS>(ops, nops, mode, err, s);
+    if (nops == 1 && epi == EPI_WEIGHT2) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
+    if (nops == 2 && epi == EPI_TRANS) return launch_tc_bn<128, EPI_TRANS>(ops, nops, mode, err, s);
+    if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
+    return GP103_ERR_ARG;                                        // no other combination is used
 }
 
 __global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t) {
@@ -403,8 +436,8 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
     o2.p.o_terms = B(w, L.w_kx);
     o2.p.o2_terms = B(w, L.w_ky);
-    o2.p.w0 = (const float*)(c + L.c_wx);
-    o2.p.w1 = (const float*)(c + L.c_wy);
+    o2.p.wrow = (const float4*)(c + L.c_wrow);
+    o2.p.wcol = (const float4*)(c + L.c_wcol);
     if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
     // 3a / 4a: Pt = (Kx Cy)^T, Qt = (Ky Sy)^T
     TcOp o3[2] = {{B(w, L.w_kx), X, B(c, L.c_cyt), Y, prob(X, Y, Y, EPI_TRANS)},

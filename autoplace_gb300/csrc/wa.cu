@@ -84,25 +84,26 @@ struct Coef {
     }
 };
 
-// A net of d <= WA_REG pins by one thread.
+// A net of d <= R pins by one thread (R = d for the exact-degree forms).
+template <int R>
 __device__ __forceinline__ void net_thread(const WaJob& j, const float2* pos, float ig, int s, int d, float& wa,
                                            float& hp) {
     Net n;
     n.init();
-    float2 x[WA_REG];
+    float2 x[R];
 #pragma unroll
-    for (int k = 0; k < WA_REG; k++)
+    for (int k = 0; k < R; k++)
         if (k < d) {
             x[k] = pin_xy(j, pos, s + k);
             n.extent(x[k]);
         }
 #pragma unroll
-    for (int k = 0; k < WA_REG; k++)
+    for (int k = 0; k < R; k++)
         if (k < d) n.add(x[k], ig);
     Coef c;
     c.from(n);
 #pragma unroll
-    for (int k = 0; k < WA_REG; k++)
+    for (int k = 0; k < R; k++)
         if (k < d) {
             const float2 g = c.grad(n, x[k], ig);
             put(j, s + k, g.x, g.y);
@@ -182,8 +183,12 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
             d = j.net_start[i + 1] - s;
         }
         if (valid && d <= WA_REG) {
+            // the code of an exact degree for the common 2- and 3-pin nets (the predicated general form issues the
+            // instructions of WA_REG pins); warps of the ordered layout take one branch
             float wa, hp;
-            net_thread(j, pos, ig, s, d, wa, hp);
+            if (d == 2) net_thread<2>(j, pos, ig, s, d, wa, hp);
+            else if (d == 3) net_thread<3>(j, pos, ig, s, d, wa, hp);
+            else net_thread<WA_REG>(j, pos, ig, s, d, wa, hp);
             if (j.out) j.out[i] = make_float2(wa, hp);
             wa_sum += wa;
             hp_sum += hp;
