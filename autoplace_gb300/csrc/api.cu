@@ -18,6 +18,17 @@ using namespace gp103;
         if (st_) return st_;             \
     } while (0)
 
+// ------------------------------------------------------------------------------------------------ options
+static int g_pdl = 1;
+bool gp103::pdl_enabled() { return g_pdl != 0; }
+
+extern "C" int gp103_set_option(int option, int value) {
+    switch (option) {
+        case GP103_OPT_PDL: g_pdl = value != 0; return GP103_OK;
+        default: return GP103_ERR_ARG;
+    }
+}
+
 // ------------------------------------------------------------------------------------------------ launch accounting
 static unsigned long long g_launches = 0;
 static struct {

@@ -33,6 +33,7 @@ __device__ __forceinline__ void add_shared(unsigned int* lo, unsigned int* hi, i
 }
 
 __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_constant__ ScatterPair pair) {
+    pdl_wait();
     __shared__ unsigned int tlo[SCAT_SMEM_BINS], thi[SCAT_SMEM_BINS];
     __shared__ int box[4];
     const bool second = (int)blockIdx.x >= pair.blocks0;
@@ -126,7 +127,7 @@ int launch_scatter(const ScatterJob* jobs, int njobs, cudaStream_t s) {
     p.blocks0 = scatter_blocks(jobs[0]);
     const int blocks = p.blocks0 + (njobs > 1 ? scatter_blocks(jobs[1]) : 0);
     if (blocks == 0) return GP103_OK;
-    scatter_kernel<<<blocks, SCAT_THREADS, 0, s>>>(p);
+    if (launch_k(scatter_kernel, dim3(blocks), dim3(SCAT_THREADS), 0, s, p) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -135,6 +136,7 @@ int launch_scatter(const ScatterJob* jobs, int njobs, cudaStream_t s) {
 // Reference layout: rho mirrored [2 nbx][2 nby] and over [nbx][nby] (density_post_kernel, gp_cuda_kernel.cu:130-139).
 __global__ void post_mirror_kernel(const unsigned long long* map, const float* fixed, float target, int nbx, int nby,
                                    float* rho, float* over) {
+    pdl_wait();
     const int nb = nbx * nby;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int bx = b / nby, by = b - bx * nby, w = 2 * nby, mx = 2 * nbx - 1 - bx, my = w - 1 - by;
@@ -151,7 +153,7 @@ __global__ void post_mirror_kernel(const unsigned long long* map, const float* f
 int launch_post_mirror(const unsigned long long* map, const float* fixed, float target, int nbx, int nby, float* rho,
                        float* over, cudaStream_t s) {
     const int nb = nbx * nby;
-    post_mirror_kernel<<<grid_for(nb, 256, 8), 256, 0, s>>>(map, fixed, target, nbx, nby, rho, over);
+    if (launch_k(post_mirror_kernel, dim3(grid_for(nb, 256, 8)), dim3(256), 0, s, map, fixed, target, nbx, nby, rho, over) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -170,19 +172,41 @@ __device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0
 }
 
 __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
+    pdl_wait();
     const bool second = (int)blockIdx.x >= pair.blocks0;
     const PostJob& j = second ? pair.j[1] : pair.j[0];
     const int bid = second ? (int)blockIdx.x - pair.blocks0 : (int)blockIdx.x;
     const int nblk = second ? (int)gridDim.x - pair.blocks0 : pair.blocks0;
     const int nb = j.nbx * j.nby;
     float ov = 0.f;
-    for (int b = bid * blockDim.x + threadIdx.x; b < nb; b += nblk * blockDim.x) {
-        const unsigned long long m0 = j.map[b];
-        const float mov = __fadd_rn(unfixed32(m0), j.fixed[b]);
+    // two bins per thread and iteration: 16-byte map loads / stores (an even bin count keeps both planes 16-byte
+    // aligned; an odd one takes the scalar loop below for every bin)
+    const int pairs = (nb & 1) ? 0 : nb >> 1;
+    ulonglong2* map2 = (ulonglong2*)j.map;
+    for (int q = bid * blockDim.x + threadIdx.x; q < pairs; q += nblk * blockDim.x) {
+        const int b = 2 * q;
+        const ulonglong2 m0 = map2[q];
+        const float2 fx = *(const float2*)(j.fixed + b);
+        const float mov0 = __fadd_rn(unfixed32(m0.x), fx.x), mov1 = __fadd_rn(unfixed32(m0.y), fx.y);
+        ov += fmaxf(__fsub_rn(mov0, j.target), 0.f) + fmaxf(__fsub_rn(mov1, j.target), 0.f);
+        if (j.with_fill) {
+            ulonglong2* fill2 = (ulonglong2*)(j.map + nb);
+            const ulonglong2 m1 = fill2[q];
+            const float r0 = __fadd_rn(mov0, unfixed32(m1.x)), r1 = __fadd_rn(mov1, unfixed32(m1.y));
+            if (j.dens) *(float2*)(j.dens + b) = make_float2(r0, r1);
+            if (j.t0) {
+                split_bf16(r0, j.terms, j.t0, j.t1, j.t2, b);
+                split_bf16(r1, j.terms, j.t0, j.t1, j.t2, b + 1);
+            }
+            fill2[q] = make_ulonglong2(0ull, 0ull);
+        }
+        map2[q] = make_ulonglong2(0ull, 0ull);
+    }
+    for (int b = (nb & 1) ? bid * blockDim.x + threadIdx.x : nb; b < nb; b += nblk * blockDim.x) {
+        const float mov = __fadd_rn(unfixed32(j.map[b]), j.fixed[b]);
         ov += fmaxf(__fsub_rn(mov, j.target), 0.f);
         if (j.with_fill) {
-            const unsigned long long m1 = j.map[nb + b];
-            const float r = __fadd_rn(mov, unfixed32(m1));
+            const float r = __fadd_rn(mov, unfixed32(j.map[nb + b]));
             if (j.dens) j.dens[b] = r;
             if (j.t0) split_bf16(r, j.terms, j.t0, j.t1, j.t2, b);
             j.map[nb + b] = 0ull;
@@ -200,7 +224,7 @@ int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s) {
     p.njobs = njobs;
     p.blocks0 = grid_for((long long)jobs[0].nbx * jobs[0].nby, 256, 4);
     const int blocks = p.blocks0 + (njobs > 1 ? grid_for((long long)jobs[1].nbx * jobs[1].nby, 256, 4) : 0);
-    post_plain_kernel<<<blocks, 256, 0, s>>>(p);
+    if (launch_k(post_plain_kernel, dim3(blocks), dim3(256), 0, s, p) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -211,6 +235,7 @@ __global__ void gather_mirror_kernel(const float2* pos, const float2* size, cons
                                      const float2* wl_grad, const float* pins, const float* area, int num_nodes,
                                      int num_wl, const float* weight_p, const float* precond_p, float inv_bx,
                                      float inv_by, int nbx, int nby, float2* grad) {
+    pdl_wait();
     const float weight = *weight_p, precond = *precond_p;
     const float* fy = field + (size_t)4 * nbx * nby;
     const int ld = 2 * nby;
@@ -244,9 +269,8 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
                          const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,
                          cudaStream_t s) {
     if (num_nodes == 0) return GP103_OK;
-    gather_mirror_kernel<<<grid_for(num_nodes, 256, 8), 256, 0, s>>>(
-        (const float2*)pos, (const float2*)size, ratio, field, (const float2*)wl_grad, pins, area, num_nodes, num_wl,
-        weight, precond, 1.f / bx, 1.f / by, nbx, nby, (float2*)grad);
+    if (launch_k(gather_mirror_kernel, dim3(grid_for(num_nodes, 256, 8)), dim3(256), 0, s, (const float2*)pos, (const float2*)size, ratio, field, (const float2*)wl_grad, pins, area, num_nodes, num_wl,
+        weight, precond, 1.f / bx, 1.f / by, nbx, nby, (float2*)grad) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -256,6 +280,7 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
 // through cell_pin); the new gradient, its squared distance to the previous one and its L1 norm over the cells
 // reduced in float64.
 __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
+    pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     float2* gout = pick_mut(j.gout_a, j.gout_b, j.sel);
     const float2* gref = j.gref_a ? pick_ref(j.gref_a, j.gref_b, j.sel) : nullptr;
@@ -316,7 +341,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
 }
 
 int launch_gather(const GatherJob& j, cudaStream_t s) {
-    gather_kernel<<<grid_for(j.num_nodes, 256, 8), 256, 0, s>>>(j);
+    if (launch_k(gather_kernel, dim3(grid_for(j.num_nodes, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

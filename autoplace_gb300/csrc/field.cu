@@ -39,6 +39,7 @@ __device__ __forceinline__ double trig(int kind, int p, int u, int n) {
 // what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]
 __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t0, __nv_bfloat16* t1,
                                    __nv_bfloat16* t2, size_t plane) {
+    pdl_wait();
     const size_t total = (size_t)n * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const int r = (int)(e / n), col = (int)(e % n);
@@ -59,6 +60,7 @@ __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t
 }
 
 __global__ void weight_kernel(int nbx, int nby, double bx, double by, float* wx, float* wy) {
+    pdl_wait();
     const size_t total = (size_t)nbx * nby;
     const double pi = 3.14159265358979323846;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -74,6 +76,7 @@ __global__ void weight_kernel(int nbx, int nby, double bx, double by, float* wx,
 // The separable parts of the weights, for epilogues that form them on the fly: per row p (kx^2, s kx / bin_x, w_p)
 // and per column q (ky^2, s ky / bin_x, w_q), s = 2 / (nbx nby); Wx = (s kx / bin_x) w_q / (kx^2 + ky^2).
 __global__ void weight_table_kernel(int n, int nbx, int nby, double bin, double bx, float4* tab) {
+    pdl_wait();
     const double pi = 3.14159265358979323846;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const double k = pi * p / (n * bin), s = 2.0 / ((double)nbx * nby);
@@ -114,18 +117,18 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
         const size_t plane = (size_t)m.n * m.n;
         float* f = fp32 ? (float*)(c + m.off) : nullptr;
         __nv_bfloat16* t0 = fp32 ? nullptr : (__nv_bfloat16*)(c + m.off);
-        trig_matrix_kernel<<<grid_for(plane, 256, 8), 256, 0, s>>>(m.what, m.n, f, t0, t0 ? t0 + plane : nullptr,
-                                                                      t0 ? t0 + 2 * plane : nullptr, plane);
+        if (launch_k(trig_matrix_kernel, dim3(grid_for(plane, 256, 8)), dim3(256), 0, s, m.what, m.n, f, t0, t0 ? t0 + plane : nullptr,
+                                                                      t0 ? t0 + 2 * plane : nullptr, plane) != cudaSuccess) return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
-    weight_kernel<<<grid_for((size_t)L.nbx * L.nby, 256, 8), 256, 0, s>>>(L.nbx, L.nby, L.bx, L.by,
-                                                                            (float*)(c + L.c_wx), (float*)(c + L.c_wy));
+    if (launch_k(weight_kernel, dim3(grid_for((size_t)L.nbx * L.nby, 256, 8)), dim3(256), 0, s, L.nbx, L.nby, L.bx, L.by,
+                                                                            (float*)(c + L.c_wx), (float*)(c + L.c_wy)) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
-    weight_table_kernel<<<grid_for(L.nbx, 256, 8), 256, 0, s>>>(L.nbx, L.nbx, L.nby, L.bx, L.bx,
-                                                                 (float4*)(c + L.c_wrow));
+    if (launch_k(weight_table_kernel, dim3(grid_for(L.nbx, 256, 8)), dim3(256), 0, s, L.nbx, L.nbx, L.nby, L.bx, L.bx,
+                                                                 (float4*)(c + L.c_wrow)) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
-    weight_table_kernel<<<grid_for(L.nby, 256, 8), 256, 0, s>>>(L.nby, L.nbx, L.nby, L.by, L.bx,
-                                                                 (float4*)(c + L.c_wcol));
+    if (launch_k(weight_table_kernel, dim3(grid_for(L.nby, 256, 8)), dim3(256), 0, s, L.nby, L.nbx, L.nby, L.by, L.bx,
+                                                                 (float4*)(c + L.c_wcol)) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -135,6 +138,7 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
 constexpr int SG_BM = 64, SG_BN = 64, SG_BK = 16;
 
 __global__ void __launch_bounds__(256) sgemm_kernel(SGemm g) {
+    pdl_wait();
     __shared__ float As[SG_BK][SG_BM + 4];
     __shared__ float Bs[SG_BK][SG_BN + 4];
     const int m0 = blockIdx.y * SG_BM, n0 = blockIdx.x * SG_BN;
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(256) sgemm_kernel(SGemm g) {
 
 int launch_sgemm(const SGemm& g, cudaStream_t s) {
     dim3 grid(ceil_div(g.N, SG_BN), ceil_div(g.M, SG_BM));
-    sgemm_kernel<<<grid, 256, 0, s>>>(g);
+    if (launch_k(sgemm_kernel, dim3(grid), dim3(256), 0, s, g) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

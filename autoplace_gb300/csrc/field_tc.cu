@@ -157,6 +157,7 @@ template <int BN, int EPI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
                    const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1, TcArgs args) {
+    pdl_wait();
     constexpr int B_TILE = BN * TC_BK * 2;
     constexpr uint32_t TMEM_COLS = 2 * BN;
     extern __shared__ uint8_t smem_raw[];
@@ -384,7 +385,7 @@ static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStrea
     args.err = err;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / BN, p.M / TC_BM, nops);
-    tc_gemm_kernel<BN, EPI><<<grid, TC_THREADS, TC_SMEM, s>>>(maps[0], maps[1], maps[2], maps[3], args);
+    if (launch_k(tc_gemm_kernel<BN, EPI>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2], maps[3], args) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -401,6 +402,7 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
 }
 
 __global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t) {
+    pdl_wait();
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
         __nv_bfloat16 a, b, c;
         split3(d[e], a, b, c);
@@ -420,7 +422,7 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     int* err = (int*)(w + L.w_err);
     int st;
     if (density) {
-        split_density_kernel<<<grid_for((size_t)X * Y, 256, 8), 256, 0, s>>>(density, (size_t)X * Y, B(w, L.w_a));
+        if (launch_k(split_density_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density, (size_t)X * Y, B(w, L.w_a)) != cudaSuccess) return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
     auto prob = [](int M, int N, int K, int epi) {

@@ -16,6 +16,31 @@
 namespace gp103 {
 
 int after_launch(cudaStream_t s, const char* name);
+bool pdl_enabled();
+
+// Programmatic dependent launch: a kernel may be launched while the one before it on the stream is finishing; it
+// waits here (at its very start, before touching any data) until that one has completed and its writes are
+// visible. Without the launch attribute this is a no-op. A kernel signals, once its blocks are past their main
+// work, that the next one may start launching.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launch with the programmatic-serialization attribute (when enabled): successive kernels of a pass overlap their
+// launch with the tail of the previous kernel; in a captured graph the edges become programmatic edges.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
 
 constexpr double DENSITY_SCALE = 4294967296.0;     // fixed point of the density map: 2^32 per bin area
 constexpr int SMS = 152;                           // GB300: 2 dies x 76 SMs
@@ -70,6 +95,7 @@ template <int K>
 __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r, int nblk, int bid) {
     __shared__ double sh[K * 32];
     __shared__ bool last;
+    pdl_trigger();                          // the main work is done: the next kernel may start launching
     block_sum<K>(v, sh);
     if (threadIdx.x == 0) {
 #pragma unroll

@@ -15,6 +15,7 @@ namespace gp103 {
 // ----------------------------------------------------------------------------- reference-layout kernels
 __global__ void nesterov_step_kernel(const float* u, const float* v, const float* g, const float* lo, const float* hi,
                                      const float* alpha_p, const float* coef_p, int n, float* u_next, float* v_next) {
+    pdl_wait();
     const float alpha = *alpha_p, coef = *coef_p;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float un = fmaf(-alpha, g[i], v[i]);
@@ -26,7 +27,7 @@ __global__ void nesterov_step_kernel(const float* u, const float* v, const float
 int launch_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,
                          const float* alpha, const float* coef, int n, float* u_next, float* v_next, cudaStream_t s) {
     if (n == 0) return GP103_OK;
-    nesterov_step_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(u, v, g, lo, hi, alpha, coef, n, u_next, v_next);
+    if (launch_k(nesterov_step_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, u, v, g, lo, hi, alpha, coef, n, u_next, v_next) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -107,18 +108,20 @@ __device__ bool control_body(double* S, float* kp, const double* c, double moved
 
 __global__ void control_kernel(double* S, float* kp, const double* c, const float* moved, const float* turned,
                                const float* hpwl, const float* ovf, const float* wa) {
+    pdl_wait();
     control_body(S, kp, c, *moved, *turned, *hpwl, *ovf, *wa);
 }
 
 int launch_control(double* S, float* kp, const double* c, const float* moved, const float* turned, const float* hpwl,
                    const float* ovf, const float* wa, cudaStream_t s) {
-    control_kernel<<<1, 1, 0, s>>>(S, kp, c, moved, turned, hpwl, ovf, wa);
+    if (launch_k(control_kernel, dim3(1), dim3(1), 0, s, S, kp, c, moved, turned, hpwl, ovf, wa) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
 
 __global__ void select_kernel(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
                               const float* g_next, float* best, int n) {
+    pdl_wait();
     if (S[S_ACCEPT] == 0) return;
     const bool is_best = S[S_IS_BEST] != 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -132,7 +135,7 @@ __global__ void select_kernel(const double* S, float* u, float* v, float* g, con
 int launch_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
                   const float* g_next, float* best, int n, cudaStream_t s) {
     if (n == 0) return GP103_OK;
-    select_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(S, u, v, g, u_next, v_next, g_next, best, n);
+    if (launch_k(select_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, S, u, v, g, u_next, v_next, g_next, best, n) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -141,6 +144,7 @@ int launch_select(const double* S, float* u, float* v, float* g, const float* u_
 // u' = v - alpha g, v' = clamp(u' + coef (u' - u)) from the current buffers into the other ones, |v' - v|^2 in
 // float64; the best placement of the previous pass (S[is_best]) is copied on the way.
 __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
+    pdl_wait();
     const int c = j.cur ? *j.cur : 0;
     const float2 *u = (const float2*)j.u[c], *v = (const float2*)j.v[c], *g = (const float2*)j.g[c];
     float2 *un_out = (float2*)j.u[1 - c], *vn_out = (float2*)j.v[1 - c];
@@ -148,7 +152,25 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
     const bool copy_best = j.best && j.S && j.S[S_IS_BEST] != 0;
     const float2 *lo = (const float2*)j.lo, *hi = (const float2*)j.hi;
     float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.n; i += gridDim.x * blockDim.x) {
+    // two nodes (four coordinates) per iteration with 16-byte accesses when the node count is even
+    const int quads = (j.n & 1) ? 0 : j.n >> 1;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += gridDim.x * blockDim.x) {
+        const float4 vi = ((const float4*)v)[q], gi = ((const float4*)g)[q], ui = ((const float4*)u)[q];
+        const float4 l = ((const float4*)lo)[q], h = ((const float4*)hi)[q];
+        float4 un, vn;
+        un.x = fmaf(-alpha, gi.x, vi.x); un.y = fmaf(-alpha, gi.y, vi.y);
+        un.z = fmaf(-alpha, gi.z, vi.z); un.w = fmaf(-alpha, gi.w, vi.w);
+        vn.x = fminf(fmaxf(fmaf(coef, un.x - ui.x, un.x), l.x), h.x);
+        vn.y = fminf(fmaxf(fmaf(coef, un.y - ui.y, un.y), l.y), h.y);
+        vn.z = fminf(fmaxf(fmaf(coef, un.z - ui.z, un.z), l.z), h.z);
+        vn.w = fminf(fmaxf(fmaf(coef, un.w - ui.w, un.w), l.w), h.w);
+        ((float4*)un_out)[q] = un;
+        ((float4*)vn_out)[q] = vn;
+        if (copy_best) ((float4*)j.best)[q] = vi;
+        const float dx = vn.x - vi.x, dy = vn.y - vi.y, dz = vn.z - vi.z, dw = vn.w - vi.w;
+        d2 += (dx * dx + dy * dy) + (dz * dz + dw * dw);
+    }
+    for (int i = (j.n & 1) ? blockIdx.x * blockDim.x + threadIdx.x : j.n; i < j.n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], ui = u[i], l = lo[i], h = hi[i];
         const float ux = fmaf(-alpha, gi.x, vi.x), uy = fmaf(-alpha, gi.y, vi.y);
         const float vx = fminf(fmaxf(fmaf(coef, ux - ui.x, ux), l.x), h.x);
@@ -164,7 +186,7 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
 }
 
 int launch_step(const StepJob& j, cudaStream_t s) {
-    step_kernel<<<grid_for(j.n, 256, 8), 256, 0, s>>>(j);
+    if (launch_k(step_kernel, dim3(grid_for(j.n, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -172,6 +194,7 @@ int launch_step(const StepJob& j, cudaStream_t s) {
 // probe = clamp(v - step g, lo, hi); |probe - v|^2
 __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step, int n,
                              float2* probe, Reduce red) {
+    pdl_wait();
     float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], l = lo[i], h = hi[i];
@@ -187,8 +210,8 @@ __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo,
 
 int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
                  Reduce red, cudaStream_t s) {
-    probe_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>((const float2*)v, (const float2*)g, (const float2*)lo,
-                                                      (const float2*)hi, step, n, (float2*)probe, red);
+    if (launch_k(probe_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, (const float2*)v, (const float2*)g, (const float2*)lo,
+                                                      (const float2*)hi, step, n, (float2*)probe, red) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -197,13 +220,14 @@ int launch_probe(const float* v, const float* g, const float* lo, const float* h
 __global__ void control_fused_kernel(double* S, float* kp, const double* c, const double* moved2,
                                      const double* turned2, const double* wa_hpwl, const double* ovf_sum,
                                      double ovf_scale, int* cur) {
+    pdl_wait();
     const double ovf = ovf_sum[0] * ovf_scale;
     if (control_body(S, kp, c, sqrt(moved2[0]), sqrt(turned2[0]), wa_hpwl[1], ovf, wa_hpwl[0])) *cur = 1 - *cur;
 }
 
 int launch_control_fused(double* S, float* kp, const double* c, const double* moved2, const double* turned2,
                          const double* wa_hpwl, const double* ovf_sum, double ovf_scale, int* cur, cudaStream_t s) {
-    control_fused_kernel<<<1, 1, 0, s>>>(S, kp, c, moved2, turned2, wa_hpwl, ovf_sum, ovf_scale, cur);
+    if (launch_k(control_fused_kernel, dim3(1), dim3(1), 0, s, S, kp, c, moved2, turned2, wa_hpwl, ovf_sum, ovf_scale, cur) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -212,6 +236,7 @@ int launch_control_fused(double* S, float* kp, const double* c, const double* mo
 // test (the WA fell by less than start_tol per iteration over the last 5), in float64.
 __global__ void control_start_kernel(double* T, float* kp, const double* moved2, const double* turned2,
                                      const double* wa_hpwl, int* cur) {
+    pdl_wait();
     T[GP103_T_ACCEPT] = 0;
     if (T[GP103_T_STOP] != 0 || T[GP103_T_DONE] != 0) return;
     const double moved = sqrt(moved2[0]), turned = sqrt(turned2[0]), wa = wa_hpwl[0], hpwl = wa_hpwl[1];
@@ -243,13 +268,14 @@ __global__ void control_start_kernel(double* T, float* kp, const double* moved2,
 
 int launch_control_start(double* T, float* kp, const double* moved2, const double* turned2, const double* wa_hpwl,
                          int* cur, cudaStream_t s) {
-    control_start_kernel<<<1, 1, 0, s>>>(T, kp, moved2, turned2, wa_hpwl, cur);
+    if (launch_k(control_start_kernel, dim3(1), dim3(1), 0, s, T, kp, moved2, turned2, wa_hpwl, cur) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
 
 __global__ void finish_kernel(const double* S, const int* cur, float* const* v_unused, const float* v0, const float* v1,
                               float* best, int n) {
+    pdl_wait();
     if (S[S_IS_BEST] == 0) return;
     const float* v = *cur ? v1 : v0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) best[i] = v[i];
@@ -258,13 +284,14 @@ __global__ void finish_kernel(const double* S, const int* cur, float* const* v_u
 int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
                   cudaStream_t s) {
     if (n == 0) return GP103_OK;
-    finish_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(S, cur, nullptr, v0, v1, best, n);
+    if (launch_k(finish_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, S, cur, nullptr, v0, v1, best, n) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
 
 __global__ void copy_doubles_kernel(const double* a, int na, const double* b, int nb, const double* c, int nc,
                                     double* out) {
+    pdl_wait();
     int k = 0;
     for (int i = 0; i < na; i++) out[k++] = a[i];
     for (int i = 0; i < nb; i++) out[k++] = b[i];
@@ -273,7 +300,7 @@ __global__ void copy_doubles_kernel(const double* a, int na, const double* b, in
 
 int launch_gather_scalars(const double* a, int na, const double* b, int nb, const double* c, int nc, double* out,
                           cudaStream_t s) {
-    copy_doubles_kernel<<<1, 1, 0, s>>>(a, na, b, nb, c, nc, out);
+    if (launch_k(copy_doubles_kernel, dim3(1), dim3(1), 0, s, a, na, b, nb, c, nc, out) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -155,7 +155,8 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
     hp = (n.hx - n.lx) + (n.hy - n.ly);
 }
 
-__global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
+__global__ void __launch_bounds__(256, 3) wa_net_kernel(WaJob j) {
+    pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
     const int lane = threadIdx.x & 31;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(256) wa_net_kernel(WaJob j) {
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const long long items = (j.split + 31) / 32 + (j.num_nets - j.split);
-    wa_net_kernel<<<grid_for(items * 32, 256, 8), 256, 0, s>>>(j);
+    if (launch_k(wa_net_kernel, dim3(grid_for(items * 32, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -223,6 +224,7 @@ int launch_wa_net(const WaJob& j, cudaStream_t s) {
 // One thread per cell: its pins' gradients in cell_pin order (the reference's fixed order).
 __global__ void wa_cell_kernel(const float2* pin_grad, const int* cell_start, const int* cell_pin, int num_mov,
                                float2* grad) {
+    pdl_wait();
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < num_mov; c += gridDim.x * blockDim.x) {
         float gx = 0.f, gy = 0.f;
         for (int k = cell_start[c]; k < cell_start[c + 1]; k++) {
@@ -237,7 +239,7 @@ __global__ void wa_cell_kernel(const float2* pin_grad, const int* cell_start, co
 int launch_wa_cell(const float2* pin_grad, const int* cell_start, const int* cell_pin, int num_mov, float2* grad,
                    cudaStream_t s) {
     if (num_mov == 0) return GP103_OK;
-    wa_cell_kernel<<<grid_for(num_mov, 256, 8), 256, 0, s>>>(pin_grad, cell_start, cell_pin, num_mov, grad);
+    if (launch_k(wa_cell_kernel, dim3(grid_for(num_mov, 256, 8)), dim3(256), 0, s, pin_grad, cell_start, cell_pin, num_mov, grad) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -45,6 +45,7 @@ _SIGS = {
     "gp103_version": ([], _i),
     "gp103_status_string": ([_i], ctypes.c_char_p),
     "gp103_launch_count": ([], ctypes.c_ulonglong),
+    "gp103_set_option": ([_i, _i], _i),
     "gp103_profile_begin": ([_vp], _i),
     "gp103_profile_end": ([ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), _i], _i),
     "gp103_wa": ([_vp] * 6 + [_i, _i] + [_vp] * 4 + [_vp], _i),

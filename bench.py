@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--cpu-iters", type=int, default=4, help="density-phase iterations of the CPU sample")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-pdl", action="store_true", help="plain stream order instead of programmatic dependent launch")
     return p.parse_args()
 
 
@@ -249,11 +250,11 @@ def roofline(prob, field, prof, peaks):
                "ms_per_launch": round(ml, 4)}
         if k in by:
             row["gbs"] = round(by[k] / (ml * 1e-3) / 1e9, 1)
-        if k == "launch_tc":
+        if k == "launch_tc_bn":
             f = tc_flops(prob, field) * (6.0 / v["launches_per_pass"])
             row["tflops"] = round(f / (ml * 1e-3) / 1e12, 1)
         table[k] = row
-    if name == "launch_tc":
+    if name == "launch_tc_bn":
         f = tc_flops(prob, field) * (6.0 / d["launches_per_pass"])
         ach = f / (ms_launch * 1e-3) / 1e12
         r = {"kernel": "tc_gemm_kernel", "bound": "tensor", "achieved": round(ach, 1), "peak": tc,
@@ -282,6 +283,9 @@ def run_gb300(args):
     import torch
     from autoplace_gb300.engine import Placer
     rank, world, local = dist_setup()
+    if args.no_pdl:
+        from autoplace_gb300 import native
+        native.call("gp103_set_option", 0, 0)
     prob, pos0 = workload(args.config, seed=rank)
     placer = Placer(prob, field=args.field)
     dpos = torch.tensor(pos0, device="cuda")

@@ -31,6 +31,12 @@ enum {
 int gp103_version(void);
 const char* gp103_status_string(int status);
 
+/* Process-wide options. GP103_OPT_PDL (default 1): launch with programmatic dependent launch, so that each kernel of
+ * a pass is launched while the previous one finishes (and graph edges become programmatic edges); 0 = plain
+ * stream order. */
+enum { GP103_OPT_PDL = 0 };
+int gp103_set_option(int option, int value);
+
 /* Kernel launches issued through this library so far (a launch captured into a CUDA graph counts once). */
 unsigned long long gp103_launch_count(void);
 
