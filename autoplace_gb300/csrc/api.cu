@@ -365,9 +365,9 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream
     g.gref_a = (const float2*)p->g[0];
     g.gref_b = (const float2*)p->g[1];
     g.with_wl = 1;
-    double* r_moved = reduce_out(p->red, R_MOVED);
-    double* r_grad = reduce_out(p->red, R_GRAD);
-    double* r_wa = reduce_out(p->red, R_WA);
+    const Reduce r_moved = reduce_slot(p->red, p->counters, R_MOVED);
+    const Reduce r_grad = reduce_slot(p->red, p->counters, R_GRAD);
+    const Reduce r_wa = reduce_slot(p->red, p->counters, R_WA);
     if (phase == GP103_PHASE_START) {
         TRY(launch_gather(g, stream));
         return launch_control_start(p->T, p->kp, r_moved, r_grad, r_wa, p->cur, stream);
@@ -378,7 +378,7 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream
     g.weight_p = p->kp + 1;
     g.precond_p = p->kp + 2;
     TRY(launch_gather(g, stream));
-    const double* ovf = reduce_out(p->red, p->jnbx > 0 ? R_JOVF : R_OVF);
+    const Reduce ovf = reduce_slot(p->red, p->counters, p->jnbx > 0 ? R_JOVF : R_OVF);
     const double scale = p->jnbx > 0 ? p->jovf_scale : p->ovf_scale;
     return launch_control_fused(p->S, p->kp, p->c, r_moved, r_grad, r_wa, ovf, scale, p->cur, stream);
 }
@@ -406,12 +406,13 @@ extern "C" int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out
         g.precond = (float)precond;
     }
     TRY(launch_gather(g, stream));
-    const double* r_wa = reduce_out(p->red, R_WA);
-    const double* r_grad = reduce_out(p->red, R_GRAD);
-    const double* ovf = reduce_out(p->red, p->jnbx > 0 ? R_JOVF : R_OVF);
+    const Reduce r_wa = reduce_slot(p->red, p->counters, R_WA);
+    const Reduce r_grad = reduce_slot(p->red, p->counters, R_GRAD);
+    const Reduce ovf = reduce_slot(p->red, p->counters, p->jnbx > 0 ? R_JOVF : R_OVF);
     // out5 = (|g - g_ref|^2, WA, HPWL, overflow sum, L1 of g over the cells)
-    TRY(launch_gather_scalars(r_grad, 1, r_wa, 2, ovf, 1, out5, stream));
-    return launch_gather_scalars(r_grad + 1, 1, nullptr, 0, nullptr, 0, out5 + 4, stream);
+    const Reduce rs[5] = {r_grad, r_wa, r_wa, ovf, r_grad};
+    const int ks[5] = {0, 0, 1, 0, 1};
+    return launch_totals(rs, ks, 5, out5, stream);
 }
 
 extern "C" int gp103_probe(const gp103_plan* plan, const float* v, const float* g, double step, float* probe,
@@ -420,7 +421,8 @@ extern "C" int gp103_probe(const gp103_plan* plan, const float* v, const float* 
     REQUIRE(v && g && probe && out1 && plan->lo && plan->hi);
     Reduce r = reduce_slot(plan->red, plan->counters, R_MOVED);
     TRY(launch_probe(v, g, plan->lo, plan->hi, (float)step, plan->num_nodes, probe, r, stream));
-    return launch_gather_scalars(r.out, 1, nullptr, 0, nullptr, 0, out1, stream);
+    const int k0 = 0;
+    return launch_totals(&r, &k0, 1, out1, stream);
 }
 
 extern "C" int gp103_finish(const gp103_plan* plan, cudaStream_t stream) {

@@ -57,12 +57,13 @@ inline int grid_for(long long n, int threads, int per_sm) {
 }
 
 // ----------------------------------------------------------------------------- deterministic float64 reductions
-// Per-block partial sums in a fixed slot per block; the last block to finish adds the partials in block order.
-// The result does not depend on which block finishes last: bit-identical on every run.
+// A producing kernel writes one partial sum per block, in a fixed slot per block (no atomics, no "last block"
+// tail); the kernel that consumes the value adds the partials in block order with a whole block. The result does
+// not depend on the scheduling of the blocks: bit-identical on every run.
+constexpr int MAX_BLOCKS = 2048;
 struct Reduce {
-    double* partials;       // [K][max_blocks]
-    unsigned int* counter;  // one counter, zero between uses (the last block resets it)
-    double* out;            // [K]
+    double* partials;       // [K][MAX_BLOCKS]
+    int* count;             // number of partials, written by block 0 of the producer
 };
 
 template <int K>
@@ -90,41 +91,38 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sh) {
     }
 }
 
-// The blocks taking part are numbered bid = 0 .. nblk - 1 (a launch may hold several independent reductions).
+// Producer side: the blocks taking part are numbered bid = 0 .. nblk - 1 (<= MAX_BLOCKS; a launch may hold several
+// independent reductions).
 template <int K>
 __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r, int nblk, int bid) {
     __shared__ double sh[K * 32];
-    __shared__ bool last;
     pdl_trigger();                          // the main work is done: the next kernel may start launching
     block_sum<K>(v, sh);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; k++) r.partials[(size_t)k * nblk + bid] = v[k];
-        __threadfence();
-        unsigned int t = atomicAdd(r.counter, 1u);
-        last = (t == (unsigned int)nblk - 1);
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        double s[K];
-#pragma unroll
-        for (int k = 0; k < K; k++) s[k] = 0.0;
-        for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-#pragma unroll
-            for (int k = 0; k < K; k++) s[k] += __ldcg(r.partials + (size_t)k * nblk + b);
-        block_sum<K>(s, sh);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int k = 0; k < K; k++) r.out[k] = s[k];
-            *r.counter = 0;
-        }
+        for (int k = 0; k < K; k++) r.partials[(size_t)k * MAX_BLOCKS + bid] = v[k];
+        if (bid == 0) *r.count = nblk;
     }
 }
 
 template <int K>
 __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
     grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
+}
+
+// Consumer side (every thread of the block calls it): value k of a reduction, returned to every thread.
+__device__ __forceinline__ double block_total(const Reduce& r, int k) {
+    __shared__ double sh[32];
+    __shared__ double total;
+    const int n = *r.count;
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < n; b += blockDim.x) v[0] += r.partials[(size_t)k * MAX_BLOCKS + b];
+    block_sum<1>(v, sh);
+    if (threadIdx.x == 0) total = v[0];
+    __syncthreads();
+    const double t = total;
+    __syncthreads();
+    return t;
 }
 
 // ----------------------------------------------------------------------------- node span on a bin grid

@@ -22,18 +22,16 @@ __device__ __forceinline__ const T* pick_ref(const T* a, const T* b, const int* 
     return sel == nullptr ? a : (*sel ? b : a);
 }
 
-// Reduction slots of a plan's `red` buffer (float64): each has K <= 4 values, MAX_BLOCKS partials per value.
-constexpr int MAX_BLOCKS = 2048;
+// Reduction slots of a plan's `red` buffer (float64): each has K <= 4 values, MAX_BLOCKS partials per value; the
+// partial counts live in the plan's `counters`.
 enum { R_WA = 0, R_OVF, R_JOVF, R_MOVED, R_GRAD, R_COUNT };
 inline Reduce reduce_slot(double* red, unsigned int* counters, int slot) {
     Reduce r;
     r.partials = red + (size_t)slot * 4 * MAX_BLOCKS;
-    r.counter = counters + slot;
-    r.out = red + (size_t)R_COUNT * 4 * MAX_BLOCKS + slot * 4;
+    r.count = (int*)(counters + slot);
     return r;
 }
-inline double* reduce_out(double* red, int slot) { return red + (size_t)R_COUNT * 4 * MAX_BLOCKS + slot * 4; }
-constexpr size_t RED_DOUBLES = (size_t)R_COUNT * 4 * MAX_BLOCKS + R_COUNT * 4;
+constexpr size_t RED_DOUBLES = (size_t)R_COUNT * 4 * MAX_BLOCKS;
 
 struct WaJob {
     const float2* pos_a; const float2* pos_b; const int* sel;
@@ -44,7 +42,7 @@ struct WaJob {
     const float* gamma;
     float2* pin_grad;
     float2* out;            // per-net (WA, HPWL), may be null
-    Reduce red;             // (WA, HPWL) totals; red.out == nullptr: none
+    Reduce red;             // (WA, HPWL) totals; red.partials == nullptr: none
 };
 
 struct ScatterJob {

@@ -216,30 +216,33 @@ int launch_probe(const float* v, const float* g, const float* lo, const float* h
     return GP103_OK;
 }
 
-// The density phase's control from the pass's float64 reductions; an accepted step flips the current buffers.
-__global__ void control_fused_kernel(double* S, float* kp, const double* c, const double* moved2,
-                                     const double* turned2, const double* wa_hpwl, const double* ovf_sum,
-                                     double ovf_scale, int* cur) {
+// The density phase's control: one block adds the pass's float64 partial sums (in block order), then one thread
+// runs the control; an accepted step flips the current buffers.
+__global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp, const double* c, Reduce moved2,
+                                                            Reduce grad, Reduce wa_hpwl, Reduce ovf_sum,
+                                                            double ovf_scale, int* cur) {
     pdl_wait();
-    const double ovf = ovf_sum[0] * ovf_scale;
-    if (control_body(S, kp, c, sqrt(moved2[0]), sqrt(turned2[0]), wa_hpwl[1], ovf, wa_hpwl[0])) *cur = 1 - *cur;
+    const double m2 = block_total(moved2, 0), t2 = block_total(grad, 0);
+    const double wa = block_total(wa_hpwl, 0), hpwl = block_total(wa_hpwl, 1);
+    const double ovf = block_total(ovf_sum, 0) * ovf_scale;
+    if (threadIdx.x == 0 && control_body(S, kp, c, sqrt(m2), sqrt(t2), hpwl, ovf, wa)) *cur = 1 - *cur;
 }
 
-int launch_control_fused(double* S, float* kp, const double* c, const double* moved2, const double* turned2,
-                         const double* wa_hpwl, const double* ovf_sum, double ovf_scale, int* cur, cudaStream_t s) {
-    if (launch_k(control_fused_kernel, dim3(1), dim3(1), 0, s, S, kp, c, moved2, turned2, wa_hpwl, ovf_sum, ovf_scale, cur) != cudaSuccess) return GP103_ERR_CUDA;
+int launch_control_fused(double* S, float* kp, const double* c, Reduce moved2, Reduce grad, Reduce wa_hpwl,
+                         Reduce ovf_sum, double ovf_scale, int* cur, cudaStream_t s) {
+    if (launch_k(control_fused_kernel, dim3(1), dim3(256), 0, s, S, kp, c, moved2, grad, wa_hpwl, ovf_sum, ovf_scale,
+                 cur) != cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
 
 // The wirelength-only start: NesterovOptimizer.step's step length and acceptance, ParamScheduler.start_step's end
 // test (the WA fell by less than start_tol per iteration over the last 5), in float64.
-__global__ void control_start_kernel(double* T, float* kp, const double* moved2, const double* turned2,
-                                     const double* wa_hpwl, int* cur) {
-    pdl_wait();
+__device__ void control_start_body(double* T, float* kp, double moved, double turned, double wa, double hpwl,
+                                   int* cur) {
     T[GP103_T_ACCEPT] = 0;
     if (T[GP103_T_STOP] != 0 || T[GP103_T_DONE] != 0) return;
-    const double moved = sqrt(moved2[0]), turned = sqrt(turned2[0]), wa = wa_hpwl[0], hpwl = wa_hpwl[1];
     if (!(isfinite(moved) && isfinite(turned) && isfinite(hpwl))) {
         T[GP103_T_STOP] = 3;
         return;
@@ -266,9 +269,17 @@ __global__ void control_start_kernel(double* T, float* kp, const double* moved2,
     kp[4] = (float)((an - 1) / ((1 + sqrt(4 * an * an + 1)) / 2));
 }
 
-int launch_control_start(double* T, float* kp, const double* moved2, const double* turned2, const double* wa_hpwl,
-                         int* cur, cudaStream_t s) {
-    if (launch_k(control_start_kernel, dim3(1), dim3(1), 0, s, T, kp, moved2, turned2, wa_hpwl, cur) != cudaSuccess) return GP103_ERR_CUDA;
+__global__ void __launch_bounds__(256) control_start_kernel(double* T, float* kp, Reduce moved2, Reduce grad,
+                                                            Reduce wa_hpwl, int* cur) {
+    pdl_wait();
+    const double m2 = block_total(moved2, 0), t2 = block_total(grad, 0);
+    const double wa = block_total(wa_hpwl, 0), hpwl = block_total(wa_hpwl, 1);
+    if (threadIdx.x == 0) control_start_body(T, kp, sqrt(m2), sqrt(t2), wa, hpwl, cur);
+}
+
+int launch_control_start(double* T, float* kp, Reduce moved2, Reduce grad, Reduce wa_hpwl, int* cur, cudaStream_t s) {
+    if (launch_k(control_start_kernel, dim3(1), dim3(256), 0, s, T, kp, moved2, grad, wa_hpwl, cur) != cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -289,18 +300,29 @@ int launch_finish(const double* S, const int* cur, const float* v0, const float*
     return GP103_OK;
 }
 
-__global__ void copy_doubles_kernel(const double* a, int na, const double* b, int nb, const double* c, int nc,
-                                    double* out) {
+// out[i] = value k[i] of reduction r[i] (i < n <= 8): the scalars of an evaluation, for the host.
+struct Totals {
+    Reduce r[8];
+    int k[8];
+    int n;
+};
+
+__global__ void __launch_bounds__(256) totals_kernel(Totals t, double* out) {
     pdl_wait();
-    int k = 0;
-    for (int i = 0; i < na; i++) out[k++] = a[i];
-    for (int i = 0; i < nb; i++) out[k++] = b[i];
-    for (int i = 0; i < nc; i++) out[k++] = c[i];
+    for (int i = 0; i < t.n; i++) {
+        const double v = block_total(t.r[i], t.k[i]);
+        if (threadIdx.x == 0) out[i] = v;
+    }
 }
 
-int launch_gather_scalars(const double* a, int na, const double* b, int nb, const double* c, int nc, double* out,
-                          cudaStream_t s) {
-    if (launch_k(copy_doubles_kernel, dim3(1), dim3(1), 0, s, a, na, b, nb, c, nc, out) != cudaSuccess) return GP103_ERR_CUDA;
+int launch_totals(const Reduce* r, const int* k, int n, double* out, cudaStream_t s) {
+    Totals t = {};
+    for (int i = 0; i < n && i < 8; i++) {
+        t.r[i] = r[i];
+        t.k[i] = k[i];
+    }
+    t.n = n < 8 ? n : 8;
+    if (launch_k(totals_kernel, dim3(1), dim3(256), 0, s, t, out) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

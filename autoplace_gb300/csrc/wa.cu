@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256, 3) wa_net_kernel(WaJob j) {
             }
         }
     }
-    if (j.red.out) {
+    if (j.red.partials) {
         double v[2] = {wa_sum, hp_sum};
         grid_sum<2>(v, j.red);
     }
