@@ -110,6 +110,30 @@ __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
     grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
 }
 
+// Consumer side (every thread of the block calls it): N totals at once (value k[i] of reduction r[i]), returned to
+// every thread; one sweep over the partials and one block-wide tree.
+template <int N>
+__device__ __forceinline__ void block_totals(const Reduce (&r)[N], const int (&k)[N], double (&out)[N]) {
+    __shared__ double sh[N * 32];
+    __shared__ double tot[N];
+    double v[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        v[i] = 0.0;
+        const int n = *r[i].count;
+        const double* p = r[i].partials + (size_t)k[i] * MAX_BLOCKS;
+        for (int b = threadIdx.x; b < n; b += blockDim.x) v[i] += p[b];
+    }
+    block_sum<N>(v, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int i = 0; i < N; i++) tot[i] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; i++) out[i] = tot[i];
+    __syncthreads();
+}
+
 // Consumer side (every thread of the block calls it): value k of a reduction, returned to every thread.
 __device__ __forceinline__ double block_total(const Reduce& r, int k) {
     __shared__ double sh[32];

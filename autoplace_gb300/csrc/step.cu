@@ -222,10 +222,12 @@ __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp
                                                             Reduce grad, Reduce wa_hpwl, Reduce ovf_sum,
                                                             double ovf_scale, int* cur) {
     pdl_wait();
-    const double m2 = block_total(moved2, 0), t2 = block_total(grad, 0);
-    const double wa = block_total(wa_hpwl, 0), hpwl = block_total(wa_hpwl, 1);
-    const double ovf = block_total(ovf_sum, 0) * ovf_scale;
-    if (threadIdx.x == 0 && control_body(S, kp, c, sqrt(m2), sqrt(t2), hpwl, ovf, wa)) *cur = 1 - *cur;
+    const Reduce r[5] = {moved2, grad, wa_hpwl, wa_hpwl, ovf_sum};
+    const int k[5] = {0, 0, 0, 1, 0};
+    double t[5];
+    block_totals<5>(r, k, t);
+    if (threadIdx.x == 0 && control_body(S, kp, c, sqrt(t[0]), sqrt(t[1]), t[3], t[4] * ovf_scale, t[2]))
+        *cur = 1 - *cur;
 }
 
 int launch_control_fused(double* S, float* kp, const double* c, Reduce moved2, Reduce grad, Reduce wa_hpwl,
@@ -272,9 +274,11 @@ __device__ void control_start_body(double* T, float* kp, double moved, double tu
 __global__ void __launch_bounds__(256) control_start_kernel(double* T, float* kp, Reduce moved2, Reduce grad,
                                                             Reduce wa_hpwl, int* cur) {
     pdl_wait();
-    const double m2 = block_total(moved2, 0), t2 = block_total(grad, 0);
-    const double wa = block_total(wa_hpwl, 0), hpwl = block_total(wa_hpwl, 1);
-    if (threadIdx.x == 0) control_start_body(T, kp, sqrt(m2), sqrt(t2), wa, hpwl, cur);
+    const Reduce r[4] = {moved2, grad, wa_hpwl, wa_hpwl};
+    const int k[4] = {0, 0, 0, 1};
+    double t[4];
+    block_totals<4>(r, k, t);
+    if (threadIdx.x == 0) control_start_body(T, kp, sqrt(t[0]), sqrt(t[1]), t[2], t[3], cur);
 }
 
 int launch_control_start(double* T, float* kp, Reduce moved2, Reduce grad, Reduce wa_hpwl, int* cur, cudaStream_t s) {
