@@ -80,6 +80,8 @@ extern "C" const char* gp103_status_string(int status) {
         case GP103_ERR_ARG: return "invalid argument (null pointer, negative size or empty grid)";
         case GP103_ERR_CUDA: return "a CUDA launch failed";
         case GP103_ERR_SHAPE: return "grid not supported by the tensor-core field (multiples of 128 bins per side)";
+        case GP103_ERR_TOO_LARGE:
+            return "grid larger than the fixed scratch of gp103_density_map_noalloc (nbx * nby <= 262144)";
         default: return "unknown status";
     }
 }

@@ -50,6 +50,7 @@ _SIGS = {
     "gp103_profile_end": ([ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), _i], _i),
     "gp103_wa": ([_vp] * 6 + [_i, _i] + [_vp] * 4 + [_vp], _i),
     "gp103_density_map": ([_vp, _vp, _vp, _i, _i, _f, _f, _i, _i, _vp, _vp, _f, _vp, _vp, _vp], _i),
+    "gp103_density_map_noalloc": ([_vp, _vp, _vp, _i, _i, _f, _f, _i, _i, _vp, _f, _vp, _vp, _vp], _i),
     "gp103_nesterov_step": ([_vp] * 7 + [_i, _vp, _vp, _vp], _i),
     "gp103_density_grad": ([_vp] * 7 + [_i, _i, _vp, _vp, _f, _f, _i, _i, _vp, _vp], _i),
     "gp103_control": ([_vp] * 8 + [_vp], _i),

@@ -24,7 +24,8 @@ enum {
     GP103_OK = 0,
     GP103_ERR_ARG = 1,       /* a size or pointer the kernels cannot take */
     GP103_ERR_CUDA = 2,      /* a launch failed (cudaGetLastError) */
-    GP103_ERR_SHAPE = 3      /* a grid the tensor-core field does not support */
+    GP103_ERR_SHAPE = 3,     /* a grid the tensor-core field does not support */
+    GP103_ERR_TOO_LARGE = 4  /* a grid larger than the fixed scratch of gp103_density_map_noalloc */
 };
 
 /* Library version and the status text of an error code. */
@@ -65,6 +66,18 @@ int gp103_wa(const float* pos, const int* pin_cell, const float* pin_off, const 
 int gp103_density_map(const float* pos, const float* size, const float* ratio, int num_nodes, int num_mov, float bx,
                       float by, int nbx, int nby, unsigned long long* map, const float* fixed, float target,
                       float* rho, float* over, cudaStream_t stream);
+
+/* No counterpart in the reference. The density map of gp103_density_map (same results, bit for bit) for callers
+ * that cannot allocate device memory: e.g. a plugin inside a host application whose device memory belongs to that
+ * application's own pool, or a latency-critical loop that must not call cudaMalloc (it can synchronise the
+ * device). Instead of a caller-provided map it uses a fixed 4 MiB device array inside this library, so grids are
+ * limited to nbx * nby <= 262,144 bins (GP103_ERR_TOO_LARGE beyond, before any work). It allocates nothing: no
+ * cudaMalloc, cudaFree or allocating library call. The first call on a device looks up the array's address
+ * (make it before any stream capture); every call clears the part of the array it uses, all calls share the array,
+ * and calls whose work overlaps on the GPU race on it. */
+int gp103_density_map_noalloc(const float* pos, const float* size, const float* ratio, int num_nodes, int num_mov,
+                              float bx, float by, int nbx, int nby, const float* fixed, float target, float* rho,
+                              float* over, cudaStream_t stream);
 
 /* gp_cuda.nesterov_step (gp_cuda.cpp:51-56; launcher nesterov_step, gp_cuda_kernel.cu:167-170).
  * n floats: u_next = v - alpha g; v_next = clamp(u_next + coef (u_next - u), lo, hi); alpha, coef on the device. */
