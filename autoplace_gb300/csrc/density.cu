@@ -179,30 +179,49 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     const int nblk = second ? (int)gridDim.x - pair.blocks0 : pair.blocks0;
     const int nb = j.nbx * j.nby;
     float ov = 0.f;
-    // two bins per thread and iteration: 16-byte map loads / stores (an even bin count keeps both planes 16-byte
-    // aligned; an odd one takes the scalar loop below for every bin)
-    const int pairs = (nb & 1) ? 0 : nb >> 1;
-    ulonglong2* map2 = (ulonglong2*)j.map;
-    for (int q = bid * blockDim.x + threadIdx.x; q < pairs; q += nblk * blockDim.x) {
-        const int b = 2 * q;
-        const ulonglong2 m0 = map2[q];
-        const float2 fx = *(const float2*)(j.fixed + b);
-        const float mov0 = __fadd_rn(unfixed32(m0.x), fx.x), mov1 = __fadd_rn(unfixed32(m0.y), fx.y);
-        ov += fmaxf(__fsub_rn(mov0, j.target), 0.f) + fmaxf(__fsub_rn(mov1, j.target), 0.f);
+    // four bins per thread and iteration: 32-byte map loads / stores, 8-byte stores of each bf16 term plane (a bin
+    // count that is a multiple of 4 keeps every plane aligned; any other takes the scalar loop below for every bin)
+    const int quads = (nb & 3) ? 0 : nb >> 2;
+    for (int q = bid * blockDim.x + threadIdx.x; q < quads; q += nblk * blockDim.x) {
+        const int b = 4 * q;
+        const ulonglong2 m0a = ((const ulonglong2*)j.map)[2 * q], m0b = ((const ulonglong2*)j.map)[2 * q + 1];
+        const float4 fx = *(const float4*)(j.fixed + b);
+        float mov[4];
+        mov[0] = __fadd_rn(unfixed32(m0a.x), fx.x);
+        mov[1] = __fadd_rn(unfixed32(m0a.y), fx.y);
+        mov[2] = __fadd_rn(unfixed32(m0b.x), fx.z);
+        mov[3] = __fadd_rn(unfixed32(m0b.y), fx.w);
+#pragma unroll
+        for (int k = 0; k < 4; k++) ov += fmaxf(__fsub_rn(mov[k], j.target), 0.f);
         if (j.with_fill) {
-            ulonglong2* fill2 = (ulonglong2*)(j.map + nb);
-            const ulonglong2 m1 = fill2[q];
-            const float r0 = __fadd_rn(mov0, unfixed32(m1.x)), r1 = __fadd_rn(mov1, unfixed32(m1.y));
-            if (j.dens) *(float2*)(j.dens + b) = make_float2(r0, r1);
+            ulonglong2* fill = (ulonglong2*)(j.map + nb);
+            const ulonglong2 m1a = fill[2 * q], m1b = fill[2 * q + 1];
+            float r[4];
+            r[0] = __fadd_rn(mov[0], unfixed32(m1a.x));
+            r[1] = __fadd_rn(mov[1], unfixed32(m1a.y));
+            r[2] = __fadd_rn(mov[2], unfixed32(m1b.x));
+            r[3] = __fadd_rn(mov[3], unfixed32(m1b.y));
+            if (j.dens) *(float4*)(j.dens + b) = make_float4(r[0], r[1], r[2], r[3]);
             if (j.t0) {
-                split_bf16(r0, j.terms, j.t0, j.t1, j.t2, b);
-                split_bf16(r1, j.terms, j.t0, j.t1, j.t2, b + 1);
+                __align__(8) __nv_bfloat16 t[3][4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    t[0][k] = __float2bfloat16_rn(r[k]);
+                    const float rem = __fsub_rn(r[k], __bfloat162float(t[0][k]));
+                    t[1][k] = __float2bfloat16_rn(rem);
+                    t[2][k] = __float2bfloat16_rn(__fsub_rn(rem, __bfloat162float(t[1][k])));
+                }
+                *(uint2*)(j.t0 + b) = *(const uint2*)t[0];
+                *(uint2*)(j.t1 + b) = *(const uint2*)t[1];
+                if (j.terms > 2) *(uint2*)(j.t2 + b) = *(const uint2*)t[2];
             }
-            fill2[q] = make_ulonglong2(0ull, 0ull);
+            fill[2 * q] = make_ulonglong2(0ull, 0ull);
+            fill[2 * q + 1] = make_ulonglong2(0ull, 0ull);
         }
-        map2[q] = make_ulonglong2(0ull, 0ull);
+        ((ulonglong2*)j.map)[2 * q] = make_ulonglong2(0ull, 0ull);
+        ((ulonglong2*)j.map)[2 * q + 1] = make_ulonglong2(0ull, 0ull);
     }
-    for (int b = (nb & 1) ? bid * blockDim.x + threadIdx.x : nb; b < nb; b += nblk * blockDim.x) {
+    for (int b = (nb & 3) ? bid * blockDim.x + threadIdx.x : nb; b < nb; b += nblk * blockDim.x) {
         const float mov = __fadd_rn(unfixed32(j.map[b]), j.fixed[b]);
         ov += fmaxf(__fsub_rn(mov, j.target), 0.f);
         if (j.with_fill) {
@@ -222,8 +241,8 @@ int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s) {
     p.j[0] = jobs[0];
     p.j[1] = njobs > 1 ? jobs[1] : jobs[0];
     p.njobs = njobs;
-    p.blocks0 = grid_for((long long)jobs[0].nbx * jobs[0].nby, 256, 4);
-    const int blocks = p.blocks0 + (njobs > 1 ? grid_for((long long)jobs[1].nbx * jobs[1].nby, 256, 4) : 0);
+    p.blocks0 = grid_for((long long)jobs[0].nbx * jobs[0].nby / 4, 256, 8);
+    const int blocks = p.blocks0 + (njobs > 1 ? grid_for((long long)jobs[1].nbx * jobs[1].nby / 4, 256, 8) : 0);
     if (launch_k(post_plain_kernel, dim3(blocks), dim3(256), 0, s, p) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;

@@ -155,27 +155,47 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
     hp = (n.hx - n.lx) + (n.hy - n.ly);
 }
 
-__global__ void __launch_bounds__(256, 3) wa_net_kernel(WaJob j) {
+// A 2-pin net by one thread. Per axis the two pins share one exponential: with hi / lo the larger / smaller
+// coordinate, e = exp((lo - hi) / g) is ep of the low pin and en of the high pin, while ep of the high pin and en
+// of the low pin are exp(0) = 1 (both 1 when the pins coincide) -- the values the general form computes, with one
+// exponential instead of four per axis.
+__device__ __forceinline__ void net_two(const WaJob& j, const float2* pos, float ig, int s, float& wa, float& hp) {
+    const float2 a = pin_xy(j, pos, s), b = pin_xy(j, pos, s + 1);
+    float g[2][2], wsum = 0.f, hsum = 0.f;
+#pragma unroll
+    for (int ax = 0; ax < 2; ax++) {
+        const float xa = ax ? a.y : a.x, xb = ax ? b.y : b.x;
+        const float hi = fmaxf(xa, xb), lo = fminf(xa, xb);
+        const float e = __expf((lo - hi) * ig);
+        const float epa = xa == hi ? 1.f : e, epb = xb == hi ? 1.f : e;
+        const float ena = xa == lo ? 1.f : e, enb = xb == lo ? 1.f : e;
+        const float sp = epa + epb, sn = ena + enb;
+        const float ip = __frcp_rn(sp), in = __frcp_rn(sn);
+        const float xp = (xa * epa + xb * epb) * ip, xn = (xa * ena + xb * enb) * in;
+        g[0][ax] = epa * (1.f + (xa - xp) * ig) * ip - ena * (1.f - (xa - xn) * ig) * in;
+        g[1][ax] = epb * (1.f + (xb - xp) * ig) * ip - enb * (1.f - (xb - xn) * ig) * in;
+        wsum += xp - xn;
+        hsum += hi - lo;
+    }
+    put(j, s, g[0][0], g[0][1]);
+    put(j, s + 1, g[1][0], g[1][1]);
+    wa = wsum;
+    hp = hsum;
+}
+
+// Short nets, one per lane: 32 consecutive nets [0, split) per warp item. LONG: nets longer than WA_REG met there
+// (any order) are done by the whole warp in turn; without it every net below split is short (the ordered layout).
+// Blocks write float64 partials at bid0 + blockIdx.x of nblk.
+template <bool LONG>
+__global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
     pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
     const int lane = threadIdx.x & 31;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    const long long chunks = (j.split + 31) / 32, items = chunks + (j.num_nets - j.split);
+    const long long chunks = (j.split + 31) / 32;
     float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float64 above
-    for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
-        if (it >= chunks) {                              // one long net
-            const int i = j.split + (int)(it - chunks);
-            const int s = j.net_start[i], d = j.net_start[i + 1] - s;
-            float wa, hp;
-            net_warp(j, pos, ig, s, d, lane, wa, hp);
-            if (lane == 0) {
-                if (j.out) j.out[i] = make_float2(wa, hp);
-                wa_sum += wa;
-                hp_sum += hp;
-            }
-            continue;
-        }
+    for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < chunks; it += nwarps) {
         const int i = (int)(it * 32) + lane;
         const bool valid = i < j.split;
         int s = 0, d = 0;
@@ -184,40 +204,75 @@ __global__ void __launch_bounds__(256, 3) wa_net_kernel(WaJob j) {
             d = j.net_start[i + 1] - s;
         }
         if (valid && d <= WA_REG) {
-            // the code of an exact degree for the common 2- and 3-pin nets (the predicated general form issues the
-            // instructions of WA_REG pins); warps of the ordered layout take one branch
             float wa, hp;
-            if (d == 2) net_thread<2>(j, pos, ig, s, d, wa, hp);
+            if (d == 2) net_two(j, pos, ig, s, wa, hp);
             else if (d == 3) net_thread<3>(j, pos, ig, s, d, wa, hp);
             else net_thread<WA_REG>(j, pos, ig, s, d, wa, hp);
             if (j.out) j.out[i] = make_float2(wa, hp);
             wa_sum += wa;
             hp_sum += hp;
         }
-        unsigned big = __ballot_sync(0xffffffffu, valid && d > WA_REG);
-        while (big) {
-            const int src = __ffs(big) - 1;
-            big &= big - 1;
-            const int bs = __shfl_sync(0xffffffffu, s, src), bd = __shfl_sync(0xffffffffu, d, src);
-            float wa, hp;
-            net_warp(j, pos, ig, bs, bd, lane, wa, hp);
-            if (lane == src) {
-                if (j.out) j.out[i] = make_float2(wa, hp);
-                wa_sum += wa;
-                hp_sum += hp;
+        if (LONG) {
+            unsigned big = __ballot_sync(0xffffffffu, valid && d > WA_REG);
+            while (big) {
+                const int src = __ffs(big) - 1;
+                big &= big - 1;
+                const int bs = __shfl_sync(0xffffffffu, s, src), bd = __shfl_sync(0xffffffffu, d, src);
+                float wa, hp;
+                net_warp(j, pos, ig, bs, bd, lane, wa, hp);
+                if (lane == src) {
+                    if (j.out) j.out[i] = make_float2(wa, hp);
+                    wa_sum += wa;
+                    hp_sum += hp;
+                }
             }
         }
     }
     if (j.red.partials) {
         double v[2] = {wa_sum, hp_sum};
-        grid_sum<2>(v, j.red);
+        grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
+    }
+}
+
+// Long nets [split, num_nets), one per warp.
+__global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
+    pdl_wait();
+    const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
+    const float ig = __frcp_rn(*j.gamma);
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    float wa_sum = 0.f, hp_sum = 0.f;
+    for (int i = j.split + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < j.num_nets; i += nwarps) {
+        const int s = j.net_start[i], d = j.net_start[i + 1] - s;
+        float wa, hp;
+        net_warp(j, pos, ig, s, d, lane, wa, hp);
+        if (lane == 0) {
+            if (j.out) j.out[i] = make_float2(wa, hp);
+            wa_sum += wa;
+            hp_sum += hp;
+        }
+    }
+    if (j.red.partials) {
+        double v[2] = {wa_sum, hp_sum};
+        grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
     }
 }
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
-    const long long items = (j.split + 31) / 32 + (j.num_nets - j.split);
-    if (launch_k(wa_net_kernel, dim3(grid_for(items * 32, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
-    GP103_CHECK_LAUNCH();
+    const long long chunks = (j.split + 31) / 32, longs = j.num_nets - j.split;
+    const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
+    const int g1 = chunks > 0 || longs == 0 ? grid_for(chunks * 32, 256, 8) : 0;
+    const int g2 = longs > 0 ? grid_for(longs * 32, 256, 4) : 0;
+    if (g1 > 0) {
+        cudaError_t e = inline_long ? launch_k(wa_short_kernel<true>, dim3(g1), dim3(256), 0, s, j, 0, g1 + g2)
+                                    : launch_k(wa_short_kernel<false>, dim3(g1), dim3(256), 0, s, j, 0, g1 + g2);
+        if (e != cudaSuccess) return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
+    if (g2 > 0) {
+        if (launch_k(wa_long_kernel, dim3(g2), dim3(256), 0, s, j, g1, g1 + g2) != cudaSuccess) return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
     return GP103_OK;
 }
 
