@@ -184,7 +184,8 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(ratio), OFF(pins), OFF(area), OFF(lo), OFF(hi), OFF(bx), OFF(by), OFF(target), OFF(fixed),
         OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
-        OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split)};
+        OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
+        OFF(order), OFF(order_counts), OFF(order_cursor)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -210,6 +211,7 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
     REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
     REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
+    REQUIRE((p->order == nullptr) == (p->order_counts == nullptr) && (p->order == nullptr) == (p->order_cursor == nullptr));
     if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
     return GP103_OK;
 }
@@ -236,8 +238,27 @@ extern "C" int gp103_field(const gp103_plan* plan, const float* density, float* 
 
 // Density map(s) at the chosen positions, post-processing, field: the force grid's plain density goes straight into
 // the field's first operand (float32 plane or bf16 terms).
+// The spatial order of the scatter: tiles of T x T force-grid bins, T = max(32, ceil(max(nbx, nby) / 32)), so
+// that there are at most 32 x 32 tiles per node class.
+static OrderJob order_job(const gp103_plan* p) {
+    OrderJob o = {};
+    const int nmax = p->nbx > p->nby ? p->nbx : p->nby;
+    int T = (nmax + 31) / 32;
+    if (T < 32) T = 32;
+    o.counts = p->order_counts;
+    o.cursor = p->order_cursor;
+    o.order = p->order;
+    o.tiles_x = (p->nbx + T - 1) / T;
+    o.tiles_y = (p->nby + T - 1) / T;
+    o.inv_tx = 1.f / (T * p->bx);
+    o.inv_ty = 1.f / (T * p->by);
+    o.num_nodes = p->num_nodes;
+    o.num_mov = p->num_mov;
+    return o;
+}
+
 static int density_and_field(const gp103_plan* p, const float* pos_a, const float* pos_b, const int* sel,
-                             cudaStream_t s) {
+                             const int* order, cudaStream_t s) {
     const size_t nb = (size_t)p->nbx * p->nby;
     ScatterJob sj = {};
     sj.pos_a = (const float2*)pos_a;
@@ -253,6 +274,7 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
     sj.nby = p->nby;
     sj.map0 = p->map;
     sj.map1 = p->map + nb;
+    sj.order = order;
     ScatterJob jobs[2] = {sj, sj};
     if (p->jnbx > 0) {
         ScatterJob& jj = jobs[1];
@@ -350,7 +372,10 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream
     sj.best = phase == GP103_PHASE_DENSITY ? p->best : nullptr;
     sj.n = p->num_nodes;
     sj.red = reduce_slot(p->red, p->counters, R_MOVED);
+    const bool ordered = phase == GP103_PHASE_DENSITY && p->order != nullptr;
+    if (ordered) sj.ord = order_job(p);
     TRY(launch_step(sj, stream));
+    if (ordered) TRY(launch_order(sj.ord, (const float2*)p->v[0], (const float2*)p->v[1], p->cur, true, stream));
 
     WaJob w = wa_job(p);
     w.pos_a = (const float2*)p->v[0];
@@ -374,7 +399,7 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream
         TRY(launch_gather(g, stream));
         return launch_control_start(p->T, p->kp, r_moved, r_grad, r_wa, p->cur, stream);
     }
-    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, stream));
+    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream));
     g.ex = p->ex;
     g.ey = p->ey;
     g.weight_p = p->kp + 1;
@@ -401,7 +426,7 @@ extern "C" int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out
     g.gref_a = g.gref_b = (const float2*)g_ref;
     g.with_wl = with_wl;
     if (weight != 0.0) {
-        TRY(density_and_field(p, pos, pos, nullptr, stream));
+        TRY(density_and_field(p, pos, pos, nullptr, nullptr, stream));
         g.ex = p->ex;
         g.ey = p->ey;
         g.weight = (float)weight;

@@ -58,9 +58,10 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_cons
     int x0 = INT_MAX, x1 = INT_MIN, y0 = INT_MAX, y1 = INT_MIN;
 #pragma unroll
     for (int k = 0; k < SCAT_PER_THREAD; k++) {
-        int i = first + k * SCAT_THREADS + threadIdx.x;
+        const int at = first + k * SCAT_THREADS + threadIdx.x;
         sx[k].b0 = 1; sx[k].b1 = 0; sy[k].b0 = 1; sy[k].b1 = 0; ratio[k] = 0.f;
-        if (i < last) {
+        if (at < last) {
+            const int i = j.order ? j.order[at] : at;
             float2 p = pos[i], s = j.size[i];
             sx[k] = span(p.x, s.x, j.inv_bx, j.nbx);
             sy[k] = span(p.y, s.y, j.inv_by, j.nby);
@@ -128,6 +129,79 @@ int launch_scatter(const ScatterJob* jobs, int njobs, cudaStream_t s) {
     const int blocks = p.blocks0 + (njobs > 1 ? scatter_blocks(jobs[1]) : 0);
     if (blocks == 0) return GP103_OK;
     if (launch_k(scatter_kernel, dim3(blocks), dim3(SCAT_THREADS), 0, s, p) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// ----------------------------------------------------------------------------- spatial order
+// Exclusive scan of the per-tile counts into the cursors (one block; at most ORDER_MAX_KEYS keys), counts zeroed
+// for the next count.
+__global__ void __launch_bounds__(1024) order_scan_kernel(OrderJob o) {
+    __shared__ int warp_total[32];
+    pdl_wait();
+    const int keys = 2 * o.tiles_x * o.tiles_y, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int a = 2 * t < keys ? o.counts[2 * t] : 0, b = 2 * t + 1 < keys ? o.counts[2 * t + 1] : 0;
+    const int sum = a + b;
+    int x = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_total[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        const int orig = lane < (int)(blockDim.x >> 5) ? warp_total[lane] : 0;
+        int z = orig;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, z, off);
+            if (lane >= off) z += y;
+        }
+        warp_total[lane] = z - orig;
+    }
+    __syncthreads();
+    const int excl = x - sum + warp_total[w];
+    if (2 * t < keys) {
+        o.cursor[2 * t] = excl;
+        o.counts[2 * t] = 0;
+    }
+    if (2 * t + 1 < keys) {
+        o.cursor[2 * t + 1] = excl + a;
+        o.counts[2 * t + 1] = 0;
+    }
+}
+
+// Every node takes the next slot of its tile (one atomic per group of lanes with the same tile).
+__global__ void __launch_bounds__(256) order_place_kernel(OrderJob o, const float2* pos_a, const float2* pos_b,
+                                                          const int* sel) {
+    pdl_wait();
+    const float2* pos = pick(pos_a, pos_b, sel);
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < o.num_nodes; base += stride) {
+        const int i = base + lane;
+        const bool valid = i < o.num_nodes;
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        const int key = order_key(o, pos[i], i);
+        const unsigned grp = __match_any_sync(act, key);
+        const int leader = __ffs(grp) - 1;
+        int slot = 0;
+        if (lane == leader) slot = atomicAdd(&o.cursor[key], __popc(grp));
+        slot = __shfl_sync(grp, slot, leader);
+        o.order[slot + __popc(grp & ((1u << lane) - 1u))] = i;
+    }
+}
+
+int launch_order(const OrderJob& o, const float2* pos_a, const float2* pos_b, const int* sel, bool counted,
+                 cudaStream_t s) {
+    if (!counted || 2 * o.tiles_x * o.tiles_y > ORDER_MAX_KEYS) return GP103_ERR_ARG;
+    if (launch_k(order_scan_kernel, dim3(1), dim3(1024), 0, s, o) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (launch_k(order_place_kernel, dim3(grid_for(o.num_nodes, 256, 8)), dim3(256), 0, s, o, pos_a, pos_b, sel) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -53,7 +53,28 @@ struct ScatterJob {
     int nbx, nby;
     unsigned long long* map0;   // nodes < num_mov
     unsigned long long* map1;   // the rest (null: not added)
+    const int* order;           // the nodes in this order (cells first, then fillers); null: index order
 };
+
+// Spatial order of the nodes for the scatter: a counting sort of the nodes by the tile (tile x tile bins of the
+// force grid) their centre is in, cells before fillers. Blocks of the scatter then take nodes that are close on
+// the grid, so their charges meet in shared memory. Any order gives the same map (integer sums); the order only
+// decides how many charges reach the global map through atomics.
+struct OrderJob {
+    int* counts;                // [2 tiles], zero between uses
+    int* cursor;                // [2 tiles]
+    int* order;                 // [num_nodes]
+    int tiles_x, tiles_y;
+    float inv_tx, inv_ty;       // 1 / (tile edge in length units)
+    int num_nodes, num_mov;
+};
+constexpr int ORDER_MAX_KEYS = 2048;
+
+__device__ __forceinline__ int order_key(const OrderJob& o, float2 p, int i) {
+    const int tx = min(max((int)(p.x * o.inv_tx), 0), o.tiles_x - 1);
+    const int ty = min(max((int)(p.y * o.inv_ty), 0), o.tiles_y - 1);
+    return tx * o.tiles_y + ty + (i < o.num_mov ? 0 : o.tiles_x * o.tiles_y);
+}
 
 // One launch for up to two scatters (the force grid and the overflow grid read the same positions).
 struct ScatterPair {
@@ -108,5 +129,7 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
                          const float* weight, const float* precond, float bx, float by, int nbx, int nby, float* grad,
                          cudaStream_t s);
 int launch_gather(const GatherJob& j, cudaStream_t s);
+int launch_order(const OrderJob& o, const float2* pos_a, const float2* pos_b, const int* sel, bool counted,
+                 cudaStream_t s);
 
 }  // namespace gp103

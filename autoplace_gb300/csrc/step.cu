@@ -142,9 +142,17 @@ int launch_select(const double* S, float* u, float* v, float* g, const float* u_
 
 // ----------------------------------------------------------------------------- fused path
 // u' = v - alpha g, v' = clamp(u' + coef (u' - u)) from the current buffers into the other ones, |v' - v|^2 in
-// float64; the best placement of the previous pass (S[is_best]) is copied on the way.
-__global__ void __launch_bounds__(256) step_kernel(StepJob j) {
+// float64; the best placement of the previous pass (S[is_best]) is copied on the way, and the nodes of v' are
+// counted per tile for the scatter's spatial order (shared-memory histogram, one global add per tile).
+__global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ StepJob j) {
+    __shared__ int hist[ORDER_MAX_KEYS];
     pdl_wait();
+    const bool counting = j.ord.counts != nullptr;
+    const int keys = 2 * j.ord.tiles_x * j.ord.tiles_y;
+    if (counting) {
+        for (int k = threadIdx.x; k < keys; k += blockDim.x) hist[k] = 0;
+        __syncthreads();
+    }
     const int c = j.cur ? *j.cur : 0;
     const float2 *u = (const float2*)j.u[c], *v = (const float2*)j.v[c], *g = (const float2*)j.g[c];
     float2 *un_out = (float2*)j.u[1 - c], *vn_out = (float2*)j.v[1 - c];
@@ -169,6 +177,10 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
         if (copy_best) ((float4*)j.best)[q] = vi;
         const float dx = vn.x - vi.x, dy = vn.y - vi.y, dz = vn.z - vi.z, dw = vn.w - vi.w;
         d2 += (dx * dx + dy * dy) + (dz * dz + dw * dw);
+        if (counting) {
+            atomicAdd(&hist[order_key(j.ord, make_float2(vn.x, vn.y), 2 * q)], 1);
+            atomicAdd(&hist[order_key(j.ord, make_float2(vn.z, vn.w), 2 * q + 1)], 1);
+        }
     }
     for (int i = (j.n & 1) ? blockIdx.x * blockDim.x + threadIdx.x : j.n; i < j.n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], ui = u[i], l = lo[i], h = hi[i];
@@ -180,6 +192,12 @@ __global__ void __launch_bounds__(256) step_kernel(StepJob j) {
         if (copy_best) ((float2*)j.best)[i] = vi;
         const float dx = vx - vi.x, dy = vy - vi.y;
         d2 += dx * dx + dy * dy;
+        if (counting) atomicAdd(&hist[order_key(j.ord, make_float2(vx, vy), i)], 1);
+    }
+    if (counting) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < keys; k += blockDim.x)
+            if (hist[k]) atomicAdd(&j.ord.counts[k], hist[k]);
     }
     double r[1] = {d2};
     grid_sum<1>(r, j.red);

@@ -1,6 +1,7 @@
 // Step / control declarations (state layout of the reference's control kernel).
 #pragma once
 #include "gp103.cuh"
+#include "kernels.cuh"
 
 namespace gp103 {
 
@@ -24,6 +25,7 @@ struct StepJob {
     float* best;
     int n;                      // nodes
     Reduce red;                 // |v' - v|^2
+    OrderJob ord;               // counts of the spatial order of v' (ord.counts null: none)
 };
 
 int launch_nesterov_step(const float* u, const float* v, const float* g, const float* lo, const float* hi,

@@ -124,6 +124,11 @@ class Placer(object):
         self.red = z((sz.red,), torch.float64)
         self.counters = z((16,), torch.int32)
         self.scal = z((8,), torch.float64)
+        self.order = z((n,), torch.int32)
+        self.order_counts = z((2048,), torch.int32)
+        self.order_cursor = z((2048,), torch.int32)
+        pl.order, pl.order_counts, pl.order_cursor = (self._p(x) for x in (self.order, self.order_counts,
+                                                                            self.order_cursor))
         self.tmp = [z((n, 2), torch.float32) for _ in range(2)]
         for k in ("best", "cur", "S", "T", "kp", "c", "pin_grad", "map", "red", "counters"):
             setattr(pl, k, self._p(getattr(self, k)))

@@ -34,6 +34,7 @@ class Plan(ctypes.Structure):
         ("S", _vp), ("T", _vp), ("kp", _vp), ("c", _vp),
         ("pin_grad", _vp), ("map", _vp), ("jmap", _vp), ("red", _vp), ("counters", _vp),
         ("pin_slot", _vp), ("net_split", _i),
+        ("order", _vp), ("order_counts", _vp), ("order_cursor", _vp),
     ]
 
 

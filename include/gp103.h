@@ -166,6 +166,9 @@ typedef struct {
      * position of p in cell order (cell_start ranges), and cell_pin is not read */
     const int* pin_slot;
     int net_split;            /* nets [net_split, num_nets) are long: one warp each (num_nets: any order) */
+    /* spatial order of the nodes for the scatter (optional; all three or none): order [num_nodes],
+     * order_counts [2048] (zero), order_cursor [2048] */
+    int* order; int* order_counts; int* order_cursor;
 } gp103_plan;
 
 typedef struct {
