@@ -356,10 +356,13 @@ static WaJob wa_job(const gp103_plan* p) {
     return w;
 }
 
-extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream) {
+extern "C" int gp103_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream) {
     TRY(check_plan(plan));
     const gp103_plan* p = plan;
+    const int phase = phase_flags & ~GP103_PASS_SORT;
+    const bool sort = (phase_flags & GP103_PASS_SORT) != 0;
     REQUIRE(phase == GP103_PHASE_START || phase == GP103_PHASE_DENSITY);
+    REQUIRE(!sort || (phase == GP103_PHASE_DENSITY && p->order != nullptr));
     REQUIRE(p->u[0] && p->u[1] && p->v[0] && p->v[1] && p->g[0] && p->g[1] && p->cur && p->lo && p->hi);
     REQUIRE(phase == GP103_PHASE_START ? p->T != nullptr : (p->S && p->c && p->best));
     StepJob sj = {};
@@ -373,9 +376,9 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase, cudaStream_t stream
     sj.n = p->num_nodes;
     sj.red = reduce_slot(p->red, p->counters, R_MOVED);
     const bool ordered = phase == GP103_PHASE_DENSITY && p->order != nullptr;
-    if (ordered) sj.ord = order_job(p);
+    if (sort) sj.ord = order_job(p);
     TRY(launch_step(sj, stream));
-    if (ordered) TRY(launch_order(sj.ord, (const float2*)p->v[0], (const float2*)p->v[1], p->cur, true, stream));
+    if (sort) TRY(launch_order(sj.ord, (const float2*)p->v[0], (const float2*)p->v[1], p->cur, true, stream));
 
     WaJob w = wa_job(p);
     w.pos_a = (const float2*)p->v[0];

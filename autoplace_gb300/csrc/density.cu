@@ -13,28 +13,111 @@
 namespace gp103 {
 
 // ----------------------------------------------------------------------------- scatter
-// A block takes a chunk of SCAT_CHUNK consecutive nodes, all movable or all fillers. If the bins its nodes touch fit
-// in shared memory (bounding box <= SCAT_SMEM_BINS), the block sums its charges there and then adds every non-zero
-// bin to the global map once; otherwise it adds each charge to the global map directly (64-bit atomics in L2).
-// In shared memory a 64-bit sum is kept as two 32-bit words: a charge (at most 2^32) adds its low word to `lo` with
-// a 32-bit atomic whose old value tells whether the word wrapped; the wrap and the charge's high bit go to `hi`.
-// Exact (integer) in any order, with a single 32-bit atomic for most charges.
+// A block takes a chunk of SCAT_CHUNK consecutive nodes (in the spatial order when one is given), all movable or all
+// fillers. If the bins its nodes touch fit in shared memory (bounding box <= SCAT_SMEM_BINS), the block sums its
+// charges there and then adds every non-zero bin to the global map once; otherwise it adds each charge to the global
+// map directly (64-bit atomics in L2).
 constexpr int SCAT_THREADS = 256;
 constexpr int SCAT_PER_THREAD = 4;
 constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;
 constexpr int SCAT_SMEM_BINS = 6144;      // 2 x 24 KB of 32-bit words
+constexpr float TWO32 = 4294967296.f, TWO33 = 8589934592.f, TWO_M32 = 2.3283064365386963e-10f;
 
-__device__ __forceinline__ void add_shared(unsigned int* lo, unsigned int* hi, int b, unsigned long long q) {
-    const unsigned int ql = (unsigned int)q;
-    unsigned int qh = (unsigned int)(q >> 32);
-    const unsigned int old = atomicAdd(lo + b, ql);
-    if (old + ql < old) qh += 1u;
-    if (qh) atomicAdd(hi + b, qh);
+__device__ __forceinline__ void red_shared(unsigned int* a, unsigned int v) {
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"((unsigned int)__cvta_generic_to_shared(a)), "r"(v) : "memory");
+}
+
+// Where a block's charges go. A charge is v = float(wx * oy) * 2^32 (the scaling is exact), truncated to an integer
+// q. In shared memory q < 2^33 is kept as two 32-bit sums: its low 16 bits in lo[b], the rest in hi[b], by adds
+// whose old values nobody reads. A block adds at most SCAT_CHUNK charges to a bin (one per node), so neither word
+// can wrap (1024 x 2^16, 1024 x 2^17 < 2^32) and the bin's sum is hi * 2^16 + lo exactly. Larger charges (only
+// from ratios above 1), infinities and NaNs take the exact 64-bit conversion and a global atomic.
+struct Tally {
+    unsigned int* lo;
+    unsigned int* hi;
+    unsigned long long* map;
+    int nby, bx0, by0, H;
+    bool local;
+
+    __device__ __forceinline__ void add(int x, int y, float v) const {
+        unsigned int q, top;
+        if (v < TWO32) {
+            q = __float2uint_rz(v);                                  // negatives and -inf clamp to 0
+            top = 0u;
+        } else if (v < TWO33) {
+            q = __float2uint_rz(__fsub_rn(v, TWO32));                // exact: v is a multiple of 2^9 here
+            top = 1u;
+        } else {
+            const unsigned long long Q = fixed32(__fmul_rn(v, TWO_M32));
+            if (Q) atomicAdd(&map[(size_t)x * nby + y], Q);
+            return;
+        }
+        if ((q | top) == 0u) return;
+        if (local) {
+            const int b = (x - bx0) * H + (y - by0);
+            red_shared(lo + b, q & 0xffffu);
+            red_shared(hi + b, (q >> 16) | (top << 16));
+        } else {
+            atomicAdd(&map[(size_t)x * nby + y], (unsigned long long)q | ((unsigned long long)top << 32));
+        }
+    }
+};
+
+// Overlaps of a span with its first three bins b0, b0 + 1, b0 + 2: overlap() with the bin edges formed by exact
+// float additions ((float)(b0 + k) == (float)b0 + k below 2^24).
+__device__ __forceinline__ void overlaps3(const Span& s, float (&o)[3]) {
+    const float e0 = (float)s.b0, e1 = __fadd_rn(e0, 1.f), e2 = __fadd_rn(e0, 2.f), e3 = __fadd_rn(e0, 3.f);
+    o[0] = fmaxf(__fsub_rn(fminf(s.hi, e1), fmaxf(s.lo, e0)), 0.f);
+    o[1] = fmaxf(__fsub_rn(fminf(s.hi, e2), fmaxf(s.lo, e1)), 0.f);
+    o[2] = fmaxf(__fsub_rn(fminf(s.hi, e3), fmaxf(s.lo, e2)), 0.f);
+}
+
+// The charges of one node. wx is scaled by 2^32 before the product: float(wx * oy) * 2^32 equals
+// float(wx 2^32 * oy) whenever the former is a normal float, and both truncate to 0 below that.
+// Fast case (every node whose smoothed size is under 2 bins, with a ratio up to 1): both spans have at most 3 bins
+// and the largest product is below 2^32 (rounding is monotonic, so then every product is), so all 9 charges are
+// plain 32-bit truncations added to shared memory, unrolled and predicated. Anything else takes Tally::add.
+__device__ __forceinline__ void node_charges(const Tally& t, const Span& sx, const Span& sy, float ratio) {
+    const int nx = sx.b1 - sx.b0, ny = sy.b1 - sy.b0;
+    if (nx < 0 || ny < 0) return;
+    if (nx <= 2 && ny <= 2) {
+        float wx[3], oy[3];
+        overlaps3(sx, wx);
+        overlaps3(sy, oy);
+#pragma unroll
+        for (int a = 0; a < 3; a++) wx[a] = __fmul_rn(__fmul_rn(ratio, wx[a]), TWO32);
+        const float vmax = __fmul_rn(fmaxf(fmaxf(wx[0], wx[1]), wx[2]), fmaxf(fmaxf(oy[0], oy[1]), oy[2]));
+        if (t.local && vmax < TWO32) {
+            const int base = (sx.b0 - t.bx0) * t.H + (sy.b0 - t.by0);
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    if (a <= nx && c <= ny) {
+                        const unsigned int q = __float2uint_rz(__fmul_rn(wx[a], oy[c]));
+                        const int b = base + a * t.H + c;
+                        red_shared(t.lo + b, q & 0xffffu);
+                        red_shared(t.hi + b, q >> 16);
+                    }
+            return;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+                if (a <= nx && c <= ny) t.add(sx.b0 + a, sy.b0 + c, __fmul_rn(wx[a], oy[c]));
+        return;
+    }
+    for (int x = sx.b0; x <= sx.b1; x++) {
+        const float wx = __fmul_rn(__fmul_rn(ratio, overlap(sx, x)), TWO32);
+        for (int y = sy.b0; y <= sy.b1; y++) t.add(x, y, __fmul_rn(wx, overlap(sy, y)));
+    }
 }
 
 __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_constant__ ScatterPair pair) {
     pdl_wait();
-    __shared__ unsigned int tlo[SCAT_SMEM_BINS], thi[SCAT_SMEM_BINS];
+    __shared__ __align__(16) unsigned int tlo[SCAT_SMEM_BINS];
+    __shared__ __align__(16) unsigned int thi[SCAT_SMEM_BINS];
     __shared__ int box[4];
     const bool second = (int)blockIdx.x >= pair.blocks0;
     const ScatterJob& j = second ? pair.j[1] : pair.j[0];
@@ -61,8 +144,12 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_cons
         const int at = first + k * SCAT_THREADS + threadIdx.x;
         sx[k].b0 = 1; sx[k].b1 = 0; sy[k].b0 = 1; sy[k].b1 = 0; ratio[k] = 0.f;
         if (at < last) {
-            const int i = j.order ? j.order[at] : at;
-            float2 p = pos[i], s = j.size[i];
+            int i = at;
+            if (j.order) {
+                const int o = j.order[at];
+                if ((unsigned)o < (unsigned)j.num_nodes) i = o;      // an order must be a permutation; never leave the arrays
+            }
+            const float2 p = pos[i], s = j.size[i];
             sx[k] = span(p.x, s.x, j.inv_bx, j.nbx);
             sy[k] = span(p.y, s.y, j.inv_by, j.nby);
             ratio[k] = j.ratio[i];
@@ -82,36 +169,27 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_cons
     const int bx0 = box[0], bx1 = box[1], by0 = box[2], by1 = box[3];
     if (bx0 > bx1 || map == nullptr) return;                       // nothing to add (uniform over the block)
     const long long w = (long long)(bx1 - bx0 + 1), h = (long long)(by1 - by0 + 1);
-    if (w * h <= SCAT_SMEM_BINS) {
-        const int H = (int)h, area = (int)(w * h);
-        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) { tlo[t] = 0u; thi[t] = 0u; }
-        __syncthreads();
+    Tally t;
+    t.lo = tlo; t.hi = thi; t.map = map; t.nby = j.nby; t.bx0 = bx0; t.by0 = by0; t.H = (int)h;
+    t.local = w * h <= SCAT_SMEM_BINS;
+    const int area = t.local ? (int)(w * h) : 0;
+    const int quads = (area + 3) >> 2;
+    for (int k = threadIdx.x; k < quads; k += SCAT_THREADS) {
+        ((uint4*)tlo)[k] = make_uint4(0u, 0u, 0u, 0u);
+        ((uint4*)thi)[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
 #pragma unroll
-        for (int k = 0; k < SCAT_PER_THREAD; k++) {
-            for (int x = sx[k].b0; x <= sx[k].b1; x++) {
-                const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
-                const int row = (x - bx0) * H - by0;
-                for (int y = sy[k].b0; y <= sy[k].b1; y++) {
-                    const unsigned long long q = charge(wx, overlap(sy[k], y));
-                    if (q) add_shared(tlo, thi, row + y, q);
-                }
-            }
-        }
-        __syncthreads();
-        for (int t = threadIdx.x; t < area; t += SCAT_THREADS) {
-            const unsigned long long q = ((unsigned long long)thi[t] << 32) | tlo[t];
-            if (q) atomicAdd(&map[(size_t)(bx0 + t / H) * j.nby + (by0 + t % H)], q);
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < SCAT_PER_THREAD; k++) {
-            for (int x = sx[k].b0; x <= sx[k].b1; x++) {
-                const float wx = __fmul_rn(ratio[k], overlap(sx[k], x));
-                for (int y = sy[k].b0; y <= sy[k].b1; y++) {
-                    const unsigned long long q = charge(wx, overlap(sy[k], y));
-                    if (q) atomicAdd(&map[(size_t)x * j.nby + y], q);
-                }
-            }
+    for (int k = 0; k < SCAT_PER_THREAD; k++) node_charges(t, sx[k], sy[k], ratio[k]);
+    if (!t.local) return;
+    __syncthreads();
+    // row = b / H by a multiply: magic = ceil(2^32 / H) is exact for b * (magic * H - 2^32) < 2^32, here < 2^26
+    const unsigned long long magic = ((1ull << 32) + (unsigned long long)(t.H - 1)) / (unsigned long long)t.H;
+    for (int b = threadIdx.x; b < area; b += SCAT_THREADS) {
+        const unsigned long long q = ((unsigned long long)thi[b] << 16) + tlo[b];
+        if (q) {
+            const int row = (int)(((unsigned long long)b * magic) >> 32);
+            atomicAdd(&map[(size_t)(bx0 + row) * j.nby + (by0 + b - row * t.H)], q);
         }
     }
 }

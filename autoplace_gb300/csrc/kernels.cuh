@@ -70,9 +70,11 @@ struct OrderJob {
 };
 constexpr int ORDER_MAX_KEYS = 2048;
 
+// Tiles in column-major order, every other column upwards (a snake), so that consecutive keys are adjacent tiles.
 __device__ __forceinline__ int order_key(const OrderJob& o, float2 p, int i) {
     const int tx = min(max((int)(p.x * o.inv_tx), 0), o.tiles_x - 1);
-    const int ty = min(max((int)(p.y * o.inv_ty), 0), o.tiles_y - 1);
+    int ty = min(max((int)(p.y * o.inv_ty), 0), o.tiles_y - 1);
+    if (tx & 1) ty = o.tiles_y - 1 - ty;
     return tx * o.tiles_y + ty + (i < o.num_mov ? 0 : o.tiles_x * o.tiles_y);
 }
 

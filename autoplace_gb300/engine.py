@@ -55,12 +55,15 @@ def net_order(net_start, cell32, cell_pin):
 
 
 class Placer(object):
-    def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None):
+    def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None,
+                 sort_every=None):
         self.p = prob
         self.dev = torch.device(device or "cuda")
         self.mode = native.FIELD_MODES[field] if isinstance(field, str) else int(field)
         self.check_every = check_every
         self.use_graphs = use_graphs
+        # density passes between refreshes of the scatter's spatial order (an order only speeds the scatter up)
+        self.sort_every = max(int(sort_every or check_every), 1)
         self.stream = stream or torch.cuda.Stream(self.dev)
         self._graphs = {}
         self._captured = self._replayed = 0
@@ -124,7 +127,7 @@ class Placer(object):
         self.red = z((sz.red,), torch.float64)
         self.counters = z((16,), torch.int32)
         self.scal = z((8,), torch.float64)
-        self.order = z((n,), torch.int32)
+        self.order = self._hold(torch.arange(n, dtype=torch.int32, device=dev))
         self.order_counts = z((2048,), torch.int32)
         self.order_cursor = z((2048,), torch.int32)
         pl.order, pl.order_counts, pl.order_cursor = (self._p(x) for x in (self.order, self.order_counts,
@@ -164,8 +167,9 @@ class Placer(object):
 
     def _passes(self, phase, k):
         s = self.stream.cuda_stream
-        for _ in range(k):
-            native.call("gp103_pass", self._ref, phase, s)
+        for i in range(k):
+            sort = phase == native.PHASE_DENSITY and i % self.sort_every == 0
+            native.call("gp103_pass", self._ref, phase | (native.PASS_SORT if sort else 0), s)
 
     def _replay(self, phase):
         if not self.use_graphs:

@@ -119,7 +119,8 @@ enum {
 /* Phases of gp103_pass. */
 enum {
     GP103_PHASE_START = 0,    /* wirelength-only start (density weight 0), src/run_placement.py:60-65 */
-    GP103_PHASE_DENSITY = 1   /* the device loop of src/gpu_loop.py:58-68 */
+    GP103_PHASE_DENSITY = 1,  /* the device loop of src/gpu_loop.py:58-68 */
+    GP103_PASS_SORT = 0x100   /* or-ed to GP103_PHASE_DENSITY: refresh plan->order from this pass's positions */
 };
 
 /* Layout of the start-phase state T [32] (float64): what NesterovOptimizer (alpha, a) and
@@ -166,8 +167,10 @@ typedef struct {
      * position of p in cell order (cell_start ranges), and cell_pin is not read */
     const int* pin_slot;
     int net_split;            /* nets [net_split, num_nets) are long: one warp each (num_nets: any order) */
-    /* spatial order of the nodes for the scatter (optional; all three or none): order [num_nodes],
-     * order_counts [2048] (zero), order_cursor [2048] */
+    /* spatial order of the nodes for the scatter (optional; all three or none): order [num_nodes], a permutation
+     * of 0..num_nodes-1 (fill it with 0, 1, ... before the first pass; density passes with GP103_PASS_SORT refresh
+     * it, the others only read it), order_counts [2048] (zero), order_cursor [2048]. Any permutation gives the same
+     * density map; a recent spatial one gives a faster scatter. */
     int* order; int* order_counts; int* order_cursor;
 } gp103_plan;
 
