@@ -382,8 +382,6 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "no recorded iteration count for %s" % args.config}))
         return
     samples = []
-    for _ in range(max(args.warmup, 0)):
-        pass
     for _ in range(max(args.steps, 1)):
         per, threads = cpu_sample(prob, pos0, args.cpu_iters, iters)
         samples.append(per)
