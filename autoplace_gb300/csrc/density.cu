@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(SCAT_THREADS) scatter_kernel(const __grid_cons
             const float2 p = pos[i], s = j.size[i];
             sx[k] = span(p.x, s.x, j.inv_bx, j.nbx);
             sy[k] = span(p.y, s.y, j.inv_by, j.nby);
-            ratio[k] = j.ratio[i];
+            ratio[k] = j.ratio ? j.ratio[i] : 1.f;
             if (sx[k].b0 <= sx[k].b1 && sy[k].b0 <= sy[k].b1) {
                 x0 = min(x0, sx[k].b0); x1 = max(x1, sx[k].b1);
                 y0 = min(y0, sy[k].b0); y1 = max(y1, sy[k].b1);
@@ -330,7 +330,8 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     const int bid = second ? (int)blockIdx.x - pair.blocks0 : (int)blockIdx.x;
     const int nblk = second ? (int)gridDim.x - pair.blocks0 : pair.blocks0;
     const int nb = j.nbx * j.nby;
-    float ov = 0.f;
+    float ov = 0.f;             // per-thread partial of the hot path (a few bins)
+    double ovd = 0.0;           // the same in float64 for an exact evaluation (j.exact)
     // four bins per thread and iteration: 32-byte map loads / stores, 8-byte stores of each bf16 term plane (a bin
     // count that is a multiple of 4 keeps every plane aligned; any other takes the scalar loop below for every bin)
     const int quads = (nb & 3) ? 0 : nb >> 2;
@@ -344,7 +345,10 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
         mov[2] = __fadd_rn(unfixed32(m0b.x), fx.z);
         mov[3] = __fadd_rn(unfixed32(m0b.y), fx.w);
 #pragma unroll
-        for (int k = 0; k < 4; k++) ov += fmaxf(__fsub_rn(mov[k], j.target), 0.f);
+        for (int k = 0; k < 4; k++) {
+            const float o = fmaxf(__fsub_rn(mov[k], j.target), 0.f);
+            if (j.exact) ovd += (double)o; else ov += o;
+        }
         if (j.with_fill) {
             ulonglong2* fill = (ulonglong2*)(j.map + nb);
             const ulonglong2 m1a = fill[2 * q], m1b = fill[2 * q + 1];
@@ -375,7 +379,8 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     }
     for (int b = (nb & 3) ? bid * blockDim.x + threadIdx.x : nb; b < nb; b += nblk * blockDim.x) {
         const float mov = __fadd_rn(unfixed32(j.map[b]), j.fixed[b]);
-        ov += fmaxf(__fsub_rn(mov, j.target), 0.f);
+        const float o = fmaxf(__fsub_rn(mov, j.target), 0.f);
+        if (j.exact) ovd += (double)o; else ov += o;
         if (j.with_fill) {
             const float r = __fadd_rn(mov, unfixed32(j.map[nb + b]));
             if (j.dens) j.dens[b] = r;
@@ -384,7 +389,7 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
         }
         j.map[b] = 0ull;
     }
-    double v[1] = {ov};
+    double v[1] = {j.exact ? ovd : (double)ov};
     grid_sum<1>(v, j.red, nblk, bid);
 }
 

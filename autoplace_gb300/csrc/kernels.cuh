@@ -47,7 +47,7 @@ struct WaJob {
 
 struct ScatterJob {
     const float2* pos_a; const float2* pos_b; const int* sel;
-    const float2* size; const float* ratio;
+    const float2* size; const float* ratio;     // ratio null: 1 for every node
     int num_nodes, num_mov;
     float inv_bx, inv_by;
     int nbx, nby;
@@ -94,6 +94,7 @@ struct PostJob {
     float* dens;                // plain density, may be null
     __nv_bfloat16 *t0, *t1, *t2;  // bf16 split terms of the density, may be null
     int terms;
+    int exact;                  // float64 per-thread partials of the sum (evaluators); 0: float32 (hot path)
     Reduce red;                 // sum of the density above the target
 };
 

@@ -326,6 +326,7 @@ int launch_finish(const double* S, const int* cur, const float* v0, const float*
 struct Totals {
     Reduce r[8];
     int k[8];
+    double mul[8];
     int n;
 };
 
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(256) totals_kernel(Totals t, double* out) {
     pdl_wait();
     for (int i = 0; i < t.n; i++) {
         const double v = block_total(t.r[i], t.k[i]);
-        if (threadIdx.x == 0) out[i] = v;
+        if (threadIdx.x == 0) out[i] = v * t.mul[i];
     }
 }
 
@@ -342,8 +343,19 @@ int launch_totals(const Reduce* r, const int* k, int n, double* out, cudaStream_
     for (int i = 0; i < n && i < 8; i++) {
         t.r[i] = r[i];
         t.k[i] = k[i];
+        t.mul[i] = 1.0;
     }
     t.n = n < 8 ? n : 8;
+    if (launch_k(totals_kernel, dim3(1), dim3(256), 0, s, t, out) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+int launch_scale_total(const Reduce& r, double mul, double* out, cudaStream_t s) {
+    Totals t = {};
+    t.r[0] = r;
+    t.mul[0] = mul;
+    t.n = 1;
     if (launch_k(totals_kernel, dim3(1), dim3(256), 0, s, t, out) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;

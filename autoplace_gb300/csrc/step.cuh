@@ -43,5 +43,7 @@ int launch_control_start(double* T, float* kp, Reduce moved2, Reduce grad, Reduc
 int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
                   cudaStream_t s);
 int launch_totals(const Reduce* r, const int* k, int n, double* out, cudaStream_t s);
+// out[0] = value 0 of r times mul
+int launch_scale_total(const Reduce& r, double mul, double* out, cudaStream_t s);
 
 }  // namespace gp103

@@ -196,6 +196,32 @@ class Placer(object):
     def overflow_scale(self):
         return self.plan.jovf_scale if self.plan.jnbx > 0 else self.plan.ovf_scale
 
+    def evaluate(self, pos):
+        """The judges of a placement, in float64 on the device: (HPWL over every net, overflow of the movable cells
+        with their real sizes on the overflow grid). The whole netlist is uploaded on the first call."""
+        p = self.p
+        if not hasattr(self, "_ev"):
+            t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.dev)
+            gr = p.real_judge
+            self._ev = dict(cell=t(p.all_cell, torch.int32), off=t(p.all_off, torch.float32),
+                            start=t(p.all_net_start, torch.int32), size=t(p.nl.size, torch.float32),
+                            fixed=t(gr.fixed_map, torch.float32),
+                            map=torch.zeros((gr.nbx, gr.nby), dtype=torch.int64, device=self.dev),
+                            scratch=torch.zeros(native.EVAL_SCRATCH_BYTES, dtype=torch.uint8, device=self.dev),
+                            out=torch.zeros(2, dtype=torch.float64, device=self.dev), grid=gr)
+        e, gr, s = self._ev, self._ev["grid"], self.stream.cuda_stream
+        with torch.cuda.stream(self.stream):
+            pos = torch.as_tensor(pos, dtype=torch.float32).to(self.dev).contiguous()
+        out = e["out"]
+        native.call("gp103_hpwl", self._p(pos), self._p(e["cell"]), self._p(e["off"]), self._p(e["start"]),
+                    len(p.all_net_start) - 1, p.num_mov, self._p(e["scratch"]), ctypes.c_void_p(out.data_ptr()), s)
+        native.call("gp103_exact_overflow", self._p(pos), self._p(e["size"]), p.num_mov, gr.bx, gr.by, gr.nbx,
+                    gr.nby, self._p(e["fixed"]), gr.target, gr.bin_area / gr.mov_area, self._p(e["map"]),
+                    self._p(e["scratch"]), ctypes.c_void_p(out.data_ptr() + 8), s)
+        self.sync()
+        h = out.cpu().numpy()
+        return float(h[0]), float(h[1])
+
     # ------------------------------------------------------------------ one level
     def run(self, pos0, log=None):
         """Place from pos0 ([num_nodes, 2], host or device) to the stop. -> dict (reason, iters, start_iters, hpwl,

@@ -65,7 +65,10 @@ _SIGS = {
     "gp103_probe": ([ctypes.POINTER(Plan), _vp, _vp, _d, _vp, _vp, _vp], _i),
     "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
+    "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
+    "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
 }
+EVAL_SCRATCH_BYTES = 16640
 
 
 def library_path():

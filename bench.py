@@ -236,7 +236,18 @@ def profile_pass(placer):
     return {k: {"launches_per_pass": v[0] / 8.0, "ms_per_pass": v[1] / 8.0} for k, v in agg.items()}, rec
 
 
-def roofline(prob, field, prof, peaks):
+def measured_traffic(config, field):
+    """DRAM bytes (read + write) per pass of each launcher, from the committed ncu summary of this workload."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_%s.json" % config)) as f:
+            rec = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    return rec["bytes"] if rec.get("field") == field else {}
+
+
+def roofline(prob, field, prof, peaks, config="c2"):
+    traffic = measured_traffic(config, field)
     hbm = peaks.get("hbm_gbs")
     tc = peaks.get("bf16_tflops")
     by = kernel_bytes(prob)
@@ -248,8 +259,8 @@ def roofline(prob, field, prof, peaks):
         ml = v["ms_per_pass"] / max(v["launches_per_pass"], 1e-9)
         row = {"ms_per_pass": round(v["ms_per_pass"], 4), "launches_per_pass": v["launches_per_pass"],
                "ms_per_launch": round(ml, 4)}
-        if k in by:
-            row["gbs"] = round(by[k] / (ml * 1e-3) / 1e9, 1)
+        if k in by:     # algorithmic bytes of the whole pass over the kernel's time per pass (all its launches)
+            row["gbs"] = round(by[k] / (v["ms_per_pass"] * 1e-3) / 1e9, 1)
         if k == "launch_tc_bn":
             f = tc_flops(prob, field) * (6.0 / v["launches_per_pass"])
             row["tflops"] = round(f / (ml * 1e-3) / 1e12, 1)
@@ -258,13 +269,14 @@ def roofline(prob, field, prof, peaks):
         f = tc_flops(prob, field) * (6.0 / d["launches_per_pass"])
         ach = f / (ms_launch * 1e-3) / 1e12
         r = {"kernel": "tc_gemm_kernel", "bound": "tensor", "achieved": round(ach, 1), "peak": tc,
-             "unit": "TFLOP/s", "frac": round(ach / tc, 4) if tc else None, "traffic": None,
+             "unit": "TFLOP/s", "frac": round(ach / tc, 4) if tc else None, "traffic": traffic.get(name),
              "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops)"}
     else:
         b = by.get(name)
-        ach = b / (ms_launch * 1e-3) / 1e9 if b else None
+        ach = b / (d["ms_per_pass"] * 1e-3) / 1e9 if b else None
         r = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1) if ach else None, "peak": hbm, "unit": "GB/s",
-             "frac": round(ach / hbm, 4) if ach and hbm else None, "traffic": None,
+             "frac": round(ach / hbm, 4) if ach and hbm else None,
+             "traffic": round(traffic[name] / max(d["launches_per_pass"], 1e-9)) if name in traffic else None,
              "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
     return r, table
 
@@ -314,9 +326,7 @@ def run_gb300(args):
     step_s = reduce_max(ms / 1000.0, world)
     last = runs[-1]
     iters = last["iters"]
-    from oracle import gp_oracle as O
-    pos = last["pos"].cpu().numpy()
-    hpwl_exact = O.hpwl_all(pos, prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
+    hpwl_exact, overflow_exact = placer.evaluate(last["pos"])
 
     # e2e: from host arrays through the public API (upload, run, download)
     e2e_s, h2d, d2h = [], 0, 0
@@ -336,7 +346,7 @@ def run_gb300(args):
 
     prof, _ = profile_pass(placer)
     peaks = load_peaks()
-    roof, table = roofline(prob, args.field, prof, peaks)
+    roof, table = roofline(prob, args.field, prof, peaks, args.config)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -356,7 +366,8 @@ def run_gb300(args):
             "data": "synthetic (seeded generator standing in for ISPD 2015/2019)",
             "config": config_dict(prob, args, world),
             "result": {"stop": last["reason"], "iterations": iters, "start_iterations": last["start_iters"],
-                       "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "ms_per_iteration":
+                       "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "overflow_exact": overflow_exact,
+                       "ms_per_iteration":
                        round(step_s * 1000 / max(iters, 1), 4), "wall_s_per_step": round(wall / args.steps, 4)},
             "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roof, "kernels": table, "cpu_baseline": cpu, "clocks": clk,

@@ -213,6 +213,25 @@ int gp103_field(const gp103_plan* plan, const float* density, float* ex, float* 
 /* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
 int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
 
+/* ------------------------------------------------------------------------------------------------ part 3
+ * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
+ * *out is written by the device (read it after synchronising the stream). */
+#define GP103_EVAL_SCRATCH_BYTES 16640
+
+/* HPWL over every net (Wirelength.hpwl, src/core/wa_wirelength_hpwl.py:66-70): pin position pos[pin_cell] +
+ * pin_off (pin_off alone for pin_cell >= num_mov: a fixed pin), per net max - min on each axis, all in float64.
+ * Nets in net_start order [num_nets + 1]; empty nets add 0. */
+int gp103_hpwl(const float* pos, const int* pin_cell, const float* pin_off, const int* net_start, int num_nets,
+               int num_mov, void* scratch, double* out, cudaStream_t stream);
+
+/* Overflow of the movable cells with their real sizes (ElectronicDensityLayer.exact_overflow,
+ * src/core/electronic_density_layer.py:112-116): fixed-point map of the cells at ratio 1 on an nbx x nby grid of
+ * bins bx x by, out = sum over bins of max(map + fixed - target, 0) in float64, times area_scale (bin area /
+ * movable area). map: u64 [nbx, nby], zero on entry, zero again on return. */
+int gp103_exact_overflow(const float* pos, const float* size, int num_mov, float bx, float by, int nbx, int nby,
+                         const float* fixed, float target, double area_scale, unsigned long long* map,
+                         void* scratch, double* out, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,6 +56,9 @@ def test_argument_errors_without_gpu():
     assert L.gp103_density_map(None, None, None, 0, 0, 1.0, 1.0, 0, 4, None, None, 1.0, None, None,
                                None) == native.ERR_ARG
     assert L.gp103_select(None, None, None, None, None, None, None, None, 0, None) == native.ERR_ARG
+    assert L.gp103_hpwl(None, None, None, None, 5, 3, None, None, None) == native.ERR_ARG
+    assert L.gp103_exact_overflow(None, None, 3, 1.0, 1.0, 0, 8, None, 1.0, 1.0, None, None, None,
+                                  None) == native.ERR_ARG
 
 
 def test_net_order_keeps_nets_and_cell_sums():
