@@ -54,9 +54,23 @@ def net_order(net_start, cell32, cell_pin):
     return perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum())
 
 
+def pinned_inputs(prob):
+    """The problem arrays a Placer uploads, as pinned CPU tensors ({name: tensor}). A caller that keeps its inputs in
+    pinned memory passes them as Placer(prob, host=...): the uploads are then asynchronous DMA copies."""
+    cs, f, j = prob.csr, prob.force, prob.judge
+    arrays = dict(net_start=cs.net_start, cell32=cs.cell32, off=cs.off, cell_pin=cs.cell_pin, cell_start=cs.cell_start,
+                  size=f.size, ratio=f.ratio, pins=prob.pins, area=prob.area, lo=f.pos_lo, hi=f.pos_hi,
+                  fixed=f.fixed_map)
+    if j is not None:
+        arrays.update(jsize=j.size, jratio=j.ratio, jfixed=j.fixed_map)
+    return {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in arrays.items()}
+
+
 class Placer(object):
     def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None,
-                 sort_every=None):
+                 sort_every=None, host=None):
+        """host: optional {name: pinned CPU tensor} holding the problem's arrays (pinned_inputs), uploaded instead
+        of the Problem's numpy arrays."""
         self.p = prob
         self.dev = torch.device(device or "cuda")
         self.mode = native.FIELD_MODES[field] if isinstance(field, str) else int(field)
@@ -68,39 +82,57 @@ class Placer(object):
         self._graphs = {}
         self._captured = self._replayed = 0
         self._keep = []
+        with torch.cuda.stream(self.stream):       # every upload and set-up kernel in the stream of the passes
+            self._setup(prob, host or {})
+
+    def _setup(self, prob, host):
         dev = self.dev
-        t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev))
+        up = lambda name, a, dt: torch.as_tensor(host[name] if name in host else np.ascontiguousarray(a),
+                                                 dtype=dt).to(dev, non_blocking=True)
+        t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev, non_blocking=True))
         z = lambda shape, dt: self._hold(torch.zeros(shape, dtype=dt, device=dev))
         cs = prob.csr
-        perm, net_start, slot, split = net_order(cs.net_start, cs.cell32, cs.cell_pin)
         n, f, judge = prob.num_nodes, prob.force, prob.judge
-        P = len(perm)
+        P, N = len(cs.cell32), cs.num_nets
         sz = Sizes()
         native.call("gp103_plan_sizes", f.nbx, f.nby, self.mode, ctypes.byref(sz))
         pl = Plan()
-        pl.num_nodes, pl.num_mov, pl.num_nets, pl.num_pins = n, prob.num_mov, cs.num_nets, P
+        pl.num_nodes, pl.num_mov, pl.num_nets, pl.num_pins = n, prob.num_mov, N, P
         pl.nbx, pl.nby = f.nbx, f.nby
         pl.field_mode = self.mode
-        self.pin_cell = t(cs.cell32[perm], torch.int32)
-        self.pin_off = t(cs.off[perm], torch.float32)
-        self.net_start = t(net_start, torch.int32)
-        self.cell_start = t(cs.cell_start, torch.int32)
-        self.pin_slot = t(slot, torch.int32)
+        # the optimised pin set as built, reordered on the device for the WA kernels (gp103_net_order)
+        ns_in, cell_in = up("net_start", cs.net_start, torch.int32), up("cell32", cs.cell32, torch.int32)
+        off_in, cp_in = up("off", cs.off, torch.float32), up("cell_pin", cs.cell_pin, torch.int32)
+        self.cell_start = self._hold(up("cell_start", cs.cell_start, torch.int32))
+        self.pin_cell, self.pin_off = z((max(P, 1),), torch.int32), z((max(P, 1), 2), torch.float32)
+        self.net_start, self.pin_slot = z((N + 1,), torch.int32), z((max(P, 1),), torch.int32)
+        split = torch.zeros(1, dtype=torch.int32, device=dev)
+        scratch = torch.empty(int(native.lib().gp103_net_order_scratch(N, P, prob.num_mov)), dtype=torch.uint8,
+                              device=dev)
+        native.call("gp103_net_order", self._p(ns_in), self._p(cell_in), self._p(off_in), self._p(cp_in), N, P,
+                    prob.num_mov, self._p(scratch), scratch.numel(), self._p(self.net_start), self._p(self.pin_cell),
+                    self._p(self.pin_off), self._p(self.pin_slot), self._p(split), self.stream.cuda_stream)
         pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
-        pl.cell_start, pl.pin_slot, pl.net_split = self._p(self.cell_start), self._p(self.pin_slot), split
-        self.size, self.ratio = t(f.size, torch.float32), t(f.ratio, torch.float32)
-        self.pins, self.area = t(prob.pins, torch.float32), t(prob.area, torch.float32)
-        self.lo, self.hi = t(f.pos_lo, torch.float32), t(f.pos_hi, torch.float32)
+        pl.cell_start, pl.pin_slot = self._p(self.cell_start), self._p(self.pin_slot)
+        pl.net_split = int(split.cpu())
+        del ns_in, cell_in, off_in, cp_in, scratch
+        self.size = self._hold(up("size", f.size, torch.float32))
+        self.ratio = self._hold(up("ratio", f.ratio, torch.float32))
+        self.pins = self._hold(up("pins", prob.pins, torch.float32))
+        self.area = self._hold(up("area", prob.area, torch.float32))
+        self.lo = self._hold(up("lo", f.pos_lo, torch.float32))
+        self.hi = self._hold(up("hi", f.pos_hi, torch.float32))
         for k in ("size", "ratio", "pins", "area", "lo", "hi"):
             setattr(pl, k, self._p(getattr(self, k)))
         pl.bx, pl.by, pl.target = f.bx, f.by, prob.target
-        self.fixed = t(f.fixed_map, torch.float32)
+        self.fixed = self._hold(up("fixed", f.fixed_map, torch.float32))
         pl.fixed = self._p(self.fixed)
         pl.ovf_scale = f.bin_area / f.mov_area
         if judge is not None:
             pl.jnbx, pl.jnby = judge.nbx, judge.nby
-            self.jsize, self.jratio = t(judge.size, torch.float32), t(judge.ratio, torch.float32)
-            self.jfixed = t(judge.fixed_map, torch.float32)
+            self.jsize = self._hold(up("jsize", judge.size, torch.float32))
+            self.jratio = self._hold(up("jratio", judge.ratio, torch.float32))
+            self.jfixed = self._hold(up("jfixed", judge.fixed_map, torch.float32))
             pl.jsize, pl.jratio, pl.jfixed = self._p(self.jsize), self._p(self.jratio), self._p(self.jfixed)
             pl.jbx, pl.jby = judge.bx, judge.by
             pl.jovf_scale = judge.bin_area / judge.mov_area
@@ -201,14 +233,15 @@ class Placer(object):
         with their real sizes on the overflow grid). The whole netlist is uploaded on the first call."""
         p = self.p
         if not hasattr(self, "_ev"):
-            t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.dev)
+            t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.dev, non_blocking=True)
             gr = p.real_judge
-            self._ev = dict(cell=t(p.all_cell, torch.int32), off=t(p.all_off, torch.float32),
-                            start=t(p.all_net_start, torch.int32), size=t(p.nl.size, torch.float32),
-                            fixed=t(gr.fixed_map, torch.float32),
-                            map=torch.zeros((gr.nbx, gr.nby), dtype=torch.int64, device=self.dev),
-                            scratch=torch.zeros(native.EVAL_SCRATCH_BYTES, dtype=torch.uint8, device=self.dev),
-                            out=torch.zeros(2, dtype=torch.float64, device=self.dev), grid=gr)
+            with torch.cuda.stream(self.stream):
+                self._ev = dict(cell=t(p.all_cell, torch.int32), off=t(p.all_off, torch.float32),
+                                start=t(p.all_net_start, torch.int32), size=t(p.nl.size, torch.float32),
+                                fixed=t(gr.fixed_map, torch.float32),
+                                map=torch.zeros((gr.nbx, gr.nby), dtype=torch.int64, device=self.dev),
+                                scratch=torch.zeros(native.EVAL_SCRATCH_BYTES, dtype=torch.uint8, device=self.dev),
+                                out=torch.zeros(2, dtype=torch.float64, device=self.dev), grid=gr)
         e, gr, s = self._ev, self._ev["grid"], self.stream.cuda_stream
         with torch.cuda.stream(self.stream):
             pos = torch.as_tensor(pos, dtype=torch.float32).to(self.dev).contiguous()

@@ -66,6 +66,8 @@ _SIGS = {
     "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
     "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
+    "gp103_net_order_scratch": ([_i, _i, _i], ctypes.c_size_t),
+    "gp103_net_order": ([_vp] * 4 + [_i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 5 + [_vp], _i),
     "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
 }
 EVAL_SCRATCH_BYTES = 16640

@@ -213,6 +213,20 @@ int gp103_field(const gp103_plan* plan, const float* density, float* ex, float* 
 /* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
 int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
 
+/* Set-up of the fused path on the device: the nets of the optimised pin set (Wirelength._pin_set,
+ * src/core/wa_wirelength_hpwl.py:38-46; net_start [num_nets + 1], pin_cell [num_pins] with num_mov for a fixed pin,
+ * pin_off [num_pins, 2], cell_pin [num_pins] = the pins in cell order) reordered for the WA kernels: a stable sort
+ * of the nets by (class, lowest cell), classes 2 pins / 3 pins / 4-8 pins / longer, pins moving with their nets.
+ * Writes net_start_out, pin_cell_out, pin_off_out (the plan's net_start, pin_cell, pin_off), pin_slot (each new
+ * pin's position in cell order: the plan's pin_slot) and *split (device int: the plan's net_split = number of nets
+ * of up to 8 pins). scratch: gp103_net_order_scratch(...) bytes. No counterpart in the reference, whose kernel
+ * reads the nets in their original order. GP103_ERR_TOO_LARGE beyond 4 (num_mov + 1) > 16,777,216. */
+size_t gp103_net_order_scratch(int num_nets, int num_pins, int num_mov);
+int gp103_net_order(const int* net_start, const int* pin_cell, const float* pin_off, const int* cell_pin,
+                    int num_nets, int num_pins, int num_mov, void* scratch, size_t scratch_bytes,
+                    int* net_start_out, int* pin_cell_out, float* pin_off_out, int* pin_slot, int* split,
+                    cudaStream_t stream);
+
 /* ------------------------------------------------------------------------------------------------ part 3
  * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
  * *out is written by the device (read it after synchronising the stream). */
