@@ -389,8 +389,13 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
         }
         j.map[b] = 0ull;
     }
-    double v[1] = {j.exact ? ovd : (double)ov};
-    grid_sum<1>(v, j.red, nblk, bid);
+    if (j.exact) {
+        double v[1] = {ovd};
+        grid_sum<1>(v, j.red, nblk, bid);
+    } else {
+        float v[1] = {ov};
+        grid_sum<1>(v, j.red, nblk, bid);
+    }
 }
 
 int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s) {
@@ -463,7 +468,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     float weight = j.weight_p ? j.weight_p[0] : j.weight;
     float precond = j.precond_p ? j.precond_p[0] : j.precond;
     const bool density = j.ex != nullptr;
-    float d2 = 0.f, l1 = 0.f;                  // per-thread partials (a few nodes); float64 above
+    float d2 = 0.f, l1 = 0.f;                  // per-thread partials (a few nodes); float32 warp trees, float64 across warps and blocks
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.num_nodes; i += gridDim.x * blockDim.x) {
         float gx = 0.f, gy = 0.f;
         if (density) {
@@ -512,7 +517,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
         }
         if (i < j.num_mov) l1 += fabsf(g.x) + fabsf(g.y);
     }
-    double v[2] = {d2, l1};
+    float v[2] = {d2, l1};
     grid_sum<2>(v, j.red);
 }
 

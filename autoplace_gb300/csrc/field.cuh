@@ -14,7 +14,9 @@ struct FieldLayout {
     size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err, work_bytes;
 };
 
-enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2 };
+// PLAIN: float32 [M][N]; TRANS: float32 [N][M] (CUDA-core GEMM); WEIGHT2: the two weighted products of the field;
+// SPLIT: the three bf16 terms of the product, [3][M][N] (tensor-core GEMM)
+enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3 };
 
 struct SGemm {
     int M, N, K;

@@ -24,11 +24,12 @@ constexpr int TC_STAGE_SPACE = 216 * 1024;                       // room for the
 constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_SMEM = TC_STAGE_SPACE + 1024 + 256;
 constexpr long long TC_WAIT_NS = 2000000000LL;                  // a wait that takes 2 s has failed
+constexpr int EPI_BOX = 128 * 128;                               // an epilogue box: 128 rows x 128 bytes
 
 struct TcProblem {
     int M, N, K;
     int epi;
-    __nv_bfloat16* o_terms;      // EPI_TRANS: [3][N][M]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
+    __nv_bfloat16* o_terms;      // EPI_SPLIT: [3][M][N]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
     __nv_bfloat16* o2_terms;
     float* out_f32;              // EPI_PLAIN: [M][N]
     const float4* wrow;          // EPI_WEIGHT2: per row p (kx^2, s kx / bin_x, w_p, 0)
@@ -40,10 +41,17 @@ struct TcProblem {
 // given (smallest first, so the truncating accumulation adds small terms while the sum is small).
 struct TcArgs {
     TcProblem p[2];
-    int na, nb, nprod, stages;
-    int prod_a[6], prod_b[6];
+    int stages;
     int* err;
 };
+
+// The products of a mode, smallest first: bf16x6 (X6 = 1) has 3 terms per operand and 6 products, bf16x3 2 and 3.
+__device__ __forceinline__ constexpr int prod_a(int x6, int q) {
+    return x6 ? (q == 0 ? 2 : q == 1 ? 1 : q == 2 ? 0 : q == 3 ? 1 : 0) : (q == 0 ? 1 : 0);
+}
+__device__ __forceinline__ constexpr int prod_b(int x6, int q) {
+    return x6 ? (q == 0 ? 0 : q == 1 ? 1 : q == 2 ? 2 : q == 3 ? 0 : q == 4 ? 1 : 0) : (q == 1 ? 1 : 0);
+}
 
 // ----------------------------------------------------------------------------- PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -91,6 +99,21 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
         ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
         : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+                 ::"l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"((uint64_t)map), "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, float4 v) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major tile of 128-byte rows, 128-byte swizzle, 8-row groups 1024 bytes apart.
@@ -153,12 +176,16 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16&
 // then stays at float32 level (~2e-7) at every grid size.
 constexpr int TC_THREADS = 192;
 
-template <int BN, int EPI>
+template <int BN, int EPI, int X6>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
-                   const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1, TcArgs args) {
-    pdl_wait();
+                   const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1,
+                   const __grid_constant__ CUtensorMap o0a, const __grid_constant__ CUtensorMap o0b,
+                   const __grid_constant__ CUtensorMap o1a, const __grid_constant__ CUtensorMap o1b, TcArgs args) {
+    // The set-up (barriers, tensor memory, tensor-map prefetch) reads nothing the previous kernel writes: it runs
+    // before griddepcontrol.wait, overlapping the previous kernel's tail.
     constexpr int B_TILE = BN * TC_BK * 2;
+    constexpr int NA = X6 ? 3 : 2, NB = NA, NPROD = X6 ? 6 : 3;
     constexpr uint32_t TMEM_COLS = 2 * BN;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -172,7 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const CUtensorMap* mb = z ? &b1 : &b0;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
     const int total = P.K / TC_BK, stages = args.stages;
-    const int stage_bytes = args.na * TC_A_TILE + args.nb * B_TILE;
+    constexpr int stage_bytes = NA * TC_A_TILE + NB * B_TILE;
     int* err = args.err;
     auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
     auto empty_bar = [&](int s) { return smem_u32(&bars[TC_MAX_STAGES + s]); };
@@ -190,15 +217,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncwarp();                                                // warp 0 converged for the .sync.aligned alloc
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    if (threadIdx.x == 32) {
+        for (const CUtensorMap* m : {ma, mb, z ? &o1a : &o0a, z ? &o1b : &o0b})
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)m) : "memory");
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    pdl_wait();
 
     if (warp == 0) {
         if (lane == 0) {                                         // TMA producer
@@ -208,10 +241,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1)) break;
                 mbar_expect_tx(full_bar(s), stage_bytes);
                 uint8_t* st = smem + s * stage_bytes;
-                for (int t = 0; t < args.na; t++)
+#pragma unroll
+                for (int t = 0; t < NA; t++)
                     tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
-                for (int t = 0; t < args.nb; t++)
-                    tma_load_3d(smem_u32(st + args.na * TC_A_TILE + t * B_TILE), mb, full_bar(s), it * TC_BK, n0, t);
+#pragma unroll
+                for (int t = 0; t < NB; t++)
+                    tma_load_3d(smem_u32(st + NA * TC_A_TILE + t * B_TILE), mb, full_bar(s), it * TC_BK, n0, t);
             }
         }
     } else if (warp == 1) {
@@ -222,15 +257,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (!mbar_wait(acce_bar(b), use ^ 1u, err, 2)) break;
                 if (!mbar_wait(full_bar(s), ph, err, 3)) break;
                 tc_fence_after();
+                // descriptors of the stage's first A and B tiles; a tile or a 16-wide K step further on is the
+                // same descriptor with its start-address field (address / 16) advanced (no carry: smem < 256 KB)
                 const uint32_t st = smem_u32(smem + s * stage_bytes);
+                const uint64_t da = smem_desc(st), db = smem_desc(st + NA * TC_A_TILE);
                 const uint32_t acc = tmem + (uint32_t)(b * BN);
-                for (int q = 0; q < args.nprod; q++) {
-                    const uint32_t sa = st + args.prod_a[q] * TC_A_TILE;
-                    const uint32_t sb = st + args.na * TC_A_TILE + args.prod_b[q] * B_TILE;
+#pragma unroll
+                for (int q = 0; q < NPROD; q++)
 #pragma unroll
                     for (int kk = 0; kk < TC_BK / 16; kk++)
-                        mma_bf16<BN>(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), (q > 0 || kk > 0) ? 1u : 0u);
-                }
+                        mma_bf16<BN>(acc, da + (uint64_t)((prod_a(X6, q) * TC_A_TILE + kk * 32) >> 4),
+                                     db + (uint64_t)((prod_b(X6, q) * B_TILE + kk * 32) >> 4), (q > 0 || kk > 0) ? 1u : 0u);
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
             }
@@ -258,56 +295,87 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(acce_bar(b));
         }
+        // Epilogue: the outputs go through shared memory (the stage buffers, idle now: every TMA load has been
+        // consumed by a completed MMA) in the 128-byte-swizzled layout of 128-row x 128-byte boxes, and leave by
+        // TMA stores, whole lines at a time (a thread holds one output row: direct stores would scatter 16-byte
+        // pieces over 32 rows per instruction).
         ok = ok && *(volatile int*)err == 0;
+        const int r_in = q4 * 32 + lane;                         // row inside the tile
+        auto chunk = [&](int box, int c) {                       // byte offset of 16-byte chunk c of this row
+            return (uint32_t)(box * EPI_BOX + r_in * 128 + ((c ^ (r_in & 7)) << 4));
+        };
+        const uint32_t sbase = smem_u32(smem);
         if (ok) {
-            const int col = n0;
-            if (EPI == EPI_PLAIN) {
-                float4* o = (float4*)(P.out_f32 + (size_t)row * P.N + col);
+            if (EPI == EPI_PLAIN) {                              // float32: boxes of 32 columns
 #pragma unroll
-                for (int i = 0; i < BN / 4; i++) o[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
-            } else if (EPI == EPI_TRANS) {
-                const size_t plane = (size_t)P.M * P.N;
+                for (int c = 0; c < BN / 4; c++)
+                    st_shared_v4(sbase + chunk(c >> 3, c & 7), make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2],
+                                                                          r[4 * c + 3]));
+            } else if (EPI == EPI_SPLIT) {                       // bf16 terms: boxes of 64 columns, term-major
 #pragma unroll
-                for (int i = 0; i < BN; i++) {
-                    __nv_bfloat16 a, bb, c;
-                    split3(r[i], a, bb, c);
-                    const size_t at = (size_t)(col + i) * P.M + row;
-                    P.o_terms[at] = a;
-                    P.o_terms[plane + at] = bb;
-                    P.o_terms[2 * plane + at] = c;
+                for (int c = 0; c < BN / 8; c++) {
+                    __align__(16) __nv_bfloat16 ta[8], tb[8], tc[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) split3(r[8 * c + i], ta[i], tb[i], tc[i]);
+                    const int g = c >> 3;
+                    st_shared_v4(sbase + chunk(0 * (BN / 64) + g, c & 7), *(const float4*)ta);
+                    st_shared_v4(sbase + chunk(1 * (BN / 64) + g, c & 7), *(const float4*)tb);
+                    st_shared_v4(sbase + chunk(2 * (BN / 64) + g, c & 7), *(const float4*)tc);
                 }
             } else {
                 // Kx = K Wx, Ky = K Wy with Wx = (s kx_p / bin_x) w_q r, Wy = (s ky_q / bin_x) w_p r,
-                // r = 1 / (kx_p^2 + ky_q^2) (0 at p = q = 0), from per-row and per-column tables
-                const size_t plane = (size_t)P.M * P.N;
-                const size_t base = (size_t)row * P.N + col;
+                // r = 1 / (kx_p^2 + ky_q^2) (0 at p = q = 0), from per-row and per-column tables; boxes 0-2: the
+                // terms of Kx, 3-5: of Ky (BN = 64: one box per term)
                 const float4 wr = P.wrow[row];
 #pragma unroll
-                for (int c0 = 0; c0 < BN; c0 += 32) {
-                    __align__(16) __nv_bfloat16 xa[32], xb[32], xc[32], ya[32], yb[32], yc[32];
+                for (int c = 0; c < BN / 8; c++) {
+                    __align__(16) __nv_bfloat16 xa[8], xb[8], xc[8], ya[8], yb[8], yc[8];
 #pragma unroll
-                    for (int i = 0; i < 32; i++) {
-                        const float4 wc = P.wcol[col + c0 + i];
+                    for (int i = 0; i < 8; i++) {
+                        const float4 wc = P.wcol[n0 + 8 * c + i];
                         const float t = wr.x + wc.x;
                         const float rr = t > 0.f ? __frcp_rn(t) : 0.f;
-                        split3(r[c0 + i] * (wr.y * wc.z * rr), xa[i], xb[i], xc[i]);
-                        split3(r[c0 + i] * (wc.y * wr.z * rr), ya[i], yb[i], yc[i]);
+                        split3(r[8 * c + i] * (wr.y * wc.z * rr), xa[i], xb[i], xc[i]);
+                        split3(r[8 * c + i] * (wc.y * wr.z * rr), ya[i], yb[i], yc[i]);
                     }
-                    __nv_bfloat16* ox = P.o_terms + base + c0;
-                    __nv_bfloat16* oy = P.o2_terms + base + c0;
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        ((uint4*)ox)[i] = ((uint4*)xa)[i];
-                        ((uint4*)(ox + plane))[i] = ((uint4*)xb)[i];
-                        ((uint4*)(ox + 2 * plane))[i] = ((uint4*)xc)[i];
-                        ((uint4*)oy)[i] = ((uint4*)ya)[i];
-                        ((uint4*)(oy + plane))[i] = ((uint4*)yb)[i];
-                        ((uint4*)(oy + 2 * plane))[i] = ((uint4*)yc)[i];
-                    }
+                    st_shared_v4(sbase + chunk(0, c), *(const float4*)xa);
+                    st_shared_v4(sbase + chunk(1, c), *(const float4*)xb);
+                    st_shared_v4(sbase + chunk(2, c), *(const float4*)xc);
+                    st_shared_v4(sbase + chunk(3, c), *(const float4*)ya);
+                    st_shared_v4(sbase + chunk(4, c), *(const float4*)yb);
+                    st_shared_v4(sbase + chunk(5, c), *(const float4*)yc);
                 }
             }
         }
+        // every reader thread reaches this barrier (all its waits above are bounded), whatever `ok` says
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (warp == 2 && lane == 0 && *(volatile int*)err == 0) {
+            const CUtensorMap* mo = z ? &o1a : &o0a;
+            const CUtensorMap* mo2 = z ? &o1b : &o0b;
+            if (EPI == EPI_PLAIN) {
+#pragma unroll
+                for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, m0);
+            } else if (EPI == EPI_SPLIT) {
+#pragma unroll
+                for (int t = 0; t < 3; t++)
+#pragma unroll
+                    for (int g = 0; g < BN / 64; g++) tma_store_3d(mo, sbase + (t * (BN / 64) + g) * EPI_BOX, n0 + 64 * g, m0, t);
+            } else {
+#pragma unroll
+                for (int t = 0; t < 3; t++) {
+                    tma_store_3d(mo, sbase + t * EPI_BOX, n0, m0, t);
+                    tma_store_3d(mo2, sbase + (3 + t) * EPI_BOX, n0, m0, t);
+                }
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        }
     }
+    // Lane 0 of warps 0 and 1 leaves its role loop long after the other 31 lanes: reconverge every warp before the
+    // block barrier (an aligned barrier reached by a diverged warp can let the block through early), so that the
+    // tensor memory is freed only after every MMA has completed and every reader is done.
+    __syncwarp();
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -344,6 +412,20 @@ static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_
     return r == CUDA_SUCCESS;
 }
 
+// A float32 plane [rows][cols] as a 2-D tensor; box = 32 columns (128 bytes) x 128 rows, 128-byte swizzle.
+static bool make_map_f32(CUtensorMap* m, const void* base, int rows, int cols) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+    cuuint32_t box[2] = {32, (cuuint32_t)TC_BM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 bool field_tc_supported(int nbx, int nby) {
     return nbx >= 128 && nby >= 128 && nbx % 128 == 0 && nby % 128 == 0 && nbx <= 4096 && nby <= 4096;
 }
@@ -354,49 +436,62 @@ struct TcOp {
     TcProblem p;
 };
 
-template <int BN, int EPI>
-static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+template <int BN, int EPI, int X6>
+static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
+        if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI, X6>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
             cudaSuccess)
             return GP103_ERR_CUDA;
         attr = true;
     }
-    CUtensorMap maps[4];
+    CUtensorMap maps[8];
     TcArgs args = {};
     for (int z = 0; z < 2; z++) {
         const TcOp& o = ops[z < nops ? z : 0];
         if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM) || !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, BN))
             return GP103_ERR_CUDA;
+        // outputs (stored by TMA): bf16 terms [3][M][N] as (N, M, term) boxes of 64 x 128; float32 [M][N]
+        CUtensorMap* oa = &maps[4 + 2 * z];
+        CUtensorMap* ob = &maps[5 + 2 * z];
+        bool ok = true;
+        if (EPI == EPI_PLAIN) {
+            ok = make_map_f32(oa, o.p.out_f32, o.p.M, o.p.N);
+            *ob = *oa;
+        } else {
+            ok = make_map(oa, o.p.o_terms, o.p.M, o.p.N, TC_BM);
+            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M, o.p.N, TC_BM);
+            else *ob = *oa;
+        }
+        if (!ok) return GP103_ERR_CUDA;
         args.p[z] = o.p;
     }
-    static const int x3a[3] = {1, 0, 0}, x3b[3] = {0, 1, 0};
-    static const int x6a[6] = {2, 1, 0, 1, 0, 0}, x6b[6] = {0, 1, 2, 0, 1, 0};
-    const bool x3 = mode == GP103_FIELD_BF16X3;
-    args.na = args.nb = x3 ? 2 : 3;
-    args.nprod = x3 ? 3 : 6;
-    args.stages = TC_STAGE_SPACE / (args.na * TC_A_TILE + args.nb * BN * TC_BK * 2);
+    constexpr int terms = X6 ? 3 : 2;
+    args.stages = TC_STAGE_SPACE / (terms * TC_A_TILE + terms * BN * TC_BK * 2);
     if (args.stages > TC_MAX_STAGES) args.stages = TC_MAX_STAGES;
-    for (int i = 0; i < args.nprod; i++) {
-        args.prod_a[i] = x3 ? x3a[i] : x6a[i];
-        args.prod_b[i] = x3 ? x3b[i] : x6b[i];
-    }
     args.err = err;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / BN, p.M / TC_BM, nops);
-    if (launch_k(tc_gemm_kernel<BN, EPI>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2], maps[3], args) != cudaSuccess) return GP103_ERR_CUDA;
+    if (launch_k(tc_gemm_kernel<BN, EPI, X6>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2],
+                 maps[3], maps[4], maps[5], maps[6], maps[7], args) != cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
+}
+
+template <int BN, int EPI>
+static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+    return mode == GP103_FIELD_BF16X3 ? launch_tc_mode<BN, EPI, 0>(ops, nops, err, s)
+                                      : launch_tc_mode<BN, EPI, 1>(ops, nops, err, s);
 }
 
 // One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles. The epilogue is a
 // template argument (every problem of a launch has the same one).
 static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
     const int epi = ops[0].p.epi;
-    if (nops == 1 && epi == EPI_TRANS) return launch_tc_bn<64, EPI_TRANS>(ops, nops, mode, err, s);
+    if (nops == 1 && epi == EPI_SPLIT) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 1 && epi == EPI_WEIGHT2) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
-    if (nops == 2 && epi == EPI_TRANS) return launch_tc_bn<128, EPI_TRANS>(ops, nops, mode, err, s);
+    if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
     return GP103_ERR_ARG;                                        // no other combination is used
 }
@@ -430,8 +525,9 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
         p.M = M; p.N = N; p.K = K; p.epi = epi;
         return p;
     };
-    // 1: Tt = (A Cy^T)^T
-    TcOp o1 = {B(w, L.w_a), X, B(c, L.c_cy), Y, prob(X, Y, Y, EPI_TRANS)};
+    // 1: Tt = (A Cy^T)^T = Cy A^T: Cy as the row operand, the density as the column operand, so the transposed
+    //    product comes out in rows (no transposing epilogue)
+    TcOp o1 = {B(c, L.c_cy), Y, B(w, L.w_a), X, prob(Y, X, Y, EPI_SPLIT)};
     o1.p.o_terms = B(w, L.w_tt);
     if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
     // 2: K = Cx T -> Kx, Ky
@@ -441,9 +537,9 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     o2.p.wrow = (const float4*)(c + L.c_wrow);
     o2.p.wcol = (const float4*)(c + L.c_wcol);
     if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
-    // 3a / 4a: Pt = (Kx Cy)^T, Qt = (Ky Sy)^T
-    TcOp o3[2] = {{B(w, L.w_kx), X, B(c, L.c_cyt), Y, prob(X, Y, Y, EPI_TRANS)},
-                  {B(w, L.w_ky), X, B(c, L.c_syt), Y, prob(X, Y, Y, EPI_TRANS)}};
+    // 3a / 4a: Pt = (Kx Cy)^T = Cy^T Kx^T, Qt = (Ky Sy)^T = Sy^T Ky^T (row operand Cy^T / Sy^T, column operand Kx / Ky)
+    TcOp o3[2] = {{B(c, L.c_cyt), Y, B(w, L.w_kx), X, prob(Y, X, Y, EPI_SPLIT)},
+                  {B(c, L.c_syt), Y, B(w, L.w_ky), X, prob(Y, X, Y, EPI_SPLIT)}};
     o3[0].p.o_terms = B(w, L.w_pt);
     o3[1].p.o_terms = B(w, L.w_qt);
     if ((st = launch_tc(o3, 2, L.mode, err, s))) return st;

@@ -110,6 +110,40 @@ __device__ __forceinline__ void grid_sum(double (&v)[K], const Reduce& r) {
     grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
 }
 
+// Producer side for float32 per-thread partials (the hot kernels): a fixed float32 tree inside each warp, then the
+// warp totals in float64 across the block, so a block spends 1 + log2(warps) float64 warp instructions per value
+// (GB300's float64 rate is 1/64 of its float32 rate: a float64 tree over every lane costs more than the kernel's own
+// arithmetic in the short kernels).
+template <int K>
+__device__ __forceinline__ void grid_sum(float (&v)[K], const Reduce& r, int nblk, int bid) {
+    __shared__ float shf[K * 32];
+    pdl_trigger();
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (l == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) shf[k * 32 + w] = v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double d = l < nw ? (double)shf[k * 32 + l] : 0.0;
+            for (int o = 16; o > 0; o >>= 1)
+                if (o < nw) d += __shfl_down_sync(0xffffffffu, d, o);
+            if (l == 0) r.partials[(size_t)k * MAX_BLOCKS + bid] = d;
+        }
+        if (l == 0 && bid == 0) *r.count = nblk;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void grid_sum(float (&v)[K], const Reduce& r) {
+    grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
+}
+
 // Consumer side (every thread of the block calls it): N totals at once (value k[i] of reduction r[i]), returned to
 // every thread; one sweep over the partials and one block-wide tree.
 template <int N>
@@ -186,11 +220,33 @@ __device__ __forceinline__ unsigned long long fixed32(float f) {
 // Fixed-point charge of one (node, bin) pair: trunc(float(wx * oy) * 2^32).
 __device__ __forceinline__ unsigned long long charge(float wx, float oy) { return fixed32(__fmul_rn(wx, oy)); }
 
-// (float)((double)q / 2^32) of a map entry, without float64 when q < 2^53 (then the double is exact and one
-// rounding to float is all there is).
+// (float)((double)q / 2^32) of a map entry. Below 2^53 the double is exact and one rounding to float is all there
+// is: q 2^-32 rounded to nearest even, built here from q's bits on the integer pipes (64-bit integer conversions
+// run on GB300's float64 pipe, at 1/64 of the float32 rate). The float is m 2^(e - 150) with the 24 leading bits
+// of q as m; the bits shifted out decide the rounding (above half: up; exactly half: up to even). No float denormal
+// can occur: the smallest non-zero value is 2^-32.
 __device__ __forceinline__ float unfixed32(unsigned long long q) {
-    if (q < (1ull << 53)) return __ull2float_rn(q) * 2.3283064365386963e-10f;      // x 2^-32, exact
-    return (float)((double)q / DENSITY_SCALE);
+    if (q >= (1ull << 53)) return (float)((double)q / DENSITY_SCALE);
+    if (q == 0ull) return 0.f;
+    const int msb = 63 - __clzll(q);                       // 0 .. 52
+    unsigned int m;
+    int top = msb;
+    if (msb <= 23) {
+        m = (unsigned int)q << (23 - msb);                 // exact
+    } else {
+        const int sh = msb - 23;                           // 1 .. 29
+        m = (unsigned int)(q >> sh);
+        const unsigned long long rest = q & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rest > half || (rest == half && (m & 1u))) {
+            m += 1u;
+            if (m == (1u << 24)) {                         // carried into a new leading bit
+                m >>= 1;
+                top += 1;
+            }
+        }
+    }
+    // value = m 2^(top - 23 - 32): biased exponent top - 32 + 127
+    return __uint_as_float(((unsigned int)(top + 95) << 23) | (m & 0x7fffffu));
 }
 
 }  // namespace gp103

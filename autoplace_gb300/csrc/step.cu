@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ StepJ
     const float alpha = j.kp[3], coef = j.kp[4];
     const bool copy_best = j.best && j.S && j.S[S_IS_BEST] != 0;
     const float2 *lo = (const float2*)j.lo, *hi = (const float2*)j.hi;
-    float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
+    float d2 = 0.f;                            // per-thread partial (a few nodes); float32 warp tree, float64 across warps and blocks
     // two nodes (four coordinates) per iteration with 16-byte accesses when the node count is even
     const int quads = (j.n & 1) ? 0 : j.n >> 1;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += gridDim.x * blockDim.x) {
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ StepJ
         for (int k = threadIdx.x; k < keys; k += blockDim.x)
             if (hist[k]) atomicAdd(&j.ord.counts[k], hist[k]);
     }
-    double r[1] = {d2};
+    float r[1] = {d2};
     grid_sum<1>(r, j.red);
 }
 
@@ -213,7 +213,7 @@ int launch_step(const StepJob& j, cudaStream_t s) {
 __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step, int n,
                              float2* probe, Reduce red) {
     pdl_wait();
-    float d2 = 0.f;                            // per-thread partial (a few nodes); float64 above
+    float d2 = 0.f;                            // per-thread partial (a few nodes); float32 warp tree, float64 across warps and blocks
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], l = lo[i], h = hi[i];
         const float px = fminf(fmaxf(fmaf(-step, gi.x, vi.x), l.x), h.x);
@@ -222,7 +222,7 @@ __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo,
         const float dx = px - vi.x, dy = py - vi.y;
         d2 += dx * dx + dy * dy;
     }
-    double r[1] = {d2};
+    float r[1] = {d2};
     grid_sum<1>(r, red);
 }
 

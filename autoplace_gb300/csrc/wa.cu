@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
     const int lane = threadIdx.x & 31;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
     const long long chunks = (j.split + 31) / 32;
-    float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float64 above
+    float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float32 warp trees, float64 across warps and blocks
     for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < chunks; it += nwarps) {
         const int i = (int)(it * 32) + lane;
         const bool valid = i < j.split;
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
         }
     }
     if (j.red.partials) {
-        double v[2] = {wa_sum, hp_sum};
+        float v[2] = {wa_sum, hp_sum};
         grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
     }
 }
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ Wa
         }
     }
     if (j.red.partials) {
-        double v[2] = {wa_sum, hp_sum};
+        float v[2] = {wa_sum, hp_sum};
         grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
     }
 }

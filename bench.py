@@ -261,11 +261,11 @@ def roofline(prob, field, prof, peaks, config="c2"):
                "ms_per_launch": round(ml, 4)}
         if k in by:     # algorithmic bytes of the whole pass over the kernel's time per pass (all its launches)
             row["gbs"] = round(by[k] / (v["ms_per_pass"] * 1e-3) / 1e9, 1)
-        if k == "launch_tc_bn":
+        if k == "launch_tc_mode":
             f = tc_flops(prob, field) * (6.0 / v["launches_per_pass"])
             row["tflops"] = round(f / (ml * 1e-3) / 1e12, 1)
         table[k] = row
-    if name == "launch_tc_bn":
+    if name == "launch_tc_mode":
         f = tc_flops(prob, field) * (6.0 / d["launches_per_pass"])
         ach = f / (ms_launch * 1e-3) / 1e12
         r = {"kernel": "tc_gemm_kernel", "bound": "tensor", "achieved": round(ach, 1), "peak": tc,
