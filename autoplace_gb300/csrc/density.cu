@@ -323,6 +323,9 @@ __device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0
     if (terms > 2) t2[at] = __float2bfloat16_rn(__fsub_rn(rem, __bfloat162float(b)));
 }
 
+// EXACT: float64 per-thread partials of the overflow (the evaluators); a template argument, so that the hot path
+// carries no float64 instruction at all (a runtime flag gets both sides if-converted).
+template <bool EXACT>
 __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     pdl_wait();
     const bool second = (int)blockIdx.x >= pair.blocks0;
@@ -347,7 +350,7 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const float o = fmaxf(__fsub_rn(mov[k], j.target), 0.f);
-            if (j.exact) ovd += (double)o; else ov += o;
+            if (EXACT) ovd += (double)o; else ov += o;
         }
         if (j.with_fill) {
             ulonglong2* fill = (ulonglong2*)(j.map + nb);
@@ -380,7 +383,7 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     for (int b = (nb & 3) ? bid * blockDim.x + threadIdx.x : nb; b < nb; b += nblk * blockDim.x) {
         const float mov = __fadd_rn(unfixed32(j.map[b]), j.fixed[b]);
         const float o = fmaxf(__fsub_rn(mov, j.target), 0.f);
-        if (j.exact) ovd += (double)o; else ov += o;
+        if (EXACT) ovd += (double)o; else ov += o;
         if (j.with_fill) {
             const float r = __fadd_rn(mov, unfixed32(j.map[nb + b]));
             if (j.dens) j.dens[b] = r;
@@ -389,7 +392,7 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
         }
         j.map[b] = 0ull;
     }
-    if (j.exact) {
+    if (EXACT) {
         double v[1] = {ovd};
         grid_sum<1>(v, j.red, nblk, bid);
     } else {
@@ -405,7 +408,9 @@ int launch_post_plain(const PostJob* jobs, int njobs, cudaStream_t s) {
     p.njobs = njobs;
     p.blocks0 = grid_for((long long)jobs[0].nbx * jobs[0].nby / 4, 256, 8);
     const int blocks = p.blocks0 + (njobs > 1 ? grid_for((long long)jobs[1].nbx * jobs[1].nby / 4, 256, 8) : 0);
-    if (launch_k(post_plain_kernel, dim3(blocks), dim3(256), 0, s, p) != cudaSuccess) return GP103_ERR_CUDA;
+    const cudaError_t e = jobs[0].exact ? launch_k(post_plain_kernel<true>, dim3(blocks), dim3(256), 0, s, p)
+                                        : launch_k(post_plain_kernel<false>, dim3(blocks), dim3(256), 0, s, p);
+    if (e != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

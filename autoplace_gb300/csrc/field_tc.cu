@@ -133,11 +133,11 @@ __device__ __forceinline__ constexpr uint32_t idesc() {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 }
 
-template <int BN>
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+template <int N>
+__device__ __forceinline__ void mma_n(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<BN>()), "r"(accumulate));
+        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N>()), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -186,7 +186,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // before griddepcontrol.wait, overlapping the previous kernel's tail.
     constexpr int B_TILE = BN * TC_BK * 2;
     constexpr int NA = X6 ? 3 : 2, NB = NA, NPROD = X6 ? 6 : 3;
-    constexpr uint32_t TMEM_COLS = 2 * BN;
+    // BN = 64: the products are grouped by B term into NBLK column blocks of the accumulator (block j = the
+    // products with b_j), so that one MMA can cover several B terms at once (below); BN = 128: one block
+    constexpr bool CONCAT = BN == 64;
+    constexpr int NBLK = CONCAT ? NB : 1;
+    constexpr uint32_t ACC_COLS = (uint32_t)(NBLK * BN);         // per accumulator buffer (two buffers)
+    constexpr uint32_t TMEM_COLS = 2 * ACC_COLS <= 128 ? 128 : 2 * ACC_COLS <= 256 ? 256 : 512;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     // barriers: full[S], empty[S], acc_full[2], acc_empty[2]
@@ -261,13 +266,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 // same descriptor with its start-address field (address / 16) advanced (no carry: smem < 256 KB)
                 const uint32_t st = smem_u32(smem + s * stage_bytes);
                 const uint64_t da = smem_desc(st), db = smem_desc(st + NA * TC_A_TILE);
-                const uint32_t acc = tmem + (uint32_t)(b * BN);
+                const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
+                auto A = [&](int t, int kk) { return da + (uint64_t)((t * TC_A_TILE + kk * 32) >> 4); };
+                auto Bd = [&](int t, int kk) { return db + (uint64_t)((t * B_TILE + kk * 32) >> 4); };
+                if constexpr (CONCAT) {
+                    // B terms are consecutive tiles, so [b0 | b1 | b2] is one operand of N = 192 rows: a_i times
+                    // several B terms is one MMA into consecutive blocks. Per block the order is still smallest
+                    // product first, and each block starts fresh (accumulate = 0) with its first product.
+                    if constexpr (X6) {
 #pragma unroll
-                for (int q = 0; q < NPROD; q++)
+                        for (int kk = 0; kk < 4; kk++) mma_n<64>(acc, A(2, kk), Bd(0, kk), kk > 0);     // a2 b0
+                        mma_n<64>(acc + 64, A(1, 0), Bd(1, 0), 0);                                      // a1 b1
+                        mma_n<64>(acc, A(1, 0), Bd(0, 0), 1);                                           // a1 b0
 #pragma unroll
-                    for (int kk = 0; kk < TC_BK / 16; kk++)
-                        mma_bf16<BN>(acc, da + (uint64_t)((prod_a(X6, q) * TC_A_TILE + kk * 32) >> 4),
-                                     db + (uint64_t)((prod_b(X6, q) * B_TILE + kk * 32) >> 4), (q > 0 || kk > 0) ? 1u : 0u);
+                        for (int kk = 1; kk < 4; kk++) mma_n<128>(acc, A(1, kk), Bd(0, kk), 1);         // a1 [b0 b1]
+                        mma_n<64>(acc + 128, A(0, 0), Bd(2, 0), 0);                                     // a0 b2
+                        mma_n<128>(acc, A(0, 0), Bd(0, 0), 1);                                          // a0 [b0 b1]
+#pragma unroll
+                        for (int kk = 1; kk < 4; kk++) mma_n<192>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1 b2]
+                    } else {
+#pragma unroll
+                        for (int kk = 0; kk < 4; kk++) mma_n<64>(acc, A(1, kk), Bd(0, kk), kk > 0);     // a1 b0
+                        mma_n<64>(acc + 64, A(0, 0), Bd(1, 0), 0);                                      // a0 b1
+                        mma_n<64>(acc, A(0, 0), Bd(0, 0), 1);                                           // a0 b0
+#pragma unroll
+                        for (int kk = 1; kk < 4; kk++) mma_n<128>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1]
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NPROD; q++)
+#pragma unroll
+                        for (int kk = 0; kk < TC_BK / 16; kk++)
+                            mma_n<BN>(acc, A(prod_a(X6, q), kk), Bd(prod_b(X6, q), kk), (q > 0 || kk > 0) ? 1u : 0u);
+                }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
             }
@@ -283,11 +314,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int b = it & 1;
             if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * BN);
+            const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)b * ACC_COLS;
 #pragma unroll
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
                 tmem_ld32(base + (uint32_t)c0, v);
+                if constexpr (NBLK > 1) {                        // blocks of the smaller products: add them first
+                    float w[32];
+                    tmem_ld32(base + (uint32_t)((NBLK - 1) * BN + c0), w);
+                    if constexpr (NBLK > 2) {
+                        float u[32];
+                        tmem_ld32(base + (uint32_t)(BN + c0), u);
+#pragma unroll
+                        for (int i = 0; i < 32; i++) w[i] = __fadd_rn(w[i], u[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 32; i++) v[i] = __fadd_rn(w[i], v[i]);
+                }
 #pragma unroll
                 for (int i = 0; i < 32; i++) r[c0 + i] = __fadd_rn(r[c0 + i], v[i]);
             }

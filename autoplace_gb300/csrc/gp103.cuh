@@ -225,28 +225,41 @@ __device__ __forceinline__ unsigned long long charge(float wx, float oy) { retur
 // run on GB300's float64 pipe, at 1/64 of the float32 rate). The float is m 2^(e - 150) with the 24 leading bits
 // of q as m; the bits shifted out decide the rounding (above half: up; exactly half: up to even). No float denormal
 // can occur: the smallest non-zero value is 2^-32.
-__device__ __forceinline__ float unfixed32(unsigned long long q) {
-    if (q >= (1ull << 53)) return (float)((double)q / DENSITY_SCALE);
-    if (q == 0ull) return 0.f;
-    const int msb = 63 - __clzll(q);                       // 0 .. 52
-    unsigned int m;
+// m 2^(e2 - 32) rounded to float (nearest even), m < 2^54: the float is m' 2^(top - 23 - 32) with the 24 leading
+// bits of m as m' (the bits shifted out decide the rounding: above half up, exactly half up to even).
+__device__ __forceinline__ float round_to_float(unsigned long long m, int e2) {
+    if (m == 0ull) return 0.f;
+    const int msb = 63 - __clzll(m);
+    unsigned int f;
     int top = msb;
     if (msb <= 23) {
-        m = (unsigned int)q << (23 - msb);                 // exact
+        f = (unsigned int)m << (23 - msb);                 // exact
     } else {
-        const int sh = msb - 23;                           // 1 .. 29
-        m = (unsigned int)(q >> sh);
-        const unsigned long long rest = q & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-        if (rest > half || (rest == half && (m & 1u))) {
-            m += 1u;
-            if (m == (1u << 24)) {                         // carried into a new leading bit
-                m >>= 1;
+        const int sh = msb - 23;
+        f = (unsigned int)(m >> sh);
+        const unsigned long long rest = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rest > half || (rest == half && (f & 1u))) {
+            f += 1u;
+            if (f == (1u << 24)) {                         // carried into a new leading bit
+                f >>= 1;
                 top += 1;
             }
         }
     }
-    // value = m 2^(top - 23 - 32): biased exponent top - 32 + 127
-    return __uint_as_float(((unsigned int)(top + 95) << 23) | (m & 0x7fffffu));
+    return __uint_as_float(((unsigned int)(top + e2 + 95) << 23) | (f & 0x7fffffu));
+}
+
+// (float)((double)q / 2^32) of a map entry, on the integer pipes (64-bit integer conversions run on GB300's float64
+// pipe, at 1/64 of the float32 rate). Below 2^53 the double is exact and one rounding to float is all there is; above,
+// q is first rounded to the 53 bits of a double (nearest even), then to float. No float denormal can occur: the
+// smallest non-zero value is 2^-32.
+__device__ __forceinline__ float unfixed32(unsigned long long q) {
+    if (q < (1ull << 53)) return round_to_float(q, 0);
+    const int sh = (63 - __clzll(q)) - 52;                 // 1 .. 11
+    unsigned long long m = q >> sh;
+    const unsigned long long rest = q & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (rest > half || (rest == half && (m & 1ull))) m += 1ull;   // may reach 2^53: still exact below
+    return round_to_float(m, sh);
 }
 
 }  // namespace gp103
