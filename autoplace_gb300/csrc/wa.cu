@@ -28,9 +28,9 @@ __device__ __forceinline__ float2 pin_xy(const WaJob& j, const float2* pos, int 
     return make_float2(q.x + o.x, q.y + o.y);
 }
 
-__device__ __forceinline__ void put(const WaJob& j, int p, float gx, float gy) {
-    j.pin_grad[j.slot ? __ldg(j.slot + p) : p] = make_float2(gx, gy);
-}
+// Where pin p's gradient goes (loaded together with the pin, ahead of the arithmetic that needs the positions).
+__device__ __forceinline__ int slot_of(const WaJob& j, int p) { return j.slot ? __ldg(j.slot + p) : p; }
+__device__ __forceinline__ void put(const WaJob& j, int q, float gx, float gy) { j.pin_grad[q] = make_float2(gx, gy); }
 
 __device__ __forceinline__ float wmax(float v) {
 #pragma unroll
@@ -91,9 +91,11 @@ __device__ __forceinline__ void net_thread(const WaJob& j, const float2* pos, fl
     Net n;
     n.init();
     float2 x[R];
+    int q[R];
 #pragma unroll
     for (int k = 0; k < R; k++)
         if (k < d) {
+            q[k] = slot_of(j, s + k);
             x[k] = pin_xy(j, pos, s + k);
             n.extent(x[k]);
         }
@@ -106,7 +108,7 @@ __device__ __forceinline__ void net_thread(const WaJob& j, const float2* pos, fl
     for (int k = 0; k < R; k++)
         if (k < d) {
             const float2 g = c.grad(n, x[k], ig);
-            put(j, s + k, g.x, g.y);
+            put(j, q[k], g.x, g.y);
         }
     wa = (c.xpx - c.xnx) + (c.xpy - c.xny);
     hp = (n.hx - n.lx) + (n.hy - n.ly);
@@ -120,9 +122,11 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
     Coef c;
     if (d <= 32 * WA_WREG) {
         float2 x[WA_WREG];
+        int q[WA_WREG];
 #pragma unroll
         for (int t = 0; t < WA_WREG; t++)
             if (lane + 32 * t < d) {
+                q[t] = slot_of(j, s + lane + 32 * t);
                 x[t] = pin_xy(j, pos, s + lane + 32 * t);
                 n.extent(x[t]);
             }
@@ -137,7 +141,7 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
         for (int t = 0; t < WA_WREG; t++)
             if (lane + 32 * t < d) {
                 const float2 g = c.grad(n, x[t], ig);
-                put(j, s + lane + 32 * t, g.x, g.y);
+                put(j, q[t], g.x, g.y);
             }
     } else {                                             // very long nets: three passes, pins re-read (cached)
         for (int p = lane; p < d; p += 32) n.extent(pin_xy(j, pos, s + p));
@@ -148,7 +152,7 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
         c.from(n);
         for (int p = lane; p < d; p += 32) {
             const float2 g = c.grad(n, pin_xy(j, pos, s + p), ig);
-            put(j, s + p, g.x, g.y);
+            put(j, slot_of(j, s + p), g.x, g.y);
         }
     }
     wa = (c.xpx - c.xnx) + (c.xpy - c.xny);
@@ -160,6 +164,7 @@ __device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, floa
 // of the low pin are exp(0) = 1 (both 1 when the pins coincide) -- the values the general form computes, with one
 // exponential instead of four per axis.
 __device__ __forceinline__ void net_two(const WaJob& j, const float2* pos, float ig, int s, float& wa, float& hp) {
+    const int qa = slot_of(j, s), qb = slot_of(j, s + 1);
     const float2 a = pin_xy(j, pos, s), b = pin_xy(j, pos, s + 1);
     float g[2][2], wsum = 0.f, hsum = 0.f;
 #pragma unroll
@@ -177,8 +182,8 @@ __device__ __forceinline__ void net_two(const WaJob& j, const float2* pos, float
         wsum += xp - xn;
         hsum += hi - lo;
     }
-    put(j, s, g[0][0], g[0][1]);
-    put(j, s + 1, g[1][0], g[1][1]);
+    put(j, qa, g[0][0], g[0][1]);
+    put(j, qb, g[1][0], g[1][1]);
     wa = wsum;
     hp = hsum;
 }
