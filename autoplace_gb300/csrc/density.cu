@@ -465,6 +465,12 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
 // gradients in the reference's order (cell CSR: contiguous when the pin gradients are stored in cell order, else
 // through cell_pin); the new gradient, its squared distance to the previous one and its L1 norm over the cells
 // reduced in float64.
+// Every load a node needs is issued in two waves: its own data (position, size, ratio, pin range, pins, area,
+// reference gradient), then the field values of its bins and its pins' gradients, all predicated and unrolled for
+// the common shapes (spans of up to 3 bins per axis, up to GATHER_PINS pins), so that a thread waits for two
+// memory latencies per node rather than one per bin and per pin.
+constexpr int GATHER_PINS = 8;
+
 __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
@@ -475,52 +481,106 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     const bool density = j.ex != nullptr;
     float d2 = 0.f, l1 = 0.f;                  // per-thread partials (a few nodes); float32 warp trees, float64 across warps and blocks
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.num_nodes; i += gridDim.x * blockDim.x) {
+        // wave 1: the node's own data
+        const bool cell = i < j.num_mov;
+        const bool wl = j.with_wl && cell;
+        float2 p = make_float2(0.f, 0.f), sz = make_float2(0.f, 0.f);
+        float r = 0.f;
+        if (density) {
+            p = pos[i];
+            sz = j.size[i];
+            r = j.ratio[i];
+        }
+        int k0 = 0, k1 = 0;
+        if (wl) {
+            k0 = j.cell_start[i];
+            k1 = j.cell_start[i + 1];
+        }
+        const float pins = j.pins[i];
+        const float area = density && precond >= 0.f ? j.area[i] : 0.f;
+        const float2 o = gref ? gref[i] : make_float2(0.f, 0.f);
+        // wave 2: field values and pin gradients
         float gx = 0.f, gy = 0.f;
         if (density) {
-            const float2 p = pos[i], sz = j.size[i];
             const Span sx = span(p.x, sz.x, j.inv_bx, j.nbx), sy = span(p.y, sz.y, j.inv_by, j.nby);
-            const float r = j.ratio[i];
-            for (int x = sx.b0; x <= sx.b1; x++) {
-                const float wx = __fmul_rn(r, overlap(sx, x));
-                const float* ex = j.ex + (size_t)x * j.nby;
-                const float* ey = j.ey + (size_t)x * j.nby;
-                for (int y = sy.b0; y <= sy.b1; y++) {
-                    const float w = __fmul_rn(wx, overlap(sy, y));
-                    gx = fmaf(-w, ex[y], gx);
-                    gy = fmaf(-w, ey[y], gy);
+            const int nx = sx.b1 - sx.b0, ny = sy.b1 - sy.b0;
+            if (nx >= 0 && ny >= 0 && nx <= 2 && ny <= 2) {
+                float fx[3][3], fy[3][3];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const bool in = a <= nx && c <= ny;
+                        const size_t at = (size_t)(sx.b0 + a) * j.nby + (sy.b0 + c);
+                        fx[a][c] = in ? j.ex[at] : 0.f;
+                        fy[a][c] = in ? j.ey[at] : 0.f;
+                    }
+                float ox[3], oy[3];
+                overlaps3(sx, ox);
+                overlaps3(sy, oy);
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    if (a > nx) break;
+                    const float wx = __fmul_rn(r, ox[a]);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        if (c > ny) break;
+                        const float w = __fmul_rn(wx, oy[c]);
+                        gx = fmaf(-w, fx[a][c], gx);
+                        gy = fmaf(-w, fy[a][c], gy);
+                    }
+                }
+            } else {
+                for (int x = sx.b0; x <= sx.b1; x++) {
+                    const float wx = __fmul_rn(r, overlap(sx, x));
+                    const float* ex = j.ex + (size_t)x * j.nby;
+                    const float* ey = j.ey + (size_t)x * j.nby;
+                    for (int y = sy.b0; y <= sy.b1; y++) {
+                        const float w = __fmul_rn(wx, overlap(sy, y));
+                        gx = fmaf(-w, ex[y], gx);
+                        gy = fmaf(-w, ey[y], gy);
+                    }
                 }
             }
             gx *= weight;
             gy *= weight;
         }
         float wx = 0.f, wy = 0.f;
-        if (j.with_wl && i < j.num_mov) {
-            const int k0 = j.cell_start[i], k1 = j.cell_start[i + 1];
-            for (int k = k0; k < k1; k++) {
-                const float2 q = j.pin_grad[j.cell_pin ? j.cell_pin[k] : k];
-                wx += q.x;
-                wy += q.y;
+        if (wl) {
+            float2 q[GATHER_PINS];
+#pragma unroll
+            for (int t = 0; t < GATHER_PINS; t++)
+                q[t] = k0 + t < k1 ? j.pin_grad[j.cell_pin ? j.cell_pin[k0 + t] : k0 + t] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < GATHER_PINS; t++) {           // in cell_pin order, as the reference sums
+                if (k0 + t >= k1) break;
+                wx += q[t].x;
+                wy += q[t].y;
+            }
+            for (int k = k0 + GATHER_PINS; k < k1; k++) {
+                const float2 qq = j.pin_grad[j.cell_pin ? j.cell_pin[k] : k];
+                wx += qq.x;
+                wy += qq.y;
             }
         }
         float2 g;
         if (density) {
             gx += wx;
             gy += wy;
-            const float scale = precond < 0.f ? 1.f : 1.f / fmaxf(j.pins[i] + precond * j.area[i], 1.f);
+            const float scale = precond < 0.f ? 1.f : 1.f / fmaxf(pins + precond * area, 1.f);
             g = make_float2(gx * scale, gy * scale);
-        } else if (i < j.num_mov) {                     // wirelength only: wl_grad / max(1, pins)
-            const float pc = fmaxf(j.pins[i], 1.f);
+        } else if (cell) {                              // wirelength only: wl_grad / max(1, pins)
+            const float pc = fmaxf(pins, 1.f);
             g = make_float2(wx / pc, wy / pc);
         } else {
             g = make_float2(0.f, 0.f);
         }
         gout[i] = g;
         if (gref) {
-            const float2 o = gref[i];
             const float dx = g.x - o.x, dy = g.y - o.y;
             d2 += dx * dx + dy * dy;
         }
-        if (i < j.num_mov) l1 += fabsf(g.x) + fabsf(g.y);
+        if (cell) l1 += fabsf(g.x) + fabsf(g.y);
     }
     float v[2] = {d2, l1};
     grid_sum<2>(v, j.red);
