@@ -103,6 +103,7 @@ extern "C" int gp103_wa(const float* pos, const int* pin_cell, const float* pin_
         j.num_nets = num_nets;
         j.num_mov = num_mov;
         j.split = num_nets;
+        j.mid = num_nets;
         j.gamma = gamma;
         j.pin_grad = (float2*)pin_grad;
         j.out = (float2*)out;
@@ -185,7 +186,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
         OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
-        OFF(order), OFF(order_counts), OFF(order_cursor)};
+        OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -210,6 +211,7 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->field_const && p->field_work && p->ex && p->ey && p->red && p->counters && p->map && p->kp);
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
     REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
+    REQUIRE(p->net_mid == 0 || (p->net_mid >= p->net_split && p->net_mid <= p->num_nets));
     REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
     REQUIRE((p->order == nullptr) == (p->order_counts == nullptr) && (p->order == nullptr) == (p->order_cursor == nullptr));
     if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
@@ -349,6 +351,7 @@ static WaJob wa_job(const gp103_plan* p) {
     w.num_nets = p->num_nets;
     w.num_mov = p->num_mov;
     w.split = p->net_split;
+    w.mid = p->net_mid > 0 ? p->net_mid : p->net_split;
     w.slot = p->pin_slot;
     w.gamma = p->kp;
     w.pin_grad = (float2*)p->pin_grad;

@@ -3,7 +3,7 @@
 // Input: the optimised pin set as AutoPlace builds it (Wirelength._pin_set, src/core/wa_wirelength_hpwl.py:38-46):
 // pins grouped by net (net_start, cell per pin with num_mov for a fixed pin, offsets) and the pins in cell order
 // (cell_pin). Output: the same nets reordered for the WA kernels (short nets by class of degree 2 / 3 / 4-8, each
-// class by the net's lowest cell, then the long nets), their pins moved with them, and for every pin its position
+// class by the net's lowest cell, then the nets of 9-32 pins and the longer ones, likewise), their pins moved with them, and for every pin its position
 // in cell order (pin_slot), where the WA kernels write its gradient. The order is exactly a stable sort of the nets
 // by (class, lowest cell): a counting sort over the keys, ties put back in net order, so the result is the same
 // on every run.
@@ -13,10 +13,14 @@
 namespace gp103 {
 
 constexpr int NO_SHORT = 8;               // nets of up to 8 pins are short (one thread each in the WA kernels)
+constexpr int NO_MID = 32;                // nets of 9 .. 32 pins: 8 lanes each; longer: a warp each
+constexpr int NO_CLASSES = 5;
 constexpr int SCAN_TILE = 4096;           // elements per block of the scans (256 threads x 16)
 constexpr int SCAN_MAX_TILES = 4096;      // one block scans the tile sums: scans of up to 16.7M elements
 
-__device__ __forceinline__ int net_class(int deg) { return deg == 2 ? 0 : deg == 3 ? 1 : deg <= NO_SHORT ? 2 : 3; }
+__device__ __forceinline__ int net_class(int deg) {
+    return deg == 2 ? 0 : deg == 3 ? 1 : deg <= NO_SHORT ? 2 : deg <= NO_MID ? 3 : 4;
+}
 
 // key of a net = class * (num_mov + 1) + lowest cell (a cell index in [0, num_mov]); count per key
 __global__ void __launch_bounds__(256) net_key_kernel(const int* ns, const int* cell, int num_nets, int num_mov,
@@ -188,10 +192,13 @@ __global__ void __launch_bounds__(256) pin_slot_kernel(const int* cell_pin, cons
         slot[newpos[cell_pin[k]]] = k;
 }
 
-// split = number of short nets = start of the first key of class 3
-__global__ void net_split_kernel(const int* start, int key3, int num_nets, int keys, int* split) {
+// split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 32 pins (class 4)
+__global__ void net_split_kernel(const int* start, int stride, int num_nets, int keys, int* split) {
     pdl_wait();
-    *split = key3 < keys ? start[key3] : num_nets;
+    for (int c = 0; c < 2; c++) {
+        const int k = (3 + c) * stride;
+        split[c] = k < keys ? start[k] : num_nets;
+    }
 }
 
 struct NetOrderScratch {
@@ -201,7 +208,7 @@ struct NetOrderScratch {
 static NetOrderScratch net_order_scratch(long long num_nets, long long num_pins, long long num_mov) {
     NetOrderScratch s = {};
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t keys = (size_t)4 * (size_t)(num_mov + 1);
+    const size_t keys = (size_t)NO_CLASSES * (size_t)(num_mov + 1);
     size_t at = 0;
     s.key = at; at += al(sizeof(int) * (size_t)num_nets);
     s.count = at; at += al(sizeof(int) * keys);
@@ -233,7 +240,7 @@ extern "C" int gp103_net_order(const int* net_start, const int* pin_cell, const 
         return GP103_ERR_ARG;
     if (num_pins > 0 && (!pin_cell || !pin_off || !cell_pin || !pin_cell_out || !pin_off_out || !pin_slot))
         return GP103_ERR_ARG;
-    const long long keys = 4LL * ((long long)num_mov + 1);
+    const long long keys = (long long)NO_CLASSES * ((long long)num_mov + 1);
     if (keys > (long long)SCAN_TILE * SCAN_MAX_TILES || num_nets + 1LL > (long long)SCAN_TILE * SCAN_MAX_TILES)
         return GP103_ERR_TOO_LARGE;
     const NetOrderScratch L = net_order_scratch(num_nets, num_pins, num_mov);
@@ -283,7 +290,7 @@ extern "C" int gp103_net_order(const int* net_start, const int* pin_cell, const 
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
-    if (launch_k(net_split_kernel, dim3(1), dim3(1), 0, s, (const int*)start, 3 * (num_mov + 1), num_nets, K,
+    if (launch_k(net_split_kernel, dim3(1), dim3(1), 0, s, (const int*)start, num_mov + 1, num_nets, K,
                  split) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();

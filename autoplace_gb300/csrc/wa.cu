@@ -32,19 +32,23 @@ __device__ __forceinline__ float2 pin_xy(const WaJob& j, const float2* pos, int 
 __device__ __forceinline__ int slot_of(const WaJob& j, int p) { return j.slot ? __ldg(j.slot + p) : p; }
 __device__ __forceinline__ void put(const WaJob& j, int q, float gx, float gy) { j.pin_grad[q] = make_float2(gx, gy); }
 
-__device__ __forceinline__ float wmax(float v) {
+// Butterfly reductions over aligned groups of L lanes (the whole warp takes part; each group gets its own value).
+template <int L>
+__device__ __forceinline__ float gmax(float v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = L / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ float wmin(float v) {
+template <int L>
+__device__ __forceinline__ float gmin(float v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = L / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ float wsum(float v) {
+template <int L>
+__device__ __forceinline__ float gsum(float v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
@@ -114,49 +118,57 @@ __device__ __forceinline__ void net_thread(const WaJob& j, const float2* pos, fl
     hp = (n.hx - n.lx) + (n.hy - n.ly);
 }
 
-// A longer net by the whole warp (every lane ends with the net's values).
-__device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, float ig, int s, int d, int lane,
-                                         float& wa, float& hp) {
+// A longer net by a group of L lanes (every lane of the group ends with the net's values; `gl` = lane in the group).
+// Up to L * WA_WREG pins stay in registers; longer nets take three passes over their pins (re-read, cached). The
+// whole warp must call it together (the reductions are warp shuffles); d = 0 for a group with no net.
+template <int L>
+__device__ __forceinline__ void net_group(const WaJob& j, const float2* pos, float ig, int s, int d, int gl,
+                                          float& wa, float& hp) {
     Net n;
     n.init();
     Coef c;
-    if (d <= 32 * WA_WREG) {
+    if (__all_sync(0xffffffffu, d <= L * WA_WREG)) {
         float2 x[WA_WREG];
         int q[WA_WREG];
 #pragma unroll
         for (int t = 0; t < WA_WREG; t++)
-            if (lane + 32 * t < d) {
-                q[t] = slot_of(j, s + lane + 32 * t);
-                x[t] = pin_xy(j, pos, s + lane + 32 * t);
+            if (gl + L * t < d) {
+                q[t] = slot_of(j, s + gl + L * t);
+                x[t] = pin_xy(j, pos, s + gl + L * t);
                 n.extent(x[t]);
             }
-        n.hx = wmax(n.hx); n.lx = wmin(n.lx); n.hy = wmax(n.hy); n.ly = wmin(n.ly);
+        n.hx = gmax<L>(n.hx); n.lx = gmin<L>(n.lx); n.hy = gmax<L>(n.hy); n.ly = gmin<L>(n.ly);
 #pragma unroll
         for (int t = 0; t < WA_WREG; t++)
-            if (lane + 32 * t < d) n.add(x[t], ig);
-        n.spx = wsum(n.spx); n.snx = wsum(n.snx); n.xpx = wsum(n.xpx); n.xnx = wsum(n.xnx);
-        n.spy = wsum(n.spy); n.sny = wsum(n.sny); n.xpy = wsum(n.xpy); n.xny = wsum(n.xny);
+            if (gl + L * t < d) n.add(x[t], ig);
+        n.spx = gsum<L>(n.spx); n.snx = gsum<L>(n.snx); n.xpx = gsum<L>(n.xpx); n.xnx = gsum<L>(n.xnx);
+        n.spy = gsum<L>(n.spy); n.sny = gsum<L>(n.sny); n.xpy = gsum<L>(n.xpy); n.xny = gsum<L>(n.xny);
         c.from(n);
 #pragma unroll
         for (int t = 0; t < WA_WREG; t++)
-            if (lane + 32 * t < d) {
+            if (gl + L * t < d) {
                 const float2 g = c.grad(n, x[t], ig);
                 put(j, q[t], g.x, g.y);
             }
     } else {                                             // very long nets: three passes, pins re-read (cached)
-        for (int p = lane; p < d; p += 32) n.extent(pin_xy(j, pos, s + p));
-        n.hx = wmax(n.hx); n.lx = wmin(n.lx); n.hy = wmax(n.hy); n.ly = wmin(n.ly);
-        for (int p = lane; p < d; p += 32) n.add(pin_xy(j, pos, s + p), ig);
-        n.spx = wsum(n.spx); n.snx = wsum(n.snx); n.xpx = wsum(n.xpx); n.xnx = wsum(n.xnx);
-        n.spy = wsum(n.spy); n.sny = wsum(n.sny); n.xpy = wsum(n.xpy); n.xny = wsum(n.xny);
+        for (int p = gl; p < d; p += L) n.extent(pin_xy(j, pos, s + p));
+        n.hx = gmax<L>(n.hx); n.lx = gmin<L>(n.lx); n.hy = gmax<L>(n.hy); n.ly = gmin<L>(n.ly);
+        for (int p = gl; p < d; p += L) n.add(pin_xy(j, pos, s + p), ig);
+        n.spx = gsum<L>(n.spx); n.snx = gsum<L>(n.snx); n.xpx = gsum<L>(n.xpx); n.xnx = gsum<L>(n.xnx);
+        n.spy = gsum<L>(n.spy); n.sny = gsum<L>(n.sny); n.xpy = gsum<L>(n.xpy); n.xny = gsum<L>(n.xny);
         c.from(n);
-        for (int p = lane; p < d; p += 32) {
+        for (int p = gl; p < d; p += L) {
             const float2 g = c.grad(n, pin_xy(j, pos, s + p), ig);
             put(j, slot_of(j, s + p), g.x, g.y);
         }
     }
     wa = (c.xpx - c.xnx) + (c.xpy - c.xny);
     hp = (n.hx - n.lx) + (n.hy - n.ly);
+}
+
+__device__ __forceinline__ void net_warp(const WaJob& j, const float2* pos, float ig, int s, int d, int lane,
+                                         float& wa, float& hp) {
+    net_group<32>(j, pos, ig, s, d, lane, wa, hp);
 }
 
 // A 2-pin net by one thread. Per axis the two pins share one exponential: with hi / lo the larger / smaller
@@ -239,22 +251,45 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
     }
 }
 
-// Long nets [split, num_nets), one per warp.
+// Long nets [split, num_nets): nets [split, mid) (9 .. 32 pins) by groups of 8 lanes, four per warp item; nets
+// [mid, num_nets) one per warp.
+constexpr int WA_GROUP = 8;
+
 __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
     pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, gl = lane & (WA_GROUP - 1), gi = lane / WA_GROUP;
     const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const int groups = (j.mid - j.split + 32 / WA_GROUP - 1) / (32 / WA_GROUP);
+    const int items = groups + (j.num_nets - j.mid);
     float wa_sum = 0.f, hp_sum = 0.f;
-    for (int i = j.split + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < j.num_nets; i += nwarps) {
-        const int s = j.net_start[i], d = j.net_start[i + 1] - s;
-        float wa, hp;
-        net_warp(j, pos, ig, s, d, lane, wa, hp);
-        if (lane == 0) {
-            if (j.out) j.out[i] = make_float2(wa, hp);
-            wa_sum += wa;
-            hp_sum += hp;
+    for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
+        if (it < groups) {                                   // uniform over the warp
+            const int i = j.split + it * (32 / WA_GROUP) + gi;
+            const bool valid = i < j.mid;
+            int s = 0, d = 0;
+            if (valid) {
+                s = j.net_start[i];
+                d = j.net_start[i + 1] - s;
+            }
+            float wa, hp;
+            net_group<WA_GROUP>(j, pos, ig, s, d, gl, wa, hp);
+            if (valid && gl == 0) {
+                if (j.out) j.out[i] = make_float2(wa, hp);
+                wa_sum += wa;
+                hp_sum += hp;
+            }
+        } else {
+            const int i = j.mid + (it - groups);
+            const int s = j.net_start[i], d = j.net_start[i + 1] - s;
+            float wa, hp;
+            net_warp(j, pos, ig, s, d, lane, wa, hp);
+            if (lane == 0) {
+                if (j.out) j.out[i] = make_float2(wa, hp);
+                wa_sum += wa;
+                hp_sum += hp;
+            }
         }
     }
     if (j.red.partials) {
@@ -264,7 +299,8 @@ __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ Wa
 }
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
-    const long long chunks = (j.split + 31) / 32, longs = j.num_nets - j.split;
+    const long long chunks = (j.split + 31) / 32;
+    const long long longs = (j.mid - j.split + 3) / 4 + (j.num_nets - j.mid);     // warp items of the long kernel
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
     const int g1 = chunks > 0 || longs == 0 ? grid_for(chunks * 32, 256, 8) : 0;
     const int g2 = longs > 0 ? grid_for(longs * 32, 256, 4) : 0;

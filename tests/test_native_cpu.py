@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from autoplace_gb300 import native, problem, synth
-from autoplace_gb300.engine import SHORT_NET, net_order
+from autoplace_gb300.engine import MID_NET, SHORT_NET, net_order
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -64,10 +64,11 @@ def test_argument_errors_without_gpu():
 def test_net_order_keeps_nets_and_cell_sums():
     nl = synth.make_netlist(3000, 3100, window=60, macros=3, cover=0.1, fixed_pin_share=0.05, seed=4)
     cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
-    perm, ns, slot, split = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    perm, ns, slot, split, mid = net_order(cs.net_start, cs.cell32, cs.cell_pin)
     deg = np.diff(ns)
     assert np.all(deg[:split] <= SHORT_NET) and np.all(deg[split:] > SHORT_NET)
-    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, 3)))
+    assert np.all(deg[split:mid] <= MID_NET) and np.all(deg[mid:] > MID_NET)
+    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, np.where(deg <= MID_NET, 3, 4))))
     assert np.all(np.diff(cls) >= 0)                       # classes in order
     assert sorted(perm.tolist()) == list(range(len(perm)))  # a permutation of the pins
     assert sorted(slot.tolist()) == list(range(len(slot)))
@@ -84,6 +85,6 @@ def test_net_order_keeps_nets_and_cell_sums():
     assert np.array_equal(cell_order, cs.cell_pin)
     # short nets of one class are ordered by their lowest cell
     first = np.minimum.reduceat(cs.cell32[perm], ns[:-1])
-    for c in range(3):
+    for c in range(5):
         f = first[cls == c]
         assert np.all(np.diff(f) >= 0)
