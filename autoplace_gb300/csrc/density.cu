@@ -18,9 +18,9 @@ namespace gp103 {
 // charges there and then adds every non-zero bin to the global map once; otherwise it adds each charge to the global
 // map directly (64-bit atomics in L2).
 constexpr int SCAT_THREADS = 256;
-constexpr int SCAT_PER_THREAD = 4;
+constexpr int SCAT_PER_THREAD = 2;
 constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;
-constexpr int SCAT_SMEM_BINS = 6144;      // 2 x 24 KB of 32-bit words
+constexpr int SCAT_SMEM_BINS = 3072;      // 2 x 12 KB of 32-bit words
 constexpr float TWO32 = 4294967296.f, TWO33 = 8589934592.f, TWO_M32 = 2.3283064365386963e-10f;
 
 __device__ __forceinline__ void red_shared(unsigned int* a, unsigned int v) {
