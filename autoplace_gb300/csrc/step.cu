@@ -33,8 +33,8 @@ int launch_nesterov_step(const float* u, const float* v, const float* g, const f
 }
 
 // One pass of the control, float64, in the order of control_kernel (gp_cuda_kernel.cu:183-240). -> accepted.
-__device__ bool control_body(double* S, float* kp, const double* c, double moved, double turned, double hpwl,
-                             double ovf, double wa) {
+__device__ __forceinline__ bool control_body(double* S, float* kp, const double* c, double moved, double turned,
+                                             double hpwl, double ovf, double wa) {
     S[S_ACCEPT] = 0;
     S[S_IS_BEST] = 0;
     if (S[S_STOP] != 0) return false;
@@ -242,10 +242,28 @@ __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp
     pdl_wait();
     const Reduce r[5] = {moved2, grad, wa_hpwl, wa_hpwl, ovf_sum};
     const int k[5] = {0, 0, 0, 1, 0};
+    // the state and the constants in registers first (one wave of loads): the control reads them one after another,
+    // and through global memory every read after a write would wait a full memory latency
+    double Sl[S_SIZE], cl[C_SIZE];
+    float kpl[5];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < S_SIZE; i++) Sl[i] = S[i];
+#pragma unroll
+        for (int i = 0; i < C_SIZE; i++) cl[i] = c[i];
+#pragma unroll
+        for (int i = 0; i < 5; i++) kpl[i] = kp[i];
+    }
     double t[5];
     block_totals<5>(r, k, t);
-    if (threadIdx.x == 0 && control_body(S, kp, c, sqrt(t[0]), sqrt(t[1]), t[3], t[4] * ovf_scale, t[2]))
-        *cur = 1 - *cur;
+    if (threadIdx.x == 0) {
+        const bool accepted = control_body(Sl, kpl, cl, sqrt(t[0]), sqrt(t[1]), t[3], t[4] * ovf_scale, t[2]);
+#pragma unroll
+        for (int i = 0; i < S_SIZE; i++) S[i] = Sl[i];
+#pragma unroll
+        for (int i = 0; i < 5; i++) kp[i] = kpl[i];
+        if (accepted) *cur = 1 - *cur;
+    }
 }
 
 int launch_control_fused(double* S, float* kp, const double* c, Reduce moved2, Reduce grad, Reduce wa_hpwl,
