@@ -160,6 +160,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 1 / t for the field weights (t > 0 normal): the hardware approximation refined by one Newton-Raphson step,
+// r' = r + r (1 - t r), within an ulp of the rounded reciprocal (the weights need float32 accuracy, not rounding).
+__device__ __forceinline__ float recip(float t) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+    return fmaf(r, fmaf(-t, r, 1.f), r);
+}
+
 __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16& b, __nv_bfloat16& c) {
     a = __float2bfloat16_rn(v);
     const float r1 = __fsub_rn(v, __bfloat162float(a));
@@ -306,6 +314,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else {                                                     // readers + epilogue
         const int q4 = warp & 3;                                 // tensor-memory lane quarter
         const int row = m0 + q4 * 32 + lane;
+        const float4 wr = EPI == EPI_WEIGHT2 ? P.wrow[row] : make_float4(0.f, 0.f, 0.f, 0.f);   // loaded early
         float r[BN];
 #pragma unroll
         for (int i = 0; i < BN; i++) r[i] = 0.f;
@@ -348,6 +357,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             return (uint32_t)(box * EPI_BOX + r_in * 128 + ((c ^ (r_in & 7)) << 4));
         };
         const uint32_t sbase = smem_u32(smem);
+        // the weighted epilogue's column weights: this tile's BN entries into shared memory (one wave of loads, read
+        // back as broadcasts), behind the six output boxes
+        const float4* wsh = (const float4*)(smem + 6 * EPI_BOX);
+        if (EPI == EPI_WEIGHT2) {
+            if (r_in < BN) ((float4*)(smem + 6 * EPI_BOX))[r_in] = P.wcol[n0 + r_in];
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+        }
         if (ok) {
             if (EPI == EPI_PLAIN) {                              // float32: boxes of 32 columns
 #pragma unroll
@@ -369,15 +385,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 // Kx = K Wx, Ky = K Wy with Wx = (s kx_p / bin_x) w_q r, Wy = (s ky_q / bin_x) w_p r,
                 // r = 1 / (kx_p^2 + ky_q^2) (0 at p = q = 0), from per-row and per-column tables; boxes 0-2: the
                 // terms of Kx, 3-5: of Ky (BN = 64: one box per term)
-                const float4 wr = P.wrow[row];
 #pragma unroll
                 for (int c = 0; c < BN / 8; c++) {
                     __align__(16) __nv_bfloat16 xa[8], xb[8], xc[8], ya[8], yb[8], yc[8];
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
-                        const float4 wc = P.wcol[n0 + 8 * c + i];
+                        const float4 wc = wsh[8 * c + i];
                         const float t = wr.x + wc.x;
-                        const float rr = t > 0.f ? __frcp_rn(t) : 0.f;
+                        const float rr = t > 0.f ? recip(t) : 0.f;
                         split3(r[8 * c + i] * (wr.y * wc.z * rr), xa[i], xb[i], xc[i]);
                         split3(r[8 * c + i] * (wc.y * wr.z * rr), ya[i], yb[i], yc[i]);
                     }
