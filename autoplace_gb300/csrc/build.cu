@@ -15,8 +15,7 @@ namespace gp103 {
 constexpr int NO_SHORT = 8;               // nets of up to 8 pins are short (one thread each in the WA kernels)
 constexpr int NO_MID = 32;                // nets of 9 .. 32 pins: 8 lanes each; longer: a warp each
 constexpr int NO_CLASSES = 5;
-constexpr int SCAN_TILE = 4096;           // elements per block of the scans (256 threads x 16)
-constexpr int SCAN_MAX_TILES = 4096;      // one block scans the tile sums: scans of up to 16.7M elements
+// SCAN_TILE, SCAN_MAX_TILES: kernels.cuh
 
 __device__ __forceinline__ int net_class(int deg) {
     return deg == 2 ? 0 : deg == 3 ? 1 : deg <= NO_SHORT ? 2 : deg <= NO_MID ? 3 : 4;
@@ -119,8 +118,8 @@ __global__ void __launch_bounds__(256) scan_apply_kernel(const int* in, int n, c
     }
 }
 
-// out[i] = sum of in[0..i) for i < n, *total = the sum of all (out may alias in)
-static int exclusive_scan(const int* in, int n, int* out, int* tile_sum, int* total, cudaStream_t s) {
+// out[i] = sum of in[0..i) for i < n, *total = the sum of all (out may alias in); tile_sum: SCAN_MAX_TILES ints
+int exclusive_scan(const int* in, int n, int* out, int* tile_sum, int* total, cudaStream_t s) {
     const int tiles = ceil_div(n, SCAN_TILE);
     if (tiles > SCAN_MAX_TILES) return GP103_ERR_TOO_LARGE;
     if (tiles == 0) return cudaMemsetAsync(total, 0, sizeof(int), s) == cudaSuccess ? GP103_OK : GP103_ERR_CUDA;

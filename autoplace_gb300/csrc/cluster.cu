@@ -1,0 +1,425 @@
+// Clustering of the cells by rounds of star matching (GB300, sm_103a): the first step of AutoPlace's two-level
+// placement, on the device.
+//
+// Reference: src/cluster.py:38-85 (cluster_cells). Pair edges: every net of at most max_degree pins gives each
+// ordered pair of distinct movable cells 420 // (degree - 1), summed per pair. A round: the non-head clusters pick
+// the head with the largest w / (area_i + area_j) (first edge on ties), a head keeps its per_head best (lower index
+// first on ties), clusters are renumbered in order, areas and edges summed. Every sum is an integer and every choice
+// has a fixed tie rule, so the result does not depend on the order atomics place things in: it is the reference's,
+// bit for bit. The head draws of a round come from the host (the reference draws them from a seeded CPU generator).
+#include "gp103.cuh"
+#include "kernels.cuh"
+
+namespace gp103 {
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------- COO -> CSR
+// rows: row index of each entry; result: per row, its columns ascending, equal columns merged (weights summed).
+struct CsrTemp {
+    int* count;    // [rows + 1]
+    int* cursor;   // [rows + 1]
+    int* merged;   // [rows + 1]
+    int* tmp_j;    // [max entries]
+    int* tmp_w;    // [max entries]
+    int* tile;     // [SCAN_MAX_TILES]
+    int* total;    // [4]
+};
+
+// (entries beyond cap were never written, rows out of range never produced: both guarded all the same)
+__global__ void __launch_bounds__(256) coo_count_kernel(const int* ci, const int* num, int cap, int rows, int* count) {
+    pdl_wait();
+    const int m = min(*num, cap);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x)
+        if ((unsigned)ci[e] < (unsigned)rows) atomicAdd(&count[ci[e]], 1);
+}
+
+__global__ void __launch_bounds__(256) coo_place_kernel(const int* ci, const int* cj, const int* cw, const int* num,
+                                                        int cap, int rows, int* cursor, int* tj, int* tw) {
+    pdl_wait();
+    const int m = min(*num, cap);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
+        if ((unsigned)ci[e] >= (unsigned)rows) continue;
+        const int at = atomicAdd(&cursor[ci[e]], 1);
+        tj[at] = cj[e];
+        tw[at] = cw[e];
+    }
+}
+
+// a row's entries sorted by column (insertion sort: rows hold a few dozen entries), equal columns merged to the front
+__global__ void __launch_bounds__(256) row_merge_kernel(const int* start, int rows, int* tj, int* tw, int* merged) {
+    pdl_wait();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int b = start[r], e = start[r + 1];
+        for (int k = b + 1; k < e; k++) {
+            const int j = tj[k], w = tw[k];
+            int q = k - 1;
+            while (q >= b && tj[q] > j) {
+                tj[q + 1] = tj[q];
+                tw[q + 1] = tw[q];
+                q--;
+            }
+            tj[q + 1] = j;
+            tw[q + 1] = w;
+        }
+        int out = b;
+        for (int k = b; k < e; k++) {
+            if (out > b && tj[out - 1] == tj[k]) {
+                tw[out - 1] += tw[k];
+            } else {
+                tj[out] = tj[k];
+                tw[out] = tw[k];
+                out++;
+            }
+        }
+        merged[r] = out - b;
+    }
+}
+
+__global__ void __launch_bounds__(256) row_compact_kernel(const int* start, const int* row_start, int rows,
+                                                          const int* tj, const int* tw, int* col, int* w) {
+    pdl_wait();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int b = start[r], o = row_start[r], k = row_start[r + 1] - o;
+        for (int t = 0; t < k; t++) {
+            col[o + t] = tj[b + t];
+            w[o + t] = tw[b + t];
+        }
+    }
+}
+
+// entries (ci, cj, cw) [*num, at most cap] -> CSR (row_start [rows + 1], col, w); *nnz = merged entries
+int coo_to_csr(const int* ci, const int* cj, const int* cw, const int* num, int cap, int rows, const CsrTemp& t,
+               int* row_start, int* col, int* w, int* nnz, cudaStream_t s) {
+    if (cudaMemsetAsync(t.count, 0, sizeof(int) * (size_t)(rows + 1), s) != cudaSuccess) return GP103_ERR_CUDA;
+    const int ge = grid_for(cap > 0 ? cap : 1, 256, 8), gr = grid_for(rows > 0 ? rows : 1, 256, 8);
+    if (launch_k(coo_count_kernel, dim3(ge), dim3(256), 0, s, ci, num, cap, rows, t.count) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    int st;
+    if ((st = exclusive_scan(t.count, rows + 1, t.cursor, t.tile, t.total, s))) return st;
+    // cursor now holds the row starts; keep a copy (placement advances cursor)
+    if (cudaMemcpyAsync(t.merged, t.cursor, sizeof(int) * (size_t)(rows + 1), cudaMemcpyDeviceToDevice, s) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    if (launch_k(coo_place_kernel, dim3(ge), dim3(256), 0, s, ci, cj, cw, num, cap, rows, t.cursor, t.tmp_j,
+                 t.tmp_w) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    // t.merged = row starts; merged counts go to t.count
+    if (launch_k(row_merge_kernel, dim3(gr), dim3(256), 0, s, (const int*)t.merged, rows, t.tmp_j, t.tmp_w, t.count) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (cudaMemsetAsync(t.count + rows, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
+    if ((st = exclusive_scan(t.count, rows + 1, row_start, t.tile, nnz, s))) return st;
+    if (launch_k(row_compact_kernel, dim3(gr), dim3(256), 0, s, (const int*)t.merged, (const int*)row_start, rows,
+                 (const int*)t.tmp_j, (const int*)t.tmp_w, col, w) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// ---------------------------------------------------------------------------------------------- pair edges
+__global__ void __launch_bounds__(256) net_degree_count_kernel(const int* pin_net, int num_pins, int num_nets,
+                                                               int* deg) {
+    pdl_wait();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < num_pins; p += gridDim.x * blockDim.x) {
+        const int net = pin_net[p];
+        if ((unsigned)net < (unsigned)num_nets) atomicAdd(&deg[net], 1);
+    }
+}
+
+// pins k apart in the pin list (k < max_degree) of one net of at most max_degree pins: both ordered pairs
+__global__ void __launch_bounds__(256) pair_emit_kernel(const int* pin_cell, const int* pin_net, int num_pins,
+                                                        int num_nets, int n, int max_degree, const int* deg, int cap,
+                                                        int* num, int* ci, int* cj, int* cw) {
+    pdl_wait();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < num_pins; p += gridDim.x * blockDim.x) {
+        const int net = pin_net[p];
+        if ((unsigned)net >= (unsigned)num_nets) continue;
+        const int d = deg[net];
+        if (d > max_degree || d < 2) continue;
+        const int a = pin_cell[p];
+        for (int k = 1; k < max_degree && p + k < num_pins; k++) {
+            if (pin_net[p + k] != net) break;
+            const int b = pin_cell[p + k];
+            if (a < 0 || b < 0 || a >= n || b >= n || a == b) continue;
+            const int wgt = 420 / (d - 1);
+            const int at = atomicAdd(num, 2);
+            if (at + 1 < cap) {
+                ci[at] = a; cj[at] = b; cw[at] = wgt;
+                ci[at + 1] = b; cj[at + 1] = a; cw[at + 1] = wgt;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------- a round
+// per non-head cluster: the head of the largest score, the first one (lowest column) on ties
+__global__ void __launch_bounds__(256) best_head_kernel(const int* row_start, const int* col, const int* w, int num,
+                                                        const long long* area, const unsigned char* head,
+                                                        long long cap, long long big, int* best_to, double* best) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
+        int to = -1;
+        double sc = 0.0;
+        if (!head[i] && area[i] < big) {
+            for (int e = row_start[i]; e < row_start[i + 1]; e++) {
+                const int j = col[e];
+                if (!head[j] || area[j] >= big) continue;
+                const long long total = area[i] + area[j];
+                if (total > cap) continue;
+                const double s = (double)w[e] / (double)total;
+                if (to < 0 || s > sc) {
+                    to = j;
+                    sc = s;
+                }
+            }
+        }
+        best_to[i] = to;
+        best[i] = sc;
+    }
+}
+
+__global__ void __launch_bounds__(256) cand_count_kernel(const int* best_to, int num, int* count, int* parent) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
+        parent[i] = i;
+        if (best_to[i] >= 0) atomicAdd(&count[best_to[i]], 1);
+    }
+}
+
+__global__ void __launch_bounds__(256) cand_place_kernel(const int* best_to, int num, int* cursor, int* list) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x)
+        if (best_to[i] >= 0) list[atomicAdd(&cursor[best_to[i]], 1)] = i;
+}
+
+// per head: its per_head best tails (score descending, lower tail first on ties) join it
+__global__ void __launch_bounds__(256) take_kernel(const int* start, const int* list, const double* best, int num,
+                                                   int per_head, int* parent) {
+    pdl_wait();
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < num; h += gridDim.x * blockDim.x) {
+        const int b = start[h], e = start[h + 1];
+        double last_s = 0.0;
+        int last_t = -1;
+        for (int k = 0; k < per_head && k < e - b; k++) {
+            // the best candidate below (last_s, last_t) in the order (score desc, tail asc)
+            int pick = -1;
+            double ps = 0.0;
+            for (int q = b; q < e; q++) {
+                const int t = list[q];
+                const double s = best[t];
+                const bool below = last_t < 0 || s < last_s || (s == last_s && t > last_t);
+                if (!below) continue;
+                if (pick < 0 || s > ps || (s == ps && t < pick)) {
+                    pick = t;
+                    ps = s;
+                }
+            }
+            if (pick < 0) break;
+            parent[pick] = h;
+            last_s = ps;
+            last_t = pick;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) kept_flag_kernel(const int* parent, int num, int* flag) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) flag[i] = parent[i] == i;
+}
+
+// new index of every cluster (its parent's rank among the kept ones), summed areas
+__global__ void __launch_bounds__(256) renumber_kernel(const int* parent, const int* rank, int num,
+                                                       const long long* area, int* new_index, long long* area_out) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
+        const int k = rank[parent[i]];
+        new_index[i] = k;
+        atomicAdd((unsigned long long*)&area_out[k], (unsigned long long)area[i]);
+    }
+}
+
+// the edges between the new clusters (a cluster's own edges dropped), as entries for coo_to_csr
+__global__ void __launch_bounds__(256) edge_relabel_kernel(const int* row_start, const int* col, const int* w, int num,
+                                                           const int* new_index, int cap, int* m, int* ci, int* cj,
+                                                           int* cw) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
+        const int a = new_index[i];
+        for (int e = row_start[i]; e < row_start[i + 1]; e++) {
+            const int b = new_index[col[e]];
+            if (a == b) continue;
+            const int at = atomicAdd(m, 1);
+            if (at < cap) {
+                ci[at] = a;
+                cj[at] = b;
+                cw[at] = w[e];
+            }
+        }
+    }
+}
+
+__global__ void relabel_kernel(int* cid, int n, const int* new_index) {
+    pdl_wait();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) cid[c] = new_index[cid[c]];
+}
+
+// ---------------------------------------------------------------------------------------------- scratch
+struct ClusterScratch {
+    size_t count, cursor, merged, tmp_j, tmp_w, coo_i, coo_j, coo_w, deg, best_to, best, list, parent, tile, total,
+        bytes;
+};
+
+ClusterScratch cluster_scratch(long long n, long long num_nets, long long max_edges) {
+    ClusterScratch c = {};
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t rows = (size_t)n + 1, e = (size_t)(max_edges > 0 ? max_edges : 1);
+    size_t at = 0;
+    c.count = at; at += al(4 * rows);
+    c.cursor = at; at += al(4 * rows);
+    c.merged = at; at += al(4 * rows);
+    c.tmp_j = at; at += al(4 * e);
+    c.tmp_w = at; at += al(4 * e);
+    c.coo_i = at; at += al(4 * e);
+    c.coo_j = at; at += al(4 * e);
+    c.coo_w = at; at += al(4 * e);
+    c.deg = at; at += al(4 * (size_t)(num_nets > 0 ? num_nets : 1));
+    c.best_to = at; at += al(4 * rows);
+    c.best = at; at += al(8 * rows);
+    c.list = at; at += al(4 * rows);
+    c.parent = at; at += al(4 * rows);
+    c.tile = at; at += al(4 * (size_t)SCAN_MAX_TILES);
+    c.total = at; at += al(4 * 8);
+    c.bytes = at;
+    return c;
+}
+
+CsrTemp csr_temp(char* base, const ClusterScratch& L) {
+    CsrTemp t;
+    t.count = (int*)(base + L.count);
+    t.cursor = (int*)(base + L.cursor);
+    t.merged = (int*)(base + L.merged);
+    t.tmp_j = (int*)(base + L.tmp_j);
+    t.tmp_w = (int*)(base + L.tmp_w);
+    t.tile = (int*)(base + L.tile);
+    t.total = (int*)(base + L.total) + 4;
+    return t;
+}
+
+}  // namespace
+}  // namespace gp103
+
+using namespace gp103;
+
+extern "C" size_t gp103_cluster_scratch(int n, int num_nets, int max_edges) {
+    if (n < 0 || num_nets < 0 || max_edges < 0) return 0;
+    return cluster_scratch(n, num_nets, max_edges).bytes;
+}
+
+extern "C" int gp103_cluster_edges(const int* pin_cell, const int* pin_net, int num_pins, int num_nets, int n,
+                                   int max_degree, int max_edges, void* scratch, size_t scratch_bytes,
+                                   int* row_start, int* col, int* w, int* counts, cudaStream_t s) {
+    if (num_pins < 0 || num_nets < 0 || n < 0 || max_degree < 2 || max_edges < 0 || !scratch || !row_start ||
+        !counts)
+        return GP103_ERR_ARG;
+    if (num_pins > 0 && (!pin_cell || !pin_net)) return GP103_ERR_ARG;
+    if (max_edges > 0 && (!col || !w)) return GP103_ERR_ARG;
+    if (n + 1LL > (long long)SCAN_TILE * SCAN_MAX_TILES) return GP103_ERR_TOO_LARGE;
+    const ClusterScratch L = cluster_scratch(n, num_nets, max_edges);
+    if (scratch_bytes < L.bytes) return GP103_ERR_ARG;
+    char* base = (char*)scratch;
+    int* deg = (int*)(base + L.deg);
+    int *ci = (int*)(base + L.coo_i), *cj = (int*)(base + L.coo_j), *cw = (int*)(base + L.coo_w);
+    int* m = (int*)(base + L.total);                              // entries appended (device)
+    if (cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)(num_nets > 0 ? num_nets : 1), s) != cudaSuccess ||
+        cudaMemsetAsync(m, 0, sizeof(int), s) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    const int gp = grid_for(num_pins > 0 ? num_pins : 1, 256, 8);
+    if (num_pins > 0) {
+        if (launch_k(net_degree_count_kernel, dim3(gp), dim3(256), 0, s, pin_net, num_pins, num_nets, deg) !=
+            cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+        if (launch_k(pair_emit_kernel, dim3(gp), dim3(256), 0, s, pin_cell, pin_net, num_pins, num_nets, n,
+                     max_degree, (const int*)deg, max_edges, m, ci, cj, cw) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
+    // counts[1] = entries appended (more than max_edges: the caller's bound was too small, the edges are not valid)
+    if (cudaMemcpyAsync(counts + 1, m, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return GP103_ERR_CUDA;
+    return coo_to_csr(ci, cj, cw, m, max_edges, n, csr_temp(base, L), row_start, col, w, counts, s);
+}
+
+extern "C" int gp103_cluster_round(const int* row_start, const int* col, const int* w, int num, int max_edges,
+                                   const long long* area, const unsigned char* head, long long cap, long long big,
+                                   int per_head, void* scratch, size_t scratch_bytes, int* new_index,
+                                   long long* area_out, int* row_out, int* col_out, int* w_out, int* counts,
+                                   cudaStream_t s) {
+    if (num < 1 || max_edges < 0 || per_head < 1 || !row_start || !area || !head || !scratch || !new_index ||
+        !area_out || !row_out || !counts)
+        return GP103_ERR_ARG;
+    if (max_edges > 0 && (!col || !w || !col_out || !w_out)) return GP103_ERR_ARG;
+    const ClusterScratch L = cluster_scratch(num, 0, max_edges);
+    if (scratch_bytes < L.bytes) return GP103_ERR_ARG;
+    char* base = (char*)scratch;
+    const CsrTemp t = csr_temp(base, L);
+    int* best_to = (int*)(base + L.best_to);
+    double* best = (double*)(base + L.best);
+    int* list = (int*)(base + L.list);
+    int* parent = (int*)(base + L.parent);
+    int *ci = (int*)(base + L.coo_i), *cj = (int*)(base + L.coo_j), *cw = (int*)(base + L.coo_w);
+    int* m = (int*)(base + L.total);
+    const int g = grid_for(num, 256, 8);
+    int st;
+    if (launch_k(best_head_kernel, dim3(g), dim3(256), 0, s, row_start, col, w, num, area, head, cap, big, best_to,
+                 best) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    // candidates grouped by head: counts, starts (in t.merged), placement
+    if (cudaMemsetAsync(t.count, 0, sizeof(int) * (size_t)(num + 1), s) != cudaSuccess) return GP103_ERR_CUDA;
+    if (launch_k(cand_count_kernel, dim3(g), dim3(256), 0, s, (const int*)best_to, num, t.count, parent) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if ((st = exclusive_scan(t.count, num + 1, t.merged, t.tile, t.total, s))) return st;
+    if (cudaMemcpyAsync(t.cursor, t.merged, sizeof(int) * (size_t)(num + 1), cudaMemcpyDeviceToDevice, s) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    if (launch_k(cand_place_kernel, dim3(g), dim3(256), 0, s, (const int*)best_to, num, t.cursor, list) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (launch_k(take_kernel, dim3(g), dim3(256), 0, s, (const int*)t.merged, (const int*)list, (const double*)best,
+                 num, per_head, parent) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    // kept clusters (their own parent), ranked: counts[0] = the new number of clusters
+    if (launch_k(kept_flag_kernel, dim3(g), dim3(256), 0, s, (const int*)parent, num, t.count) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (cudaMemsetAsync(t.count + num, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
+    if ((st = exclusive_scan(t.count, num + 1, t.cursor, t.tile, counts, s))) return st;
+    if (cudaMemsetAsync(area_out, 0, sizeof(long long) * (size_t)num, s) != cudaSuccess) return GP103_ERR_CUDA;
+    if (launch_k(renumber_kernel, dim3(g), dim3(256), 0, s, (const int*)parent, (const int*)t.cursor, num, area,
+                 new_index, area_out) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    // the new edges: relabelled, internal ones dropped, merged (rows: at most num)
+    if (cudaMemsetAsync(m, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
+    if (launch_k(edge_relabel_kernel, dim3(g), dim3(256), 0, s, row_start, col, w, num, (const int*)new_index,
+                 max_edges, m, ci, cj, cw) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return coo_to_csr(ci, cj, cw, m, max_edges, num, t, row_out, col_out, w_out, counts + 1, s);
+}
+
+extern "C" int gp103_cluster_relabel(int* cid, int n, const int* new_index, cudaStream_t s) {
+    if (n < 0 || (n > 0 && (!cid || !new_index))) return GP103_ERR_ARG;
+    if (n == 0) return GP103_OK;
+    if (launch_k(relabel_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, cid, n, new_index) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}

@@ -121,6 +121,12 @@ struct GatherJob {
     Reduce red;                 // (|g - gref|^2, L1 of g over the cells)
 };
 
+// Exclusive scan of n ints (build.cu): out[i] = in[0] + ... + in[i - 1], *total = the whole sum (device int);
+// tile_sum is SCAN_MAX_TILES ints of scratch; GP103_ERR_TOO_LARGE beyond SCAN_TILE * SCAN_MAX_TILES elements.
+constexpr int SCAN_TILE = 4096;           // elements per block of the scans (256 threads x 16)
+constexpr int SCAN_MAX_TILES = 4096;      // one block scans the tile sums: scans of up to 16.7M elements
+int exclusive_scan(const int* in, int n, int* out, int* tile_sum, int* total, cudaStream_t s);
+
 int launch_wa_net(const WaJob& j, cudaStream_t s);
 int launch_wa_cell(const float2* pin_grad, const int* cell_start, const int* cell_pin, int num_mov, float2* grad,
                    cudaStream_t s);

@@ -68,6 +68,11 @@ _SIGS = {
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
     "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
     "gp103_net_order_scratch": ([_i, _i, _i], ctypes.c_size_t),
+    "gp103_cluster_scratch": ([_i, _i, _i], ctypes.c_size_t),
+    "gp103_cluster_edges": ([_vp, _vp, _i, _i, _i, _i, _i, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp], _i),
+    "gp103_cluster_round": ([_vp, _vp, _vp, _i, _i, _vp, _vp, ctypes.c_longlong, ctypes.c_longlong, _i, _vp,
+                             ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
+    "gp103_cluster_relabel": ([_vp, _i, _vp, _vp], _i),
     "gp103_net_order": ([_vp] * 4 + [_i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 5 + [_vp], _i),
     "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
 }

@@ -231,6 +231,32 @@ int gp103_net_order(const int* net_start, const int* pin_cell, const float* pin_
                     int* net_start_out, int* pin_cell_out, float* pin_off_out, int* pin_slot, int* split,
                     cudaStream_t stream);
 
+/* Clustering of the cells (src/cluster.py:38-85, cluster_cells), the first step of the two-level placement: rounds
+ * of star matching on the pair edges of the small nets. Integer weights and areas, fixed tie rules: the clusters are
+ * the reference's, bit for bit. Scratch: gp103_cluster_scratch(n, num_nets, max_edges) bytes, max_edges >= the
+ * number of ordered pin pairs of the nets of 2 .. max_degree pins (sum of d (d - 1)).
+ *
+ * gp103_cluster_edges: the pair edges of the pins (pin_cell [num_pins] with n for a fixed pin, pin_net sorted by
+ * net, nets < num_nets) as a CSR over the n cells: row_start [n + 1], col / w [max_edges], columns ascending per row,
+ * w = the summed 420 / (degree - 1). counts (device int [2]): [0] = edges, [1] = ordered pairs found (above
+ * max_edges: the bound was too small and the edges are not valid).
+ *
+ * gp103_cluster_round: one round on `num` clusters (their edges in CSR, areas int64, head [num] = 1 for the heads of
+ * the round, drawn by the caller): writes new_index [num] (each cluster's index among the kept ones), area_out
+ * [num] (the first counts[0] valid), the new edges row_out [num + 1] / col_out / w_out (counts[1] of them) and
+ * counts (device int [2]) = (clusters kept, edges). counts[0] == num: nothing merged (the reference stops there).
+ *
+ * gp103_cluster_relabel: cid[c] = new_index[cid[c]] for the n cells after a round that merged. */
+size_t gp103_cluster_scratch(int n, int num_nets, int max_edges);
+int gp103_cluster_edges(const int* pin_cell, const int* pin_net, int num_pins, int num_nets, int n, int max_degree,
+                        int max_edges, void* scratch, size_t scratch_bytes, int* row_start, int* col, int* w,
+                        int* counts, cudaStream_t stream);
+int gp103_cluster_round(const int* row_start, const int* col, const int* w, int num, int max_edges,
+                        const long long* area, const unsigned char* head, long long cap, long long big, int per_head,
+                        void* scratch, size_t scratch_bytes, int* new_index, long long* area_out, int* row_out,
+                        int* col_out, int* w_out, int* counts, cudaStream_t stream);
+int gp103_cluster_relabel(int* cid, int n, const int* new_index, cudaStream_t stream);
+
 /* ------------------------------------------------------------------------------------------------ part 3
  * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
  * *out is written by the device (read it after synchronising the stream). */

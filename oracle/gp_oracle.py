@@ -18,6 +18,7 @@ Each function names the reference lines it restates (paths inside the AutoPlace 
   control         gp_cuda_kernel.cu:183-240 with src/param_scheduler.py:63-116, src/resolution.py:33-56 (float64)
   select          gp_cuda_kernel.cu:243-249
   place_level     src/run_placement.py:41-76 + src/gpu_loop.py:35-81 (host loop; the CPU baseline)
+  cluster_*       src/cluster.py:38-85 (star matching: pair edges, rounds), integer sums: exact
 """
 import ctypes
 import math
@@ -204,6 +205,92 @@ def density_grad(pos, size, ratio, fx, fy, wl_grad, pins, area, weight, precond,
                               wl.ctypes.data if wl is not None else None, 0 if wl is None else len(wl),
                               _c32(pins), _c32(area), n, float(weight), float(precond), bx, by, nbx, nby, g)
     return g
+
+
+# ------------------------------------------------------------------------------------------------ clustering
+def cluster_edges(pin_cell, pin_net, n, max_degree=8):
+    """The pair edges of cluster_cells (src/cluster.py:44-56): for every net of at most max_degree pins (its degree
+    counts every pin) each ordered pair of distinct movable cells (index < n) weighs 420 // (degree - 1), once per
+    pair of its pins; the same (i, j) summed. -> (i, j, w) int64, sorted by i then j."""
+    pin_cell = np.asarray(pin_cell, np.int64)
+    pin_net = np.asarray(pin_net, np.int64)
+    degree = np.bincount(pin_net)[pin_net]
+    small = degree <= max_degree
+    pc, pn, dg = pin_cell[small], pin_net[small], degree[small]
+    keys, weights = [], []
+    for k in range(1, max_degree):
+        a, b, d = pc[:-k], pc[k:], dg[:-k]
+        m = (pn[:-k] == pn[k:]) & (a < n) & (b < n) & (a != b)
+        a, b, w = a[m], b[m], 420 // (d[m] - 1)
+        keys += [a * n + b, b * n + a]
+        weights += [w, w]
+    if not keys:
+        e = np.zeros(0, np.int64)
+        return e, e, e
+    key, inv = np.unique(np.concatenate(keys), return_inverse=True)
+    w = np.zeros(len(key), np.int64)
+    np.add.at(w, inv, np.concatenate(weights))
+    return key // n, key % n, w
+
+
+def cluster_round(i, j, w, area, head, cap, big, per_head=3):
+    """One round of star matching (src/cluster.py:66-84). head [num] bool. A cluster that is not a head joins the head
+    with the largest w / (area_i + area_j) among its edges (first such edge on ties), if the merged area is at most
+    cap and neither is at or above big; a head takes the per_head largest scores (lower cluster index first on ties).
+    -> (new index of every cluster, cluster areas, merged edges) or None when nothing merges."""
+    num = len(area)
+    total = area[i] + area[j]
+    m = ~head[i] & head[j] & (total <= cap) & (area[i] < big) & (area[j] < big)
+    tail, to, score = i[m], j[m], w[m].astype(np.float64) / total[m].astype(np.float64)
+    # per tail: the best score, the first candidate (in edge order) on ties
+    order = np.lexsort((np.arange(len(tail)), -score, tail))
+    first = np.ones(len(order), bool)
+    first[1:] = tail[order][1:] != tail[order][:-1]
+    best = order[first]                                  # one per tail, tails ascending
+    tail, to, score = tail[best], to[best], score[best]
+    # per head: the per_head best scores, lower tail first on ties
+    order = np.lexsort((tail, -score, to))
+    g = to[order]
+    start = np.ones(len(order), bool)
+    start[1:] = g[1:] != g[:-1]
+    pos = np.arange(len(order))
+    rank = pos - np.maximum.accumulate(np.where(start, pos, 0))
+    taken = order[rank < per_head]
+    parent = np.arange(num)
+    parent[tail[taken]] = to[taken]
+    kept, new = np.unique(parent, return_inverse=True)
+    if len(kept) == num:
+        return None
+    carea = np.zeros(len(kept), np.int64)
+    np.add.at(carea, new, area)
+    ni, nj = new[i], new[j]
+    keep = ni != nj
+    key, inv = np.unique(ni[keep] * len(kept) + nj[keep], return_inverse=True)
+    nw = np.zeros(len(key), np.int64)
+    np.add.at(nw, inv, w[keep])
+    return new, carea, (key // len(kept), key % len(kept), nw)
+
+
+def cluster_cells(pin_cell, pin_net, area, ratio, draws, max_degree=8, per_head=3, max_rounds=12):
+    """cluster_cells (src/cluster.py:38-85) with the head draws given: draws(r, num) -> float32 [num] uniform draws of
+    round r (the reference's torch.rand of its seeded generator). -> (cluster of every cell, cluster areas)."""
+    area = np.asarray(area, np.int64)
+    n = len(area)
+    i, j, w = cluster_edges(pin_cell, pin_net, n, max_degree)
+    cid, num = np.arange(n), n
+    big = 20 * int(area.sum()) // n
+    small = area < big
+    cap = 3 * ratio * int(area[small].sum()) // (2 * int(small.sum()))
+    for r in range(max_rounds):
+        if num * ratio <= n:
+            break
+        head = np.asarray(draws(r, num)) < np.float32(0.5)
+        res = cluster_round(i, j, w, area, head, cap, big, per_head)
+        if res is None:
+            break
+        new, area, (i, j, w) = res
+        cid, num = new[cid], len(area)
+    return cid, area
 
 
 # ------------------------------------------------------------------------------------------------ optimiser

@@ -20,3 +20,8 @@ def golden(name):
 @pytest.fixture
 def gold():
     return golden
+
+
+@pytest.fixture
+def gold_cluster():
+    return golden("golden_cluster.npz")

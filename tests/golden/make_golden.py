@@ -13,6 +13,7 @@ tests read only these files: the reference sources are not needed to run them.
                        exact / smoothed overflow on a second (overflow) grid
   golden_control.npz   ParamScheduler + resolution: the state after each step of a driven sequence
   golden_place.npz     global_placement_main (one level) on a small netlist: stop reason, iterations, HPWL, overflow
+  golden_cluster.npz   cluster_cells: the merged pair edges, the head draws and edges of every round, the clusters
 """
 import math
 import os
@@ -194,7 +195,52 @@ def gen_place():
     print("place:", stats["stop_reason"], stats["iters"], stats["start_iters"], hpwl, ovf)
 
 
+def gen_cluster():
+    """cluster_cells on a netlist with fixed pins, nets above max_degree and a few cells above 20 x the mean area.
+    The edges are read from the reference's own _merge_edges (after the pair loop, and after every round) and the
+    head draws from torch.rand, so that a restatement can be checked step by step."""
+    from src import cluster as C
+    nl = synth.make_netlist(4000, 4300, window=120, macros=3, cover=0.1, fixed_pin_share=0.05, seed=31)
+    size = nl.size.copy()
+    size[[7, 1500, 3333], 0] *= 400                      # three cells above 20 x the mean area
+    area = np.round(size.prod(1) * 1024).astype(np.int64)
+    ratio, seed = 5, 17
+    calls, draws = [], []
+    merge, rand = C._merge_edges, torch.rand
+
+    def spy_merge(parts, n):
+        r = merge(parts, n)
+        calls.append([x.numpy().copy() for x in r])
+        return r
+
+    def spy_rand(*a, **k):
+        r = rand(*a, **k)
+        draws.append(r.numpy().copy())
+        return r
+
+    C._merge_edges, C.torch.rand = spy_merge, spy_rand
+    try:
+        cid, carea = C.cluster_cells(torch.tensor(nl.pin_cell), torch.tensor(nl.pin_net), torch.tensor(area), ratio, seed)
+    finally:
+        C._merge_edges, C.torch.rand = merge, rand
+    out = dict(pin_cell=nl.pin_cell, pin_net=nl.pin_net, area=area, ratio=ratio, seed=seed, n=nl.num_mov,
+               edge_i=calls[6][0], edge_j=calls[6][1], edge_w=calls[6][2], rounds=len(draws),
+               cid=cid.numpy(), carea=carea.numpy())
+    for r, d in enumerate(draws):
+        out["draw%d" % r] = d
+        if 7 + r < len(calls):
+            out["round%d_i" % r], out["round%d_j" % r], out["round%d_w" % r] = calls[7 + r]
+    np.savez_compressed(os.path.join(HERE, "golden_cluster.npz"), **out)
+    print("cluster:", nl.num_mov, "cells ->", len(carea), "clusters in", len(draws), "rounds;", len(calls[6][0]), "edges")
+
+
+if __name__ == "__main__" and len(sys.argv) > 1:
+    for name in sys.argv[1:]:
+        globals()["gen_" + name]()
+    sys.exit(0)
+
 if __name__ == "__main__":
+    gen_cluster()
     gen_wa()
     gen_density()
     gen_control()

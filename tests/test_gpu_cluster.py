@@ -1,0 +1,67 @@
+"""Clustering on the device (gp103_cluster_*) against the reference's own output (golden_cluster.npz) and against
+the oracle's restatement on larger netlists: integer work, so bit for bit."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from autoplace_gb300 import cluster, native, synth
+from oracle import gp_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _edges(pin_cell, pin_net, n):
+    E = max(cluster.pair_bound(pin_net), 1)
+    num_nets = int(np.max(pin_net)) + 1
+    pc = torch.as_tensor(np.asarray(pin_cell, np.int32)).cuda()
+    pn = torch.as_tensor(np.asarray(pin_net, np.int32)).cuda()
+    scratch = torch.empty(int(native.lib().gp103_cluster_scratch(n, num_nets, E)), dtype=torch.uint8, device="cuda")
+    rows = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    col = torch.zeros(E, dtype=torch.int32, device="cuda")
+    w = torch.zeros(E, dtype=torch.int32, device="cuda")
+    counts = torch.zeros(2, dtype=torch.int32, device="cuda")
+    native.call("gp103_cluster_edges", pc.data_ptr(), pn.data_ptr(), len(pin_net), num_nets, n, 8, E,
+                scratch.data_ptr(), scratch.numel(), rows.data_ptr(), col.data_ptr(), w.data_ptr(), counts.data_ptr(),
+                torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    m = int(counts[0])
+    r = rows.cpu().numpy()
+    i = np.repeat(np.arange(n), np.diff(r))
+    return i, col.cpu().numpy()[:m], w.cpu().numpy()[:m], int(counts[1]), E
+
+
+def test_pair_edges_match_reference(gold_cluster):
+    g = gold_cluster
+    i, j, w, found, E = _edges(g["pin_cell"], g["pin_net"], int(g["n"]))
+    assert found <= E
+    assert np.array_equal(i, g["edge_i"]) and np.array_equal(j, g["edge_j"]) and np.array_equal(w, g["edge_w"])
+
+
+def test_clusters_match_reference(gold_cluster):
+    g = gold_cluster
+    cid, area = cluster.cluster_cells(g["pin_cell"], g["pin_net"], g["area"], int(g["ratio"]), int(g["seed"]),
+                                      draws=lambda r, num: g["draw%d" % r])
+    assert np.array_equal(cid, g["cid"]) and np.array_equal(area, g["carea"])
+    # the seeded generator of the product path draws the same heads as the reference did
+    cid2, area2 = cluster.cluster_cells(g["pin_cell"], g["pin_net"], g["area"], int(g["ratio"]), int(g["seed"]))
+    assert np.array_equal(cid2, g["cid"]) and np.array_equal(area2, g["carea"])
+
+
+@pytest.mark.parametrize("cells,seed,ratio", [(30000, 2, 5), (12000, 9, 2)])
+def test_clusters_match_oracle(cells, seed, ratio):
+    nl = synth.make_netlist(cells, int(cells * 1.05), window=300, macros=2, cover=0.1, fixed_pin_share=0.05, seed=seed)
+    area = np.round(nl.size.prod(1) * 1024).astype(np.int64)
+    gen = torch.Generator().manual_seed(seed)
+    cache = {}
+
+    def draws(r, num):
+        if r not in cache:
+            cache[r] = torch.rand(num, generator=gen).numpy()
+        return cache[r]
+
+    ocid, oarea = O.cluster_cells(nl.pin_cell, nl.pin_net, area, ratio, draws)
+    cid, carea = cluster.cluster_cells(nl.pin_cell, nl.pin_net, area, ratio, seed, draws=draws)
+    assert np.array_equal(cid, ocid) and np.array_equal(carea, oarea)
+    assert len(carea) < cells and int(carea.sum()) == int(area.sum())

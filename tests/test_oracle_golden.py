@@ -173,3 +173,14 @@ def test_cpu_placement_matches_reference(gold):
     assert abs(r["iters"] - int(g["iters"])) <= 5
     h = O.hpwl_all(r["pos"], prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
     assert abs(h - float(g["hpwl"])) <= 0.005 * float(g["hpwl"])
+
+
+def test_cluster_matches_reference(gold):
+    """cluster_cells (src/cluster.py:38-85): the pair edges and, with the reference's own head draws, every cluster
+    and its area."""
+    g = gold("golden_cluster.npz")
+    i, j, w = O.cluster_edges(g["pin_cell"], g["pin_net"], int(g["n"]))
+    assert np.array_equal(i, g["edge_i"]) and np.array_equal(j, g["edge_j"]) and np.array_equal(w, g["edge_w"])
+    cid, area = O.cluster_cells(g["pin_cell"], g["pin_net"], g["area"], int(g["ratio"]), lambda r, num: g["draw%d" % r])
+    assert np.array_equal(cid, g["cid"]) and np.array_equal(area, g["carea"])
+    assert len(area) < int(g["n"]) and int(area.sum()) == int(g["area"].sum())
