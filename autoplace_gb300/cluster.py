@@ -8,6 +8,8 @@ host draws the heads and reads two counts per round. Integer weights and areas a
 the reference's, bit for bit.
 """
 import ctypes
+import math
+from types import SimpleNamespace
 
 import numpy as np
 import torch
@@ -20,6 +22,18 @@ def pair_bound(pin_net, max_degree=8):
     deg = np.bincount(np.asarray(pin_net, np.int64))
     d = deg[(deg >= 2) & (deg <= max_degree)].astype(np.int64)
     return int((d * (d - 1)).sum())
+
+
+def limits(area, ratio):
+    """(big, cap) of cluster_cells, evaluated as the reference evaluates them (torch scalar arithmetic on the CPU: with
+    a float ratio, cap is a float32 floor division): a cell of area >= big stays alone, two clusters merge only when
+    their areas add up to at most cap (exact as integers below 2^24, the float32 range the comparison runs in)."""
+    a = torch.as_tensor(np.asarray(area, np.int64))
+    n = len(a)
+    big = 20 * a.sum() // n
+    small = a < big
+    cap = 3 * ratio * a[small].sum() // (2 * int(small.sum()))
+    return int(big), int(math.floor(float(cap)))
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
@@ -35,9 +49,7 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     stream = stream or torch.cuda.current_stream(dev)
     s = stream.cuda_stream
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    big = 20 * int(area.sum()) // n
-    small = area < big
-    cap = 3 * int(ratio) * int(area[small].sum()) // (2 * int(small.sum()))
+    big, cap = limits(area, ratio)
     pin_net = np.asarray(pin_net, np.int64)
     num_nets = int(pin_net.max()) + 1 if len(pin_net) else 0
     E = max(pair_bound(pin_net, max_degree), 1)
@@ -78,3 +90,79 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
         num, a = kept, b
     stream.synchronize()
     return cid.cpu().numpy().astype(np.int64), areas[a][:num].cpu().numpy()
+
+
+def coarse_problem(prob, device="cuda", stream=None):
+    """The problem of the clusters (coarse_problem, src/cluster.py:88-130), from a cell-level Problem:
+      - the cells clustered (cluster_cells, areas in 1/1024 of a site area, rounded from the float32 area);
+      - a merged cluster is a square of its summed area with its pins at the centre, one per net; a cluster of one
+        cell keeps its shape and pins (the pin selection runs on the device: gp103_coarse_pins);
+      - the same fillers, target and options; one grid, between the overflow grid and the cells' force grid, as
+        the cells' grid follows the cells.
+    -> SimpleNamespace(cid [n], num, size [num, 2] float32, problem: the clusters' Problem)."""
+    from . import problem as P
+    dev = torch.device(device)
+    stream = stream or torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    nl, o, n = prob.nl, prob.opts, prob.num_mov
+    size = np.asarray(prob.node_size[:n], np.float32)
+    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
+    cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream)
+    num = len(carea)
+    csize = np.repeat(np.sqrt(carea.astype(np.float64) / 1024).astype(np.float32)[:, None], 2, 1)
+    count = np.bincount(cid, minlength=num)
+    single = count == 1
+    member = np.zeros(num, np.int64)
+    member[cid] = np.arange(n)                         # a one-cell cluster's cell
+    csize[single] = size[member[single]]
+    # pins: on the device
+    P_ = len(nl.pin_cell)
+    with torch.cuda.stream(stream):
+        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev)
+        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev)
+        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev)
+        cd = torch.as_tensor(cid.astype(np.int32)).to(dev)
+        sg = torch.as_tensor(single.astype(np.uint8)).to(dev)
+        scratch = torch.empty(int(native.lib().gp103_coarse_pins_scratch(P_)), dtype=torch.uint8, device=dev)
+        oc = torch.empty(max(P_, 1), dtype=torch.int32, device=dev)
+        oo = torch.empty((max(P_, 1), 2), dtype=torch.float32, device=dev)
+        on = torch.empty(max(P_, 1), dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    native.call("gp103_coarse_pins", p(pc), p(po), p(pn), P_, n, p(cd), num, p(sg), p(scratch), scratch.numel(),
+                p(oc), p(oo), p(on), p(cnt), s)
+    stream.synchronize()
+    k = int(cnt.item())
+    c_cell, c_off, c_net = oc[:k].cpu().numpy(), oo[:k].cpu().numpy(), on[:k].cpu().numpy()
+    # the grid: as the cells' force grid follows the cells (at most the cells' grid)
+    fine_ff = nl.fixed_fraction(prob.force_bin, prob.force_bin)
+    judge_bin = prob.num_bin
+    nb = min(prob.force_bin, P.force_num_bin(num, 1.0 - float(fine_ff.mean()), judge_bin))
+    fixed_fraction = fine_ff if nb == prob.force_bin else nl.fixed_fraction(nb, nb)
+    copts = SimpleNamespace(**vars(o))
+    copts.settle_iter, copts.min_iter = 0, 0
+    cprob = P.Problem.clusters(prob, csize, c_cell, c_off, c_net, nb, fixed_fraction, copts)
+    return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob)
+
+
+def expand(cpos, coarse, prob, seed, device="cuda", stream=None):
+    """Positions of clusters + fillers ([num + F, 2], host or device) -> positions of cells + fillers (expand,
+    src/cluster.py:133-144): a cell at a random point of its cluster's square, the draws from the seeded CPU
+    generator as the reference takes them; the fillers keep theirs. -> device tensor [n + F, 2]."""
+    dev = torch.device(device)
+    stream = stream or torch.cuda.current_stream(dev)
+    n, num = prob.num_mov, coarse.num
+    gen = torch.Generator().manual_seed(int(seed))
+    r = torch.rand(n, 2, generator=gen)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    with torch.cuda.stream(stream):
+        cpos = torch.as_tensor(cpos, dtype=torch.float32).to(dev).contiguous()
+        out = torch.empty((n + cpos.shape[0] - num, 2), dtype=torch.float32, device=dev)
+        out[n:] = cpos[num:]
+        cid = torch.as_tensor(coarse.cid.astype(np.int32)).to(dev)
+        cs = torch.as_tensor(coarse.size).to(dev)
+        sz = torch.as_tensor(np.asarray(prob.node_size[:n], np.float32)).to(dev)
+        rd = r.to(dev)
+    native.call("gp103_expand", p(cpos), p(cid), p(cs), p(sz), p(rd), n, p(out), stream.cuda_stream)
+    stream.synchronize()
+    return out

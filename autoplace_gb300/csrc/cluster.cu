@@ -262,6 +262,61 @@ __global__ void __launch_bounds__(256) edge_relabel_kernel(const int* row_start,
     }
 }
 
+// ---------------------------------------------------------------------------------------------- cluster problem
+// A pin of the cluster problem: its cluster (num for a fixed pin); kept if its cluster has one cell or the pin is
+// fixed (then with its offset), or if it is the first pin of its net on its (merged) cluster (then at the centre).
+__global__ void __launch_bounds__(256) coarse_keep_kernel(const int* pin_cell, const int* pin_net, int num_pins, int n,
+                                                          const int* cid, int num, const unsigned char* single,
+                                                          int* owner, int* keep) {
+    pdl_wait();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < num_pins; p += gridDim.x * blockDim.x) {
+        const int c = pin_cell[p];
+        const int o = (c >= 0 && c < n) ? cid[c] : num;
+        owner[p] = o;
+        const bool fixed_off = o >= num || single[o];
+        bool first = true;
+        if (!fixed_off) {
+            const int net = pin_net[p];
+            for (int q = p - 1; q >= 0 && pin_net[q] == net; q--) {
+                const int cq = pin_cell[q];
+                if (((cq >= 0 && cq < n) ? cid[cq] : num) == o) {
+                    first = false;
+                    break;
+                }
+            }
+        }
+        keep[p] = fixed_off || first;
+    }
+}
+
+__global__ void __launch_bounds__(256) coarse_write_kernel(const float2* pin_off, const int* pin_net, int num_pins,
+                                                           int num, const unsigned char* single, const int* owner,
+                                                           const int* keep, const int* at, int* out_cell,
+                                                           float2* out_off, int* out_net) {
+    pdl_wait();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < num_pins; p += gridDim.x * blockDim.x) {
+        if (!keep[p]) continue;
+        const int o = owner[p], k = at[p];
+        out_cell[k] = o;
+        out_off[k] = (o >= num || single[o]) ? pin_off[p] : make_float2(0.f, 0.f);
+        out_net[k] = pin_net[p];
+    }
+}
+
+// cells at a point of their cluster's square: cpos[cid] + (r - 0.5) (csize[cid] - size, clamped at 0), in float32
+// with the reference's operation order (no contraction into fused multiply-adds)
+__global__ void __launch_bounds__(256) expand_kernel(const float2* cpos, const int* cid, const float2* csize,
+                                                     const float2* size, const float2* r, int n, float2* pos) {
+    pdl_wait();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int k = cid[c];
+        const float2 cs = csize[k], s = size[c], q = cpos[k], u = r[c];
+        const float rx = fmaxf(__fsub_rn(cs.x, s.x), 0.f), ry = fmaxf(__fsub_rn(cs.y, s.y), 0.f);
+        pos[c] = make_float2(__fadd_rn(q.x, __fmul_rn(__fsub_rn(u.x, 0.5f), rx)),
+                             __fadd_rn(q.y, __fmul_rn(__fsub_rn(u.y, 0.5f), ry)));
+    }
+}
+
 __global__ void relabel_kernel(int* cid, int n, const int* new_index) {
     pdl_wait();
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) cid[c] = new_index[cid[c]];
@@ -419,6 +474,54 @@ extern "C" int gp103_cluster_relabel(int* cid, int n, const int* new_index, cuda
     if (n < 0 || (n > 0 && (!cid || !new_index))) return GP103_ERR_ARG;
     if (n == 0) return GP103_OK;
     if (launch_k(relabel_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, cid, n, new_index) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+extern "C" size_t gp103_coarse_pins_scratch(int num_pins) {
+    if (num_pins < 0) return 0;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    return 3 * al(4 * ((size_t)num_pins + 1)) + al(4 * (size_t)SCAN_MAX_TILES) + al(64);
+}
+
+extern "C" int gp103_coarse_pins(const int* pin_cell, const float* pin_off, const int* pin_net, int num_pins, int n,
+                                 const int* cid, int num, const unsigned char* single, void* scratch,
+                                 size_t scratch_bytes, int* out_cell, float* out_off, int* out_net, int* count,
+                                 cudaStream_t s) {
+    if (num_pins < 0 || n < 0 || num < 0 || !scratch || !count) return GP103_ERR_ARG;
+    if (num_pins > 0 && (!pin_cell || !pin_off || !pin_net || !out_cell || !out_off || !out_net)) return GP103_ERR_ARG;
+    if (n > 0 && (!cid || !single)) return GP103_ERR_ARG;
+    if (num_pins + 1LL > (long long)SCAN_TILE * SCAN_MAX_TILES) return GP103_ERR_TOO_LARGE;
+    if (scratch_bytes < gp103_coarse_pins_scratch(num_pins)) return GP103_ERR_ARG;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    char* base = (char*)scratch;
+    const size_t seg = al(4 * ((size_t)num_pins + 1));
+    int *owner = (int*)base, *keep = (int*)(base + seg), *at = (int*)(base + 2 * seg);
+    int* tile = (int*)(base + 3 * seg);
+    if (num_pins == 0) return cudaMemsetAsync(count, 0, sizeof(int), s) == cudaSuccess ? GP103_OK : GP103_ERR_CUDA;
+    const int g = grid_for(num_pins, 256, 8);
+    if (launch_k(coarse_keep_kernel, dim3(g), dim3(256), 0, s, pin_cell, pin_net, num_pins, n, cid, num, single, owner,
+                 keep) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (cudaMemsetAsync(keep + num_pins, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
+    int st;
+    if ((st = exclusive_scan(keep, num_pins + 1, at, tile, count, s))) return st;
+    if (launch_k(coarse_write_kernel, dim3(g), dim3(256), 0, s, (const float2*)pin_off, pin_net, num_pins, num, single,
+                 (const int*)owner, (const int*)keep, (const int*)at, out_cell, (float2*)out_off, out_net) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+extern "C" int gp103_expand(const float* cpos, const int* cid, const float* csize, const float* size,
+                            const float* draws, int n, float* pos, cudaStream_t s) {
+    if (n < 0 || (n > 0 && (!cpos || !cid || !csize || !size || !draws || !pos))) return GP103_ERR_ARG;
+    if (n == 0) return GP103_OK;
+    if (launch_k(expand_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, (const float2*)cpos, cid,
+                 (const float2*)csize, (const float2*)size, (const float2*)draws, n, (float2*)pos) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;

@@ -73,6 +73,9 @@ _SIGS = {
     "gp103_cluster_round": ([_vp, _vp, _vp, _i, _i, _vp, _vp, ctypes.c_longlong, ctypes.c_longlong, _i, _vp,
                              ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_cluster_relabel": ([_vp, _i, _vp, _vp], _i),
+    "gp103_coarse_pins_scratch": ([_i], ctypes.c_size_t),
+    "gp103_coarse_pins": ([_vp, _vp, _vp, _i, _i, _vp, _i, _vp, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp], _i),
+    "gp103_expand": ([_vp] * 5 + [_i, _vp, _vp], _i),
     "gp103_net_order": ([_vp] * 4 + [_i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 5 + [_vp], _i),
     "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
 }

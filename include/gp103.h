@@ -257,6 +257,22 @@ int gp103_cluster_round(const int* row_start, const int* col, const int* w, int 
                         int* col_out, int* w_out, int* counts, cudaStream_t stream);
 int gp103_cluster_relabel(int* cid, int n, const int* new_index, cudaStream_t stream);
 
+/* The pins of the cluster problem (coarse_problem, src/cluster.py:88-130): every pin of every net (pin_cell with n
+ * for a fixed pin, pin_off [num_pins, 2], pin_net sorted by net) mapped to its cluster (cid [n]; num for a fixed
+ * pin); a pin on a one-cell cluster (single [num] = 1) or a fixed pin is kept with its offset, otherwise only the first
+ * pin of its net on its cluster is kept, at the cluster's centre. Writes the kept pins in order (out_cell, out_off,
+ * out_net) and their number to count (device int). Scratch: gp103_coarse_pins_scratch(num_pins) bytes. */
+size_t gp103_coarse_pins_scratch(int num_pins);
+int gp103_coarse_pins(const int* pin_cell, const float* pin_off, const int* pin_net, int num_pins, int n, const int* cid,
+                      int num, const unsigned char* single, void* scratch, size_t scratch_bytes, int* out_cell,
+                      float* out_off, int* out_net, int* count, cudaStream_t stream);
+
+/* expand (src/cluster.py:133-144): pos[c] = cpos[cid[c]] + (draws[c] - 0.5) max(csize[cid[c]] - size[c], 0) for the n
+ * cells, float32 in the reference's operation order; draws [n, 2] are the caller's uniform draws (the reference's
+ * seeded CPU generator). The fillers' positions are the caller's to copy. */
+int gp103_expand(const float* cpos, const int* cid, const float* csize, const float* size, const float* draws, int n,
+                 float* pos, cudaStream_t stream);
+
 /* ------------------------------------------------------------------------------------------------ part 3
  * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
  * *out is written by the device (read it after synchronising the stream). */

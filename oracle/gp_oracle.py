@@ -19,6 +19,8 @@ Each function names the reference lines it restates (paths inside the AutoPlace 
   select          gp_cuda_kernel.cu:243-249
   place_level     src/run_placement.py:41-76 + src/gpu_loop.py:35-81 (host loop; the CPU baseline)
   cluster_*       src/cluster.py:38-85 (star matching: pair edges, rounds), integer sums: exact
+  coarse_pins     src/cluster.py:101-115 (the pins of the cluster problem)
+  expand          src/cluster.py:133-144
 """
 import ctypes
 import math
@@ -271,6 +273,17 @@ def cluster_round(i, j, w, area, head, cap, big, per_head=3):
     return new, carea, (key // len(kept), key % len(kept), nw)
 
 
+def cluster_limits(area, ratio):
+    """big and cap of cluster_cells (src/cluster.py:59-60) with the reference's own scalar arithmetic: torch on the
+    CPU (a float ratio makes cap a float32 floor division)."""
+    import torch
+    a = torch.as_tensor(np.asarray(area, np.int64))
+    big = 20 * a.sum() // len(a)
+    small = a < big
+    cap = 3 * ratio * a[small].sum() // (2 * int(small.sum()))
+    return int(big), int(math.floor(float(cap)))
+
+
 def cluster_cells(pin_cell, pin_net, area, ratio, draws, max_degree=8, per_head=3, max_rounds=12):
     """cluster_cells (src/cluster.py:38-85) with the head draws given: draws(r, num) -> float32 [num] uniform draws of
     round r (the reference's torch.rand of its seeded generator). -> (cluster of every cell, cluster areas)."""
@@ -278,9 +291,7 @@ def cluster_cells(pin_cell, pin_net, area, ratio, draws, max_degree=8, per_head=
     n = len(area)
     i, j, w = cluster_edges(pin_cell, pin_net, n, max_degree)
     cid, num = np.arange(n), n
-    big = 20 * int(area.sum()) // n
-    small = area < big
-    cap = 3 * ratio * int(area[small].sum()) // (2 * int(small.sum()))
+    big, cap = cluster_limits(area, ratio)
     for r in range(max_rounds):
         if num * ratio <= n:
             break
@@ -291,6 +302,31 @@ def cluster_cells(pin_cell, pin_net, area, ratio, draws, max_degree=8, per_head=
         new, area, (i, j, w) = res
         cid, num = new[cid], len(area)
     return cid, area
+
+
+def coarse_pins(pin_cell, pin_off, pin_net, n, cid, num, single):
+    """The pins of the cluster problem (src/cluster.py:101-115): each pin's cluster (num: fixed); pins of one-cell
+    clusters and fixed pins kept with their offsets, otherwise the first pin of each (net, cluster) at the centre.
+    -> (cell, off, net) of the kept pins, in pin order."""
+    pin_cell = np.asarray(pin_cell, np.int64)
+    owner = np.concatenate([np.asarray(cid, np.int64), [num]])[np.minimum(pin_cell, n)]
+    keep_off = np.concatenate([np.asarray(single, bool), [True]])[owner]
+    key = np.asarray(pin_net, np.int64) * (num + 1) + owner
+    order = np.argsort(key, kind="stable")
+    sk = key[order]
+    repeat = np.zeros(len(key), bool)
+    repeat[order[1:]] = (sk[1:] == sk[:-1]) & ~keep_off[order[1:]]
+    sel = ~repeat
+    off = np.where(keep_off[sel][:, None], np.asarray(pin_off, np.float32)[sel], np.float32(0))
+    return owner[sel], off.astype(np.float32), np.asarray(pin_net, np.int64)[sel]
+
+
+def expand(cpos, cid, csize, size, draws, num):
+    """expand (src/cluster.py:133-144) with the draws [n, 2] given: float32, in the reference's operation order."""
+    cpos = np.asarray(cpos, np.float32)
+    room = np.maximum(np.asarray(csize, np.float32)[cid] - np.asarray(size, np.float32), np.float32(0))
+    cells = cpos[:num][cid] + (np.asarray(draws, np.float32) - np.float32(0.5)) * room
+    return np.concatenate([cells, cpos[num:]]).astype(np.float32)
 
 
 # ------------------------------------------------------------------------------------------------ optimiser

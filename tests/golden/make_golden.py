@@ -14,6 +14,8 @@ tests read only these files: the reference sources are not needed to run them.
   golden_control.npz   ParamScheduler + resolution: the state after each step of a driven sequence
   golden_place.npz     global_placement_main (one level) on a small netlist: stop reason, iterations, HPWL, overflow
   golden_cluster.npz   cluster_cells: the merged pair edges, the head draws and edges of every round, the clusters
+  golden_coarse.npz    coarse_problem + expand: the cluster problem (sizes, pins, grid) and the expanded positions
+  golden_place2.npz    global_placement_main with two levels (cluster_ratio 5) on a small netlist
 """
 import math
 import os
@@ -234,12 +236,77 @@ def gen_cluster():
     print("cluster:", nl.num_mov, "cells ->", len(carea), "clusters in", len(draws), "rounds;", len(calls[6][0]), "edges")
 
 
+def _ref_problem(nl, opts):
+    """The reference's objects for a netlist, as run_placement_main builds them (CPU operators)."""
+    prob = problem.Problem(nl, opts)
+    n = nl.num_mov
+    t = lambda a, dt: torch.tensor(a, dtype=dt)
+    wl = Wirelength(t(nl.pin_cell, torch.long), t(nl.pin_off, torch.float32), t(nl.pin_net, torch.long), nl.num_nets,
+                    n, opts.ignore_net_degree)
+    ff = nl.fixed_fraction(prob.force_bin, prob.force_bin)
+    density = ElectronicDensityLayer(nl.width, nl.height, prob.force_bin, prob.force_bin, ff, prob.target,
+                                     prob.node_size, n, "cpu", np.concatenate([nl.cell_pins, np.zeros(prob.num_nodes - n)]))
+    if prob.force_bin != prob.num_bin:
+        density.judge = ElectronicDensityLayer(nl.width, nl.height, prob.num_bin, prob.num_bin,
+                                               nl.fixed_fraction(prob.num_bin, prob.num_bin), prob.target, nl.size, n,
+                                               "cpu", field=False)
+    data = SimpleNamespace(num_mov=n, mov_area=nl.mov_area, cell_pins=nl.cell_pins, width=nl.width, height=nl.height,
+                           fixed_fraction=nl.fixed_fraction)
+    return prob, wl, density, ff, data
+
+
+def gen_coarse():
+    """coarse_problem (src/cluster.py:88-130) and expand (:133-144) on a netlist with macros and fixed pins."""
+    from src import cluster as C
+    nl = synth.make_netlist(3000, 3200, window=100, macros=3, cover=0.1, fixed_pin_share=0.05, seed=41)
+    opts = problem.options(target_density=0.9, num_bin=32, force_num_bin=64, cluster_ratio=4.0, seed=3)
+    prob, wl, density, ff, data = _ref_problem(nl, opts)
+    args = SimpleNamespace(**vars(opts))
+    coarse = C.coarse_problem(data, prob.node_size, wl, density, ff, args)
+    cw = coarse.wirelength.all
+    rng = np.random.default_rng(9)
+    cpos = torch.tensor(rng.random((coarse.num_nodes, 2)) * [nl.width, nl.height], dtype=torch.float32)
+    pos = C.expand(cpos, coarse, prob.node_size, opts.seed)
+    cd = coarse.density
+    np.savez_compressed(os.path.join(HERE, "golden_coarse.npz"), seed=41, cells=3000, nets=3200, window=100, macros=3,
+                        cover=0.1, fixed_pin_share=0.05, target_density=0.9, num_bin=32, force_num_bin=64,
+                        cluster_ratio=4.0, cluster_seed=3,
+                        cid=coarse.cid.numpy(), num=coarse.num, size=coarse.size.numpy(),
+                        pin_cell=cw["cell"].numpy(), pin_off=cw["off"].numpy(), pin_net=cw["net"].numpy(),
+                        num_nets=cw["num_nets"], nbx=cd.nbx, smooth_size=cd.smooth["size"].numpy(),
+                        smooth_ratio=cd.smooth["ratio"].numpy(), pins=cd.pins.numpy(), fixed_map=cd.fixed_map.numpy(),
+                        total_pins=coarse.total_pins, total_area=coarse.total_area, num_nodes=coarse.num_nodes,
+                        cpos=cpos.numpy(), pos=pos.numpy())
+    print("coarse:", coarse.num, "clusters,", cd.nbx, "bins,", len(cw["cell"]), "pins")
+
+
+def gen_place2():
+    """The two-level run: clusters placed first (until the hand-over smoothing), then the cells."""
+    nl = synth.make_netlist(2500, 2620, window=80, macros=0, seed=21)
+    opts = problem.options(target_density=1.0, num_bin=32, force_num_bin=0, cluster_ratio=5.0, inner_iter=3000, seed=2)
+    prob, wl, density, ff, data = _ref_problem(nl, opts)
+    n = nl.num_mov
+    pos0 = synth.init_positions(nl, prob.num_nodes, seed=0)
+    pos = torch.tensor(pos0)
+    args = SimpleNamespace(**vars(opts))
+    stats = run_placement.global_placement_main(data, wl, density, pos, prob.node_size, ff, args, _Log())
+    hpwl = float(wl.hpwl(pos))
+    ovf = float(density.exact_overflow(pos[:n].contiguous()))
+    np.savez_compressed(os.path.join(HERE, "golden_place2.npz"), pos0=pos0, cells=2500, nets=2620, window=80, seed=21,
+                        num_bin=32, cluster_ratio=5.0, cluster_seed=2, clusters=stats["clusters"],
+                        coarse_iters=stats["coarse_iters"], iters=stats["iters"], reason=stats["stop_reason"], hpwl=hpwl,
+                        overflow=ovf, coarse_num_bin=stats["coarse_num_bin"])
+    print("place2:", stats)
+
+
 if __name__ == "__main__" and len(sys.argv) > 1:
     for name in sys.argv[1:]:
         globals()["gen_" + name]()
     sys.exit(0)
 
 if __name__ == "__main__":
+    gen_coarse()
+    gen_place2()
     gen_cluster()
     gen_wa()
     gen_density()

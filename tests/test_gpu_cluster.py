@@ -65,3 +65,29 @@ def test_clusters_match_oracle(cells, seed, ratio):
     cid, carea = cluster.cluster_cells(nl.pin_cell, nl.pin_net, area, ratio, seed, draws=draws)
     assert np.array_equal(cid, ocid) and np.array_equal(carea, oarea)
     assert len(carea) < cells and int(carea.sum()) == int(area.sum())
+
+
+def test_coarse_problem_and_expand_match_reference(gold):
+    """The cluster problem built on the device (clusters, sizes, pins, grid, smoothed nodes, totals) and expand."""
+    from autoplace_gb300 import problem
+    g = gold("golden_coarse.npz")
+    nl = synth.make_netlist(int(g["cells"]), int(g["nets"]), window=int(g["window"]), macros=int(g["macros"]),
+                            cover=float(g["cover"]), fixed_pin_share=float(g["fixed_pin_share"]), seed=int(g["seed"]))
+    opts = problem.options(target_density=float(g["target_density"]), num_bin=int(g["num_bin"]),
+                           force_num_bin=int(g["force_num_bin"]), cluster_ratio=float(g["cluster_ratio"]),
+                           seed=int(g["cluster_seed"]))
+    prob = problem.Problem(nl, opts)
+    coarse = cluster.coarse_problem(prob)
+    cp = coarse.problem
+    assert np.array_equal(coarse.cid, g["cid"]) and coarse.num == int(g["num"])
+    assert np.array_equal(coarse.size.view(np.uint32), np.asarray(g["size"], np.float32).view(np.uint32))
+    assert np.array_equal(cp.nl.pin_cell, g["pin_cell"]) and np.array_equal(cp.nl.pin_net, g["pin_net"])
+    assert np.array_equal(np.asarray(cp.nl.pin_off, np.float32).view(np.uint32), g["pin_off"].view(np.uint32))
+    assert cp.force_bin == int(g["nbx"]) and cp.num_nodes == int(g["num_nodes"])
+    assert np.array_equal(cp.force.size.view(np.uint32), g["smooth_size"].view(np.uint32))
+    assert np.array_equal(cp.force.ratio.view(np.uint32), g["smooth_ratio"].view(np.uint32))
+    assert np.array_equal(cp.pins.view(np.uint32), g["pins"].view(np.uint32))
+    assert np.array_equal(cp.force.fixed_map.view(np.uint32), g["fixed_map"].view(np.uint32))
+    assert cp.total_pins == float(g["total_pins"]) and abs(cp.total_area - float(g["total_area"])) <= 1e-9 * cp.total_area
+    pos = cluster.expand(g["cpos"], coarse, prob, int(g["cluster_seed"])).cpu().numpy()
+    assert np.array_equal(pos.view(np.uint32), g["pos"].view(np.uint32))

@@ -184,3 +184,36 @@ def test_cluster_matches_reference(gold):
     cid, area = O.cluster_cells(g["pin_cell"], g["pin_net"], g["area"], int(g["ratio"]), lambda r, num: g["draw%d" % r])
     assert np.array_equal(cid, g["cid"]) and np.array_equal(area, g["carea"])
     assert len(area) < int(g["n"]) and int(area.sum()) == int(g["area"].sum())
+
+
+def _coarse_case(g):
+    nl = synth.make_netlist(int(g["cells"]), int(g["nets"]), window=int(g["window"]), macros=int(g["macros"]),
+                            cover=float(g["cover"]), fixed_pin_share=float(g["fixed_pin_share"]), seed=int(g["seed"]))
+    opts = problem.options(target_density=float(g["target_density"]), num_bin=int(g["num_bin"]),
+                           force_num_bin=int(g["force_num_bin"]), cluster_ratio=float(g["cluster_ratio"]),
+                           seed=int(g["cluster_seed"]))
+    return nl, problem.Problem(nl, opts)
+
+
+def test_coarse_problem_and_expand_match_reference(gold):
+    """coarse_problem (src/cluster.py:88-130: clusters, their sizes and pins) and expand (:133-144), with the
+    reference's own generator draws."""
+    torch = pytest.importorskip("torch")
+    g = gold("golden_coarse.npz")
+    nl, prob = _coarse_case(g)
+    n = nl.num_mov
+    size = np.asarray(prob.node_size[:n], np.float32)
+    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
+    gen = torch.Generator().manual_seed(int(g["cluster_seed"]))
+    cid, carea = O.cluster_cells(nl.pin_cell, nl.pin_net, area, float(g["cluster_ratio"]),
+                                 lambda r, num: torch.rand(num, generator=gen).numpy())
+    assert np.array_equal(cid, g["cid"]) and len(carea) == int(g["num"])
+    num = len(carea)
+    single = np.bincount(cid, minlength=num) == 1
+    c, off, net = O.coarse_pins(nl.pin_cell, nl.pin_off, nl.pin_net, n, cid, num, single)
+    assert np.array_equal(c, g["pin_cell"]) and np.array_equal(net, g["pin_net"])
+    assert np.array_equal(off.view(np.uint32), g["pin_off"].view(np.uint32))
+    gen = torch.Generator().manual_seed(int(g["cluster_seed"]))
+    csize = np.asarray(g["size"], np.float32)
+    pos = O.expand(g["cpos"], cid, csize, size, torch.rand(n, 2, generator=gen).numpy(), num)
+    assert np.array_equal(pos.view(np.uint32), g["pos"].view(np.uint32))
