@@ -56,6 +56,18 @@ def net_order(net_start, cell32, cell_pin):
     return perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum()), int((cls < 4).sum())
 
 
+def field_mode(mode, nbx, nby):
+    """The field mode a grid of nbx x nby bins runs in: `mode`, or fp32 where the tensor-core field cannot tile the
+    grid (gp103_plan_sizes answers GP103_ERR_SHAPE)."""
+    if mode == native.FIELD_FP32:
+        return mode
+    rc = native.lib().gp103_plan_sizes(nbx, nby, mode, ctypes.byref(Sizes()))
+    if rc == native.ERR_SHAPE:
+        return native.FIELD_FP32
+    native.check(rc, "gp103_plan_sizes")
+    return mode
+
+
 def pinned_inputs(prob):
     """The problem arrays a Placer uploads, as pinned CPU tensors ({name: tensor}). A caller that keeps its inputs in
     pinned memory passes them as Placer(prob, host=...): the uploads are then asynchronous DMA copies."""
@@ -70,12 +82,17 @@ def pinned_inputs(prob):
 
 class Placer(object):
     def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None,
-                 sort_every=None, host=None):
+                 sort_every=None, host=None, handover_gamma=0.0):
         """host: optional {name: pinned CPU tensor} holding the problem's arrays (pinned_inputs), uploaded instead
-        of the Problem's numpy arrays."""
+        of the Problem's numpy arrays. handover_gamma: a run on clusters stops ("handover") once its smoothing is
+        down to this (the smoothing the cells start with); 0 = never.
+        A tensor-core field (bf16x3, bf16x6) needs a grid of multiples of 128 bins per side: on a smaller grid
+        (clusters, small designs) the field runs in fp32."""
         self.p = prob
         self.dev = torch.device(device or "cuda")
-        self.mode = native.FIELD_MODES[field] if isinstance(field, str) else int(field)
+        self.mode = field_mode(native.FIELD_MODES[field] if isinstance(field, str) else int(field),
+                               prob.force.nbx, prob.force.nby)
+        self.handover_gamma = float(handover_gamma or 0.0)
         self.check_every = check_every
         self.use_graphs = use_graphs
         # density passes between refreshes of the scatter's spatial order (an order only speeds the scatter up)
@@ -155,7 +172,7 @@ class Placer(object):
         self.S = z((len(S_FIELDS),), torch.float64)
         self.T = z((T_SIZE,), torch.float64)
         self.kp = z((5,), torch.float32)
-        self.c = t(prob.constants(), torch.float64)
+        self.c = t(prob.constants(self.handover_gamma), torch.float64)
         self.pin_grad = z((max(P, 1), 2), torch.float32)
         self.map = z((2, f.nbx, f.nby), torch.int64)
         self.red = z((sz.red,), torch.float64)
@@ -257,73 +274,99 @@ class Placer(object):
         h = out.cpu().numpy()
         return float(h[0]), float(h[1])
 
+    def tension_unit(self, pos):
+        """(#pins / L1 norm over the cells of the plain density gradient at pos, overflow at pos): the unit the
+        density weight is given in (Objective.tension_unit, src/calculator.py:20-24) and the overflow of the same
+        density pass (density.forward(pos)[1])."""
+        out = self.eval(pos, self.tmp[0], weight=1.0, precond=-1.0, with_wl=False)
+        return float(self.p.pins.astype(np.float64).sum()) / float(out[4]), float(out[3]) * self.overflow_scale()
+
+    def hpwl(self, pos):
+        """HPWL of the optimised nets at pos (wirelength.forward(pos, wa_coeff)[2])."""
+        with torch.cuda.stream(self.stream):
+            self.kp[0] = 10 * self.p.base_gamma
+        return float(self.eval(pos, self.tmp[0], weight=0.0, with_wl=True)[2])
+
     # ------------------------------------------------------------------ one level
-    def run(self, pos0, log=None):
+    def run(self, pos0, log=None, resume=None):
         """Place from pos0 ([num_nodes, 2], host or device) to the stop. -> dict (reason, iters, start_iters, hpwl,
-        overflow, evals, seconds, pos = final positions on the device)."""
+        overflow, evals, seconds, pos = final positions on the device, iter, lam, gam).
+        resume: dict(lam, gam, iter, hpwl, first_iter) to go on where a run on the clusters stopped
+        (ParamScheduler.resume, src/param_scheduler.py:53-60; _place_level from first_iter, src/run_placement.py:41):
+        the density weight lam and smoothing gam carried over, the scheduler's iteration count and last HPWL, the
+        loop counted on from first_iter; no wirelength-only start while lam > 0."""
         p, o = self.p, self.p.opts
         t0 = time.time()
+        r = resume or {}
+        lam0 = float(r.get("lam", 0.0))
+        gam = float(r["gam"]) if resume else 10 * p.base_gamma
+        first = int(r.get("first_iter", 0))
+        w, pc = (lam0, lam0) if lam0 > 0 else (0.0, -1.0)
         with torch.cuda.stream(self.stream):
             v = self.V[0]
             v.copy_(torch.as_tensor(pos0, dtype=torch.float32).to(self.dev, non_blocking=True))
             torch.max(torch.min(v, self.hi), self.lo, out=v)
-            gam = 10 * p.base_gamma
-            self.kp.copy_(torch.tensor([gam, 0, 0, 0, 0], dtype=torch.float32))
+            self.kp.copy_(torch.tensor([gam, lam0, lam0, 0, 0], dtype=torch.float32))
             self.cur.zero_()
         g, probe, g2 = self.G[0], self.tmp[0], self.tmp[1]
         evals = 0
-        # estimate_initial_learning_rate
-        self.eval(v, g)
+        # estimate_initial_learning_rate (with the density term once its weight is on)
+        self.eval(v, g, weight=w, precond=pc)
         d1 = self.probe(v, g, o.lr, probe)
-        d2 = self.eval(probe, g2, g_ref=g)[0]
+        d2 = self.eval(probe, g2, g_ref=g, weight=w, precond=pc)[0]
         lr = math.sqrt(d1) / math.sqrt(d2)
         # NesterovOptimizer.__init__: the gradient again (same point, same bits), then the optimiser's own probe
-        self.eval(v, g)
+        self.eval(v, g, weight=w, precond=pc)
         with torch.cuda.stream(self.stream):
             self.U[0].copy_(v)
         d1 = self.probe(v, g, lr, probe)
-        d2 = self.eval(probe, g2, g_ref=g)[0]
+        d2 = self.eval(probe, g2, g_ref=g, weight=w, precond=pc)[0]
         alpha = math.sqrt(d1) / math.sqrt(d2)
         evals += 4
-        # the wirelength-only start
-        Th = np.zeros(T_SIZE)
-        Th[TI["alpha"]], Th[TI["a"]] = alpha, 1.0
-        Th[TI["start_tol"]], Th[TI["inner"]] = o.start_tol, o.inner_iter
-        with torch.cuda.stream(self.stream):
-            self.T.copy_(torch.as_tensor(Th))
-            self.kp.copy_(torch.tensor([gam, 0, 0, alpha, 0.0], dtype=torch.float32))
-        while True:
-            self._replay(native.PHASE_START)
-            self.sync()
-            Th = self.T.cpu().numpy()
-            if Th[TI["done"]] or Th[TI["stop"]]:
-                break
-        evals += int(Th[TI["evals"]])
-        start_iters = int(Th[TI["loop_it"]])
-        if Th[TI["stop"]]:
-            reason = REASON[int(Th[TI["stop"]])]
+        if lam0 > 0:
+            start_iters, cur = 0, 0
+            lam, a, it0, iter0, hpwl_prev = lam0, 1.0, first, int(r["iter"]), float(r["hpwl"])
+        else:
+            # the wirelength-only start
+            Th = np.zeros(T_SIZE)
+            Th[TI["alpha"]], Th[TI["a"]] = alpha, 1.0
+            Th[TI["start_tol"]], Th[TI["inner"]] = o.start_tol, o.inner_iter
+            Th[TI["iter"]], Th[TI["loop_it"]] = int(r.get("iter", 0)), first
+            with torch.cuda.stream(self.stream):
+                self.T.copy_(torch.as_tensor(Th))
+                self.kp.copy_(torch.tensor([gam, 0, 0, alpha, 0.0], dtype=torch.float32))
+            while True:
+                self._replay(native.PHASE_START)
+                self.sync()
+                Th = self.T.cpu().numpy()
+                if Th[TI["done"]] or Th[TI["stop"]]:
+                    break
+            evals += int(Th[TI["evals"]])
+            start_iters = int(Th[TI["loop_it"]])
+            if Th[TI["stop"]]:
+                reason = REASON[int(Th[TI["stop"]])]
+                cur = int(self.cur.cpu())
+                return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
+                            overflow=float("nan"), evals=evals, seconds=time.time() - t0, pos=self.V[cur],
+                            iter=int(Th[TI["iter"]]), lam=0.0, gam=gam, density_iters=0)
             cur = int(self.cur.cpu())
-            return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
-                        overflow=float("nan"), evals=evals, seconds=time.time() - t0, pos=self.V[cur])
-        cur = int(self.cur.cpu())
-        # first density weight: density_weight x tension unit (Objective.tension_unit)
-        out = self.eval(self.V[cur], self.tmp[0], weight=1.0, precond=-1.0, with_wl=False)
-        lam = o.density_weight * float(p.pins.astype(np.float64).sum()) / float(out[4])
-        if log:
-            log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
-                % (start_iters, Th[TI["hpwl"]], lam))
+            # first density weight: density_weight x tension unit (Objective.tension_unit)
+            lam = o.density_weight * self.tension_unit(self.V[cur])[0]
+            if log:
+                log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
+                    % (start_iters, Th[TI["hpwl"]], lam))
+            alpha, a, it0, iter0, hpwl_prev = Th[TI["alpha"]], Th[TI["a"]], start_iters, Th[TI["iter"]], Th[TI["hpwl"]]
         S = np.zeros(len(S_FIELDS))
-        S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, gam, Th[TI["alpha"]], Th[TI["a"]]
-        S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = Th[TI["iter"]], Th[TI["hpwl"]], 1.0
+        S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, gam, alpha, a
+        S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = iter0, hpwl_prev, 1.0
         S[SK["best_hpwl"]] = S[SK["best_ovf"]] = math.inf
-        S[SK["loop_it"]] = start_iters
-        a = Th[TI["a"]]
+        S[SK["loop_it"]] = it0
         coef = (a - 1) / ((1 + math.sqrt(4 * a * a + 1)) / 2)
         with torch.cuda.stream(self.stream):
             self.S.copy_(torch.as_tensor(S))
-            self.kp.copy_(torch.tensor([gam, lam, lam, Th[TI["alpha"]], coef], dtype=torch.float32))
+            self.kp.copy_(torch.tensor([gam, lam, lam, alpha, coef], dtype=torch.float32))
             self.best.copy_(self.V[cur])
-        logged = start_iters // o.log_freq
+        logged = it0 // o.log_freq
         while True:
             self._replay(native.PHASE_DENSITY)
             self.sync()
@@ -343,5 +386,5 @@ class Placer(object):
         return dict(reason=REASON[int(Sh[SK["stop"]])], iters=int(Sh[SK["loop_it"]]), start_iters=start_iters,
                     hpwl=float(Sh[SK["res_hpwl"]]), overflow=float(Sh[SK["res_ovf"]]),
                     evals=evals + int(Sh[SK["evals"]]), seconds=time.time() - t0, pos=pos,
-                    density_iters=int(Sh[SK["loop_it"]]) - start_iters, lam=float(Sh[SK["lam"]]),
-                    gam=float(Sh[SK["gam"]]))
+                    density_iters=int(Sh[SK["loop_it"]]) - it0, lam=float(Sh[SK["lam"]]),
+                    gam=float(Sh[SK["gam"]]), iter=int(Sh[SK["iter"]]))

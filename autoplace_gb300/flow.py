@@ -1,0 +1,89 @@
+"""Global placement of one design: one level, or two (the clusters first, then the cells), on the device.
+
+Mirrors global_placement_main (src/run_placement.py:79-122):
+  - cluster_ratio <= 1: one level of the cells (engine.Placer.run);
+  - cluster_ratio > 1 (two levels):
+      1. the clusters and their problem (cluster.coarse_problem: star matching, pins and sizes on the device);
+      2. one level of the clusters, with no settle and no minimum iteration count, stopped ("handover") once its
+         smoothing is down to the one the cells start with (10 x the cells' base gamma);
+      3. the cells spread over their clusters' squares (cluster.expand) and clamped into the region;
+      4. the density weight carried over in tension units: weight = lam of the clusters x tension unit of the cells
+         / tension unit of the clusters (the same share of the wire tension on both levels); the smoothing in units
+         of the bin (wa_rule accuracy) or from the cells' overflow (wa_rule overflow); the scheduler's iteration
+         count and the cells' HPWL (ParamScheduler.resume);
+      5. one level of the cells from there, counted on from the clusters' last iteration, with no wirelength-only
+         start.
+"""
+import time
+
+import torch
+
+from . import cluster
+from .engine import Placer
+
+
+def _gamma(base_gamma, overflow):
+    """ParamScheduler.gamma (src/param_scheduler.py:50-51): the smoothing of the overflow rule."""
+    return base_gamma * 10 ** ((overflow - 0.1) * 20 / 9 - 1)
+
+
+def global_placement(prob, pos0, field="bf16x6", device="cuda", log=None, check_every=16, use_graphs=True,
+                     stream=None):
+    """Place prob from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
+    (stop_reason, iters, start_iters, gp_time_s, per_iter_s, grad_calls; with two levels also clusters,
+    cluster_time_s, coarse_num_bin, coarse_iters) plus pos (final positions on the device), hpwl and overflow
+    of the kept placement as the control measured them, and placer (the cells' Placer: placer.evaluate(pos) gives
+    the exact HPWL and overflow)."""
+    o, n = prob.opts, prob.num_mov
+    dev = torch.device(device)
+    stream = stream or torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    start = time.time()
+    kw = dict(field=field, device=dev, check_every=check_every, use_graphs=use_graphs, stream=stream)
+    fine = Placer(prob, **kw)
+    stats, evals, resume, start_iters = {}, 0, None, 0
+    if o.cluster_ratio > 1:
+        coarse = cluster.coarse_problem(prob, device=dev, stream=stream)
+        cp = coarse.problem
+        stream.synchronize()
+        stats = dict(clusters=coarse.num, cluster_time_s=time.time() - start, coarse_num_bin=cp.force.nbx)
+        if log:
+            log("two levels: %d clusters of %d cells (%.2fs), %d x %d bins"
+                % (coarse.num, n, stats["cluster_time_s"], cp.force.nbx, cp.force.nby))
+        start_gamma = 10 * prob.base_gamma                      # the smoothing the cells start with
+        cplacer = Placer(cp, handover_gamma=start_gamma, **kw)
+        with torch.cuda.stream(stream):
+            p0 = torch.as_tensor(pos0, dtype=torch.float32).to(dev)
+            cpos0 = torch.cat([p0[:coarse.num], p0[n:]])
+        level = cplacer.run(cpos0, log=log)
+        cpos = level["pos"]
+        pos = cluster.expand(cpos, coarse, prob, o.seed, device=dev, stream=stream)
+        with torch.cuda.stream(stream):
+            torch.max(torch.min(pos, fine.hi), fine.lo, out=pos)
+        # the same share of the wire tension on both levels
+        tu_fine, ovf_fine = fine.tension_unit(pos)
+        tu_coarse = cplacer.tension_unit(cpos)[0]
+        weight = level["lam"] * tu_fine / tu_coarse
+        if o.wa_rule == "accuracy":                             # the same smoothing in units of the bin
+            gam = level["gam"] / cp.base_gamma * prob.base_gamma
+        else:
+            gam = _gamma(prob.base_gamma, ovf_fine)
+        resume = dict(lam=weight, gam=gam, iter=level["iter"], hpwl=fine.hpwl(pos), first_iter=level["iters"])
+        if log:
+            log("clusters placed after %d iterations (stop: %s, hpwl %.4E, overflow %.4f): the cells take over, "
+                "density weight %.4E" % (level["iters"], level["reason"], level["hpwl"], level["overflow"], weight))
+        evals, start_iters = level["evals"], level["start_iters"]
+        stats["coarse_iters"] = level["iters"]
+        pos0 = pos
+        del cplacer, coarse, cp, cpos                            # the clusters' buffers are not needed any more
+    level = fine.run(pos0, log=log, resume=resume)
+    torch.cuda.synchronize(dev)
+    gp_time, iters = time.time() - start, level["iters"]
+    if log:
+        log("GP stop (%s): #iters %d hpwl: %.6E overflow: %.4f GP time: %.4fs per iter: %.6fs (%d gradient calls)"
+            % (level["reason"], iters, level["hpwl"], level["overflow"], gp_time, gp_time / max(iters, 1),
+               evals + level["evals"]))
+    stats.update(stop_reason=level["reason"], iters=iters, start_iters=start_iters or level["start_iters"],
+                 gp_time_s=gp_time, per_iter_s=gp_time / max(iters, 1), grad_calls=evals + level["evals"],
+                 pos=level["pos"], hpwl=level["hpwl"], overflow=level["overflow"], placer=fine)
+    return stats

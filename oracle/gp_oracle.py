@@ -21,6 +21,7 @@ Each function names the reference lines it restates (paths inside the AutoPlace 
   cluster_*       src/cluster.py:38-85 (star matching: pair edges, rounds), integer sums: exact
   coarse_pins     src/cluster.py:101-115 (the pins of the cluster problem)
   expand          src/cluster.py:133-144
+  two_level       src/run_placement.py:87-110 with src/param_scheduler.py:53-60 (clusters first, then the cells)
 """
 import ctypes
 import math
@@ -485,12 +486,18 @@ class CpuLevel(object):
         g, _ = self.density(pos, None, 1.0, -1.0)
         return float(self.p.pins.astype(np.float64).sum() / np.abs(g[:self.p.num_mov]).sum())
 
-    def run(self, pos0, max_iters=None, time_budget=None, log=None):
+    def run(self, pos0, max_iters=None, time_budget=None, log=None, resume=None, handover_gamma=0.0):
         """Place from pos0 until the stop (or `max_iters` iterations / `time_budget` seconds of the loop).
-        -> dict(reason, iters, hpwl, overflow, pos, start_iters, seconds, density_iters)."""
+        resume: dict(lam, gam, iter, hpwl, first_iter): go on where a run on the clusters stopped
+        (ParamScheduler.resume, src/param_scheduler.py:53-60): the loop counted from first_iter, no wirelength-only
+        start while lam > 0. handover_gamma: stop ("handover") once the smoothing is down to it.
+        -> dict(reason, iters, hpwl, overflow, pos, start_iters, seconds, density_iters, iter, lam, gam)."""
         p, o = self.p, self.p.opts
         lo, hi = p.force.pos_lo.astype(np.float64), p.force.pos_hi.astype(np.float64)
-        gam, lam = 10 * p.base_gamma, 0.0
+        r = resume or {}
+        gam, lam = (float(r["gam"]), float(r["lam"])) if resume else (10 * p.base_gamma, 0.0)
+        first = int(r.get("first_iter", 0))
+        cvec = p.constants(handover_gamma)
         t0 = time.time()
         # estimate_initial_learning_rate + NesterovOptimizer.__init__ (src/nesterov_optimizer.py:15-32,56-61)
         v = np.clip(np.asarray(pos0, np.float64), lo, hi)
@@ -503,14 +510,23 @@ class CpuLevel(object):
         alpha = np.linalg.norm(v - probe) / np.linalg.norm(g - self.grad(probe, lam, gam)[0])
         a = 1.0
         wa_hist, hpwl_hist = [], []
-        it_sched, start_iters, reason = 0, 0, "max_iter"
-        it = 0
+        it_sched, start_iters, reason = int(r.get("iter", 0)), 0, "max_iter"
+        it = first
         S = None
         best = None
         hpwl = ovf = float("nan")
-        limit = o.inner_iter if max_iters is None else min(o.inner_iter, max_iters)
+        limit = o.inner_iter if max_iters is None else min(o.inner_iter, first + max_iters)
         density_iters = 0
-        for it in range(o.inner_iter):
+        if lam > 0:                                         # resumed with the density term on
+            S = np.zeros(len(FIELDS))
+            S[K["lam"]], S[K["gam"]], S[K["alpha"]], S[K["a"]] = lam, gam, alpha, a
+            S[K["iter"]], S[K["hpwl_prev"]] = it_sched, float(r["hpwl"])
+            S[K["mu"]] = 1.0
+            S[K["best_hpwl"]] = S[K["best_ovf"]] = float("inf")
+            S[K["loop_it"]] = first
+            kp = np.array([gam, lam, lam, alpha, 0.0], np.float32)
+            best = v.copy()
+        for it in range(first, o.inner_iter):
             if it >= limit or (time_budget is not None and time.time() - t0 > time_budget):
                 reason = "sample"
                 break
@@ -537,7 +553,6 @@ class CpuLevel(object):
                     S[K["best_hpwl"]] = S[K["best_ovf"]] = float("inf")
                     S[K["loop_it"]] = it + 1
                     kp = np.array([gam, lam, lam, alpha, (a - 1) / ((1 + math.sqrt(4 * a * a + 1)) / 2)], np.float32)
-                    cvec = p.constants()
                     best = v.copy()
                 continue
             density_iters += 1
@@ -559,4 +574,55 @@ class CpuLevel(object):
         res_h = float(S[K["res_hpwl"]]) if S is not None else hpwl
         res_o = float(S[K["res_ovf"]]) if S is not None else ovf
         return dict(reason=reason, iters=iters, hpwl=res_h, overflow=res_o, pos=v, start_iters=start_iters,
-                    seconds=time.time() - t0, density_iters=density_iters, evals=self.evals)
+                    seconds=time.time() - t0, density_iters=density_iters, evals=self.evals,
+                    iter=int(S[K["iter"]]) if S is not None else it_sched,
+                    lam=float(S[K["lam"]]) if S is not None else 0.0, gam=float(S[K["gam"]]) if S is not None else gam)
+
+
+def two_level(prob, pos0, dtype=np.float64, field="dct"):
+    """global_placement_main's two-level branch (src/run_placement.py:87-110) on the CPU: the clusters (cluster_cells
+    with the reference's seeded torch draws), their problem (coarse_pins; sizes as squares of the summed area, a
+    one-cell cluster keeping its shape; the grid between the overflow grid and the cells' force grid), one level of
+    the clusters until the hand-over smoothing (10 x the cells' base gamma), expand, the density weight carried over
+    in tension units, then one level of the cells resumed from there.
+    -> dict(clusters, coarse_num_bin, coarse_iters, reason, iters, pos, hpwl, overflow)."""
+    import torch
+    from types import SimpleNamespace
+    from autoplace_gb300 import problem as P
+    nl, o, n = prob.nl, prob.opts, prob.num_mov
+    size = np.asarray(prob.node_size[:n], np.float32)
+    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
+    gen = torch.Generator().manual_seed(int(o.seed))
+    cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio,
+                               lambda r, num: torch.rand(num, generator=gen).numpy())
+    num = len(carea)
+    csize = np.repeat(np.sqrt(carea.astype(np.float64) / 1024).astype(np.float32)[:, None], 2, 1)
+    single = np.bincount(cid, minlength=num) == 1
+    member = np.zeros(num, np.int64)
+    member[cid] = np.arange(n)
+    csize[single] = size[member[single]]
+    c_cell, c_off, c_net = coarse_pins(nl.pin_cell, nl.pin_off, nl.pin_net, n, cid, num, single)
+    fine_ff = nl.fixed_fraction(prob.force_bin, prob.force_bin)
+    nb = min(prob.force_bin, P.force_num_bin(num, 1.0 - float(fine_ff.mean()), prob.num_bin))
+    ff = fine_ff if nb == prob.force_bin else nl.fixed_fraction(nb, nb)
+    copts = SimpleNamespace(**vars(o))
+    copts.settle_iter, copts.min_iter = 0, 0
+    cprob = P.Problem.clusters(prob, csize, c_cell, c_off, c_net, nb, ff, copts)
+    pos0 = np.asarray(pos0, np.float32)
+    coarse = CpuLevel(cprob, dtype, field)
+    level = coarse.run(np.concatenate([pos0[:num], pos0[n:]]), handover_gamma=10 * prob.base_gamma)
+    cpos = np.asarray(level["pos"], np.float32)
+    gen = torch.Generator().manual_seed(int(o.seed))
+    pos = expand(cpos, cid, csize, size, torch.rand(n, 2, generator=gen).numpy(), num)
+    pos = np.clip(pos, prob.force.pos_lo, prob.force.pos_hi)
+    fine = CpuLevel(prob, dtype, field)
+    weight = level["lam"] * fine.tension_unit(pos.astype(np.float64)) / coarse.tension_unit(cpos.astype(np.float64))
+    if o.wa_rule == "accuracy":
+        gam = level["gam"] / cprob.base_gamma * prob.base_gamma
+    else:
+        ovf = fine.density(pos.astype(np.float64), None, 1.0, -1.0)[1]
+        gam = prob.base_gamma * 10 ** ((ovf - 0.1) * 20 / 9 - 1)
+    hpwl = fine.wirelength(pos.astype(np.float64), 10 * prob.base_gamma)[2]
+    r = fine.run(pos, resume=dict(lam=weight, gam=gam, iter=level["iter"], hpwl=hpwl, first_iter=level["iters"]))
+    return dict(clusters=num, coarse_num_bin=nb, coarse_iters=level["iters"], coarse_reason=level["reason"],
+                reason=r["reason"], iters=r["iters"], pos=r["pos"], hpwl=r["hpwl"], overflow=r["overflow"])

@@ -120,3 +120,42 @@ def test_divergence_keeps_last_finite_point():
     S = pl.S.cpu().numpy()
     assert S[SK["stop"]] == 3 and int(pl.cur.cpu()) == cur
     assert torch.equal(pl.V[cur], before) and bool(torch.isfinite(pl.V[cur]).all())
+
+
+def _two_level_case(g):
+    nl = synth.make_netlist(int(g["cells"]), int(g["nets"]), window=int(g["window"]), macros=0, seed=int(g["seed"]))
+    opts = problem.options(target_density=1.0, num_bin=int(g["num_bin"]), force_num_bin=0,
+                           cluster_ratio=float(g["cluster_ratio"]), inner_iter=3000, seed=int(g["cluster_seed"]))
+    return problem.Problem(nl, opts)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_two_levels_match_reference_run(gold, graphs):
+    """The reference's own two-level run (golden_place2.npz: the clusters placed until the hand-over smoothing, then
+    the cells) and this GPU run (global_placement, src/run_placement.py:79-122): the same clusters (integer work,
+    exact) and cluster grid, the same stop, the clusters' iterations within 3, the total within 5 %, HPWL within
+    0.5 %, overflow within 0.005."""
+    from autoplace_gb300.flow import global_placement
+    g = gold("golden_place2.npz")
+    prob = _two_level_case(g)
+    st = global_placement(prob, g["pos0"], field="fp32", use_graphs=graphs)
+    assert st["clusters"] == int(g["clusters"]) and st["coarse_num_bin"] == int(g["coarse_num_bin"])
+    assert abs(st["coarse_iters"] - int(g["coarse_iters"])) <= 3
+    assert st["stop_reason"] == str(g["reason"])
+    assert abs(st["iters"] - int(g["iters"])) <= 0.05 * int(g["iters"])
+    hpwl, ovf = st["placer"].evaluate(st["pos"])
+    assert abs(hpwl - float(g["hpwl"])) <= 0.005 * float(g["hpwl"])
+    assert abs(ovf - float(g["overflow"])) <= 0.005
+
+
+def test_two_levels_single_level_when_ratio_is_one(gold):
+    """cluster_ratio 1: global_placement is one level of the cells, as Placer.run."""
+    from autoplace_gb300.engine import Placer
+    from autoplace_gb300.flow import global_placement
+    g = gold("golden_place2.npz")
+    prob = _two_level_case(g)
+    prob.opts.cluster_ratio = 1.0
+    st = global_placement(prob, g["pos0"], field="fp32")
+    r = Placer(prob, field="fp32").run(g["pos0"])
+    assert "clusters" not in st and st["iters"] == r["iters"] and st["stop_reason"] == r["reason"]
+    assert np.array_equal(st["pos"].cpu().numpy(), r["pos"].cpu().numpy())

@@ -88,3 +88,13 @@ def test_net_order_keeps_nets_and_cell_sums():
     for c in range(5):
         f = first[cls == c]
         assert np.all(np.diff(f) >= 0)
+
+
+def test_field_mode_falls_back_to_fp32_on_small_grids():
+    """A tensor-core field needs multiples of 128 bins per side: smaller grids (clusters, small designs) run the
+    fp32 field (decided by gp103_plan_sizes, host only)."""
+    from autoplace_gb300.engine import field_mode
+    assert field_mode(native.FIELD_BF16X6, 32, 32) == native.FIELD_FP32
+    assert field_mode(native.FIELD_BF16X3, 64, 128) == native.FIELD_FP32
+    assert field_mode(native.FIELD_BF16X6, 256, 128) == native.FIELD_BF16X6
+    assert field_mode(native.FIELD_FP32, 256, 256) == native.FIELD_FP32

@@ -217,3 +217,21 @@ def test_coarse_problem_and_expand_match_reference(gold):
     csize = np.asarray(g["size"], np.float32)
     pos = O.expand(g["cpos"], cid, csize, size, torch.rand(n, 2, generator=gen).numpy(), num)
     assert np.array_equal(pos.view(np.uint32), g["pos"].view(np.uint32))
+
+
+def test_two_levels_match_reference(gold):
+    """The oracle's two-level run (clusters until the hand-over smoothing, expand, the density weight in tension
+    units, the cells resumed) and the reference's own (golden_place2.npz): the same clusters and cluster grid, the
+    same stop, the clusters' iterations within 3, the total within 5, HPWL within 0.5 %."""
+    pytest.importorskip("torch")
+    g = gold("golden_place2.npz")
+    nl = synth.make_netlist(int(g["cells"]), int(g["nets"]), window=int(g["window"]), macros=0, seed=int(g["seed"]))
+    prob = problem.Problem(nl, problem.options(target_density=1.0, num_bin=int(g["num_bin"]), force_num_bin=0,
+                                               cluster_ratio=float(g["cluster_ratio"]), inner_iter=3000,
+                                               seed=int(g["cluster_seed"])))
+    r = O.two_level(prob, g["pos0"])
+    assert r["clusters"] == int(g["clusters"]) and r["coarse_num_bin"] == int(g["coarse_num_bin"])
+    assert r["coarse_reason"] == "handover" and abs(r["coarse_iters"] - int(g["coarse_iters"])) <= 3
+    assert r["reason"] == str(g["reason"]) and abs(r["iters"] - int(g["iters"])) <= 5
+    h = O.hpwl_all(r["pos"], prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
+    assert abs(h - float(g["hpwl"])) <= 0.005 * float(g["hpwl"])
