@@ -68,6 +68,13 @@ def field_mode(mode, nbx, nby):
     return mode
 
 
+def _tensor(a, dt):
+    """A host array or a tensor (host or device, e.g. from Problem.on_device) as a tensor of type dt."""
+    if torch.is_tensor(a):
+        return a.to(dtype=dt)
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dt)
+
+
 def pinned_inputs(prob):
     """The problem arrays a Placer uploads, as pinned CPU tensors ({name: tensor}). A caller that keeps its inputs in
     pinned memory passes them as Placer(prob, host=...): the uploads are then asynchronous DMA copies."""
@@ -106,9 +113,8 @@ class Placer(object):
 
     def _setup(self, prob, host):
         dev = self.dev
-        up = lambda name, a, dt: torch.as_tensor(host[name] if name in host else np.ascontiguousarray(a),
-                                                 dtype=dt).to(dev, non_blocking=True)
-        t = lambda a, dt: self._hold(torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev, non_blocking=True))
+        up = lambda name, a, dt: _tensor(host[name] if name in host else a, dt).to(dev, non_blocking=True)
+        t = lambda a, dt: self._hold(_tensor(a, dt).to(dev, non_blocking=True))
         z = lambda shape, dt: self._hold(torch.zeros(shape, dtype=dt, device=dev))
         cs = prob.csr
         n, f, judge = prob.num_nodes, prob.force, prob.judge
@@ -252,7 +258,7 @@ class Placer(object):
         with their real sizes on the overflow grid). The whole netlist is uploaded on the first call."""
         p = self.p
         if not hasattr(self, "_ev"):
-            t = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.dev, non_blocking=True)
+            t = lambda a, dt: _tensor(a, dt).to(self.dev, non_blocking=True)
             gr = p.real_judge
             with torch.cuda.stream(self.stream):
                 self._ev = dict(cell=t(p.all_cell, torch.int32), off=t(p.all_off, torch.float32),
@@ -279,7 +285,7 @@ class Placer(object):
         density weight is given in (Objective.tension_unit, src/calculator.py:20-24) and the overflow of the same
         density pass (density.forward(pos)[1])."""
         out = self.eval(pos, self.tmp[0], weight=1.0, precond=-1.0, with_wl=False)
-        return float(self.p.pins.astype(np.float64).sum()) / float(out[4]), float(out[3]) * self.overflow_scale()
+        return float(self.p.total_pins) / float(out[4]), float(out[3]) * self.overflow_scale()
 
     def hpwl(self, pos):
         """HPWL of the optimised nets at pos (wirelength.forward(pos, wa_coeff)[2])."""

@@ -273,6 +273,32 @@ int gp103_coarse_pins(const int* pin_cell, const float* pin_off, const int* pin_
 int gp103_expand(const float* cpos, const int* cid, const float* csize, const float* size, const float* draws, int n,
                  float* pos, cudaStream_t stream);
 
+/* Problem build on the device: the arrays AutoPlace builds once per level before the first iteration.
+ *
+ * gp103_build_csr: the optimised pin set (Wirelength.__init__ net filter and Wirelength._pin_set,
+ * src/core/wa_wirelength_hpwl.py:26-46) from the netlist's pins sorted by net (pin_cell [num_pins] with num_mov for a
+ * fixed pin, pin_off [num_pins, 2], pin_net [num_pins] ascending, nets < num_nets): nets of 2 .. ignore_degree pins
+ * renumbered in order; net_start [num_nets + 1] (the first num_opt + 1 written), cell32 / off [num_pins] (the first
+ * num_opt_pins written), cell_start [num_mov + 1], cell_pin [num_pins] (a stable argsort of cell32), all_net_start
+ * [num_nets + 1] (every net's first pin, for the exact HPWL), cell_pins [num_mov] (pins per movable cell over every
+ * pin). counts (device int [4]) = (num_opt, num_opt_pins, error bits: 1 = pin_net unsorted or out of range, 2 = a
+ * cell out of [0, num_mov], pins on movable cells). Integer work and copies: the host build's arrays, bit for bit.
+ * scratch: gp103_build_csr_scratch(...) bytes. GP103_ERR_TOO_LARGE beyond 16,777,215 pins, nets or cells. */
+size_t gp103_build_csr_scratch(int num_pins, int num_nets, int num_mov);
+int gp103_build_csr(const int* pin_cell, const float* pin_off, const int* pin_net, int num_pins, int num_nets,
+                    int num_mov, int ignore_degree, void* scratch, size_t scratch_bytes, int* net_start, int* cell32,
+                    float* off, int* cell_start, int* cell_pin, int* all_net_start, int* cell_pins, int* counts,
+                    cudaStream_t stream);
+
+/* gp103_smooth_nodes: the n nodes (size [n, 2] float64) as one density grid sees them (ElectronicDensityLayer
+ * smoothing, src/core/electronic_density_layer.py:36-58): size_s = float32(max(size, (min_x, min_y))) with min =
+ * sqrt(2) x the bin, ratio = float32(real area / smoothed area) in float64, lo = size_s / 2 and hi = (width, height) -
+ * lo in float32 (lo, hi may be NULL); area = float32(real area) and pins = float32(cell_pins[i]) for the num_mov cells,
+ * 0 for the rest (each may be NULL). */
+int gp103_smooth_nodes(const double* size, int n, int num_mov, double min_x, double min_y, float width, float height,
+                       float* size_s, float* ratio, float* lo, float* hi, float* area, const int* cell_pins,
+                       float* pins, cudaStream_t stream);
+
 /* ------------------------------------------------------------------------------------------------ part 3
  * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
  * *out is written by the device (read it after synchronising the stream). */

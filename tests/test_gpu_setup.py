@@ -51,3 +51,76 @@ def test_device_net_order_empty():
     cs = problem.build_csr(np.zeros(0, np.int64), np.zeros((0, 2), np.float32), np.zeros(0, np.int64), 0, 10, 100)
     ns_d, _, _, _, split_d = device_order(cs, 10)
     assert ns_d.tolist() == [0] and split_d == [0, 0]
+
+
+def _same(a, b):
+    a = a.cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape and a.dtype.itemsize == b.dtype.itemsize
+    return np.array_equal(a.view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+
+
+def _check_device_problem(nl, opts):
+    hp = problem.Problem(nl, opts)
+    dp = problem.Problem(nl, opts, arrays=False).on_device()
+    hc, dc = hp.csr, dp.csr
+    assert dc.num_nets == hc.num_nets
+    for k in ("net_start", "cell32", "off", "cell_start", "cell_pin"):
+        assert _same(getattr(dc, k), getattr(hc, k)), k
+    for k in ("all_cell", "all_off", "all_net_start", "pins", "area"):
+        assert _same(getattr(dp, k), getattr(hp, k)), k
+    for g in ("force", "judge"):
+        if getattr(hp, g) is None:
+            assert getattr(dp, g) is None
+            continue
+        for k in ("size", "ratio", "pos_lo", "pos_hi"):
+            assert _same(getattr(getattr(dp, g), k), getattr(getattr(hp, g), k)), (g, k)
+    assert dp.total_pins == hp.total_pins
+    assert np.array_equal(dp.constants(), hp.constants())
+    return hp, dp
+
+
+@pytest.mark.parametrize("cells,seed,ignore", [(3000, 0, 100), (20000, 7, 100), (20000, 3, 6)])
+def test_device_problem_build_matches_host(cells, seed, ignore):
+    """The net filter, CSR, cell order, every net's start and the smoothed nodes built on the device
+    (gp103_build_csr, gp103_smooth_nodes) against the host build: bit for bit."""
+    nl = synth.make_netlist(cells, int(cells * 1.05), window=200, macros=3, cover=0.1, fixed_pin_share=0.02,
+                            seed=seed)
+    _check_device_problem(nl, problem.options(target_density=0.9, num_bin=64, force_num_bin=128,
+                                              ignore_net_degree=ignore))
+
+
+def test_device_problem_build_big_cells_and_placement():
+    """Cells of many pins (33 .. a few thousand: the block-sorted path) keep their pins in pin order; the Placer runs
+    the device-built problem to the same placement as the host-built one."""
+    from autoplace_gb300.engine import Placer
+    nl = synth.make_netlist(6000, 6300, window=150, macros=2, cover=0.1, fixed_pin_share=0.02, seed=5)
+    pc = np.array(nl.pin_cell)
+    movable = np.flatnonzero(pc < nl.num_mov)
+    pc[movable[::40]] = 7                           # one cell with ~500 pins
+    pc[movable[5::97]] = 11                         # another with ~200
+    pc[movable[3:200:5]] = 13                       # and one with 40
+    nl.pin_cell = pc
+    hp, dp = _check_device_problem(nl, problem.options(target_density=0.9, num_bin=64, force_num_bin=128))
+    assert np.diff(hp.csr.cell_start)[[7, 11, 13]].min() > 32
+    pos0 = synth.init_positions(nl, hp.num_nodes, seed=1)
+    rh = Placer(hp, field="fp32").run(pos0)
+    rd = Placer(dp, field="fp32").run(pos0)
+    assert rh["iters"] == rd["iters"] and rh["reason"] == rd["reason"]
+    assert np.array_equal(rh["pos"].cpu().numpy(), rd["pos"].cpu().numpy())
+
+
+def test_device_problem_build_rejects_bad_pins():
+    """An unsorted pin_net or a pin on a cell out of range: the device build raises (the kernels stay in bounds)."""
+    nl = synth.make_netlist(2000, 2100, window=100, macros=0, seed=2)
+    opts = problem.options(target_density=1.0, num_bin=32)
+    base = problem.Problem(nl, opts, arrays=False)
+    src = problem.netlist_arrays(base)
+    bad = dict(src, pin_net=src["pin_net"].copy())
+    bad["pin_net"][[10, 400]] = bad["pin_net"][[400, 10]]
+    with pytest.raises(ValueError, match="not sorted"):
+        base.on_device(host=bad)
+    bad = dict(src, pin_cell=src["pin_cell"].copy())
+    bad["pin_cell"][17] = nl.num_mov + 5
+    with pytest.raises(ValueError, match="cell out of range"):
+        base.on_device(host=bad)
