@@ -37,10 +37,10 @@ def limits(area, ratio):
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
-                  draws=None, stream=None):
+                  draws=None, stream=None, dev_pins=None):
     """pin_cell / pin_net [P] sorted by net (cell index len(area) = a fixed pin); area [n] int64. -> (cluster of
     every cell [n] int64, area of every cluster [K] int64), as numpy arrays. draws(round, num) -> float32 [num] can
-    stand in for the seeded generator (tests)."""
+    stand in for the seeded generator (tests). dev_pins: (pin_cell, pin_net) already on the device as int32."""
     area = np.ascontiguousarray(area, np.int64)
     n = len(area)
     if n == 0:
@@ -54,8 +54,11 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     num_nets = int(pin_net.max()) + 1 if len(pin_net) else 0
     E = max(pair_bound(pin_net, max_degree), 1)
     with torch.cuda.stream(stream):
-        pc = torch.as_tensor(np.asarray(pin_cell, np.int32)).to(dev)
-        pn = torch.as_tensor(pin_net.astype(np.int32)).to(dev)
+        if dev_pins is not None:
+            pc, pn = dev_pins
+        else:
+            pc = torch.as_tensor(np.asarray(pin_cell, np.int32)).to(dev)
+            pn = torch.as_tensor(pin_net.astype(np.int32)).to(dev)
         scratch = torch.empty(int(native.lib().gp103_cluster_scratch(n, num_nets, E)), dtype=torch.uint8, device=dev)
         rows = [torch.zeros(n + 1, dtype=torch.int32, device=dev) for _ in range(2)]
         col = [torch.zeros(E, dtype=torch.int32, device=dev) for _ in range(2)]
@@ -92,13 +95,15 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     return cid.cpu().numpy().astype(np.int64), areas[a][:num].cpu().numpy()
 
 
-def coarse_problem(prob, device="cuda", stream=None):
+def coarse_problem(prob, device="cuda", stream=None, build="device"):
     """The problem of the clusters (coarse_problem, src/cluster.py:88-130), from a cell-level Problem:
       - the cells clustered (cluster_cells, areas in 1/1024 of a site area, rounded from the float32 area);
       - a merged cluster is a square of its summed area with its pins at the centre, one per net; a cluster of one
         cell keeps its shape and pins (the pin selection runs on the device: gp103_coarse_pins);
       - the same fillers, target and options; one grid, between the overflow grid and the cells' force grid, as
         the cells' grid follows the cells.
+    build: "device" = the clusters' per-pin and per-node arrays built on the device from the selected pins
+    (Problem.on_device: torch tensors), "host" = downloaded and built in numpy (the same arrays, bit for bit).
     -> SimpleNamespace(cid [n], num, size [num, 2] float32, problem: the clusters' Problem)."""
     from . import problem as P
     dev = torch.device(device)
@@ -106,9 +111,15 @@ def coarse_problem(prob, device="cuda", stream=None):
     s = stream.cuda_stream
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     nl, o, n = prob.nl, prob.opts, prob.num_mov
+    P_ = len(nl.pin_cell)
+    with torch.cuda.stream(stream):
+        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev, non_blocking=True)
+        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
+        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
     size = np.asarray(prob.node_size[:n], np.float32)
     area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
-    cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream)
+    cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
+                               dev_pins=(pc, pn))
     num = len(carea)
     csize = np.repeat(np.sqrt(carea.astype(np.float64) / 1024).astype(np.float32)[:, None], 2, 1)
     count = np.bincount(cid, minlength=num)
@@ -117,11 +128,7 @@ def coarse_problem(prob, device="cuda", stream=None):
     member[cid] = np.arange(n)                         # a one-cell cluster's cell
     csize[single] = size[member[single]]
     # pins: on the device
-    P_ = len(nl.pin_cell)
     with torch.cuda.stream(stream):
-        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev)
-        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev)
-        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev)
         cd = torch.as_tensor(cid.astype(np.int32)).to(dev)
         sg = torch.as_tensor(single.astype(np.uint8)).to(dev)
         scratch = torch.empty(int(native.lib().gp103_coarse_pins_scratch(P_)), dtype=torch.uint8, device=dev)
@@ -133,15 +140,28 @@ def coarse_problem(prob, device="cuda", stream=None):
                 p(oc), p(oo), p(on), p(cnt), s)
     stream.synchronize()
     k = int(cnt.item())
-    c_cell, c_off, c_net = oc[:k].cpu().numpy(), oo[:k].cpu().numpy(), on[:k].cpu().numpy()
     # the grid: as the cells' force grid follows the cells (at most the cells' grid)
-    fine_ff = nl.fixed_fraction(prob.force_bin, prob.force_bin)
-    judge_bin = prob.num_bin
-    nb = min(prob.force_bin, P.force_num_bin(num, 1.0 - float(fine_ff.mean()), judge_bin))
-    fixed_fraction = fine_ff if nb == prob.force_bin else nl.fixed_fraction(nb, nb)
+    fine_ff = getattr(prob, "fixed_fraction", None)
+    if fine_ff is None:
+        fine_ff = nl.fixed_fraction(prob.force_bin, prob.force_bin)
+    nb = min(prob.force_bin, P.force_num_bin(num, 1.0 - float(fine_ff.mean()), prob.num_bin))
+    if nb == prob.force_bin:
+        fixed_fraction = fine_ff
+    elif nb == prob.num_bin and getattr(prob, "judge_fraction", None) is not None:
+        fixed_fraction = prob.judge_fraction
+    else:
+        fixed_fraction = nl.fixed_fraction(nb, nb)
     copts = SimpleNamespace(**vars(o))
     copts.settle_iter, copts.min_iter = 0, 0
-    cprob = P.Problem.clusters(prob, csize, c_cell, c_off, c_net, nb, fixed_fraction, copts)
+    if build == "host":
+        c_cell, c_off, c_net = oc[:k].cpu().numpy(), oo[:k].cpu().numpy(), on[:k].cpu().numpy()
+        cprob = P.Problem.clusters(prob, csize, c_cell, c_off, c_net, nb, fixed_fraction, copts)
+    else:
+        pins = dict(pin_cell=oc[:k], pin_off=oo[:k], pin_net=on[:k])
+        cprob = P.Problem.clusters(prob, csize, pins["pin_cell"], pins["pin_off"], pins["pin_net"], nb,
+                                   fixed_fraction, copts, arrays=False)
+        pins["node_size"] = np.ascontiguousarray(cprob.node_size, np.float64)
+        cprob = cprob.on_device(dev, stream, host=pins)
     return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob)
 
 

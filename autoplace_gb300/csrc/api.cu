@@ -186,7 +186,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
         OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
-        OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid)};
+        OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid), OFF(net_two), OFF(net_three)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -212,6 +212,8 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
     REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
     REQUIRE(p->net_mid == 0 || (p->net_mid >= p->net_split && p->net_mid <= p->num_nets));
+    REQUIRE(p->net_three == 0 || (p->net_two >= 0 && p->net_two <= p->net_three && p->net_three <= p->net_split &&
+                                  2LL * p->net_two + 3LL * (p->net_three - p->net_two) <= (long long)p->num_pins));
     REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
     REQUIRE((p->order == nullptr) == (p->order_counts == nullptr) && (p->order == nullptr) == (p->order_cursor == nullptr));
     if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
@@ -352,6 +354,8 @@ static WaJob wa_job(const gp103_plan* p) {
     w.num_mov = p->num_mov;
     w.split = p->net_split;
     w.mid = p->net_mid > 0 ? p->net_mid : p->net_split;
+    w.two = p->net_three > 0 ? p->net_two : 0;
+    w.three = p->net_three;
     w.slot = p->pin_slot;
     w.gamma = p->kp;
     w.pin_grad = (float2*)p->pin_grad;

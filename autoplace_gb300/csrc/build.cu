@@ -191,11 +191,13 @@ __global__ void __launch_bounds__(256) pin_slot_kernel(const int* cell_pin, cons
         slot[newpos[cell_pin[k]]] = k;
 }
 
-// split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 32 pins (class 4)
+// split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 32 pins (class 4),
+// split[2] = nets of 2 pins (class 0), split[3] = nets of up to 3 pins (class 1)
 __global__ void net_split_kernel(const int* start, int stride, int num_nets, int keys, int* split) {
     pdl_wait();
-    for (int c = 0; c < 2; c++) {
-        const int k = (3 + c) * stride;
+    const int cls[4] = {3, 4, 1, 2};
+    for (int c = 0; c < 4; c++) {
+        const int k = cls[c] * stride;
         split[c] = k < keys ? start[k] : num_nets;
     }
 }

@@ -200,7 +200,40 @@ __device__ __forceinline__ void net_two(const WaJob& j, const float2* pos, float
     hp = hsum;
 }
 
-// Short nets, one per lane: 32 consecutive nets [0, split) per warp item. LONG: nets longer than WA_REG met there
+// A 2-pin net whose pins are s, s + 1 with s even (the 2-pin class of the ordered layout): cells, offsets and slots of
+// both pins in one 8-, one 16- and one 8-byte load, all issued before the position gathers.
+__device__ __forceinline__ void net_two_pair(const WaJob& j, const float2* pos, float ig, int s, float& wa,
+                                             float& hp) {
+    const int2 c = __ldg((const int2*)(j.pin_cell + s));
+    const float4 o = __ldg((const float4*)(j.pin_off + s));
+    const int2 q = j.slot ? __ldg((const int2*)(j.slot + s)) : make_int2(s, s + 1);
+    const float2 pa = c.x < j.num_mov ? pos[c.x] : make_float2(0.f, 0.f);
+    const float2 pb = c.y < j.num_mov ? pos[c.y] : make_float2(0.f, 0.f);
+    const float2 a = make_float2(pa.x + o.x, pa.y + o.y), b = make_float2(pb.x + o.z, pb.y + o.w);
+    float g[2][2], wsum = 0.f, hsum = 0.f;
+#pragma unroll
+    for (int ax = 0; ax < 2; ax++) {
+        const float xa = ax ? a.y : a.x, xb = ax ? b.y : b.x;
+        const float hi = fmaxf(xa, xb), lo = fminf(xa, xb);
+        const float e = __expf((lo - hi) * ig);
+        const float epa = xa == hi ? 1.f : e, epb = xb == hi ? 1.f : e;
+        const float ena = xa == lo ? 1.f : e, enb = xb == lo ? 1.f : e;
+        const float sp = epa + epb, sn = ena + enb;
+        const float ip = __frcp_rn(sp), in = __frcp_rn(sn);
+        const float xp = (xa * epa + xb * epb) * ip, xn = (xa * ena + xb * enb) * in;
+        g[0][ax] = epa * (1.f + (xa - xp) * ig) * ip - ena * (1.f - (xa - xn) * ig) * in;
+        g[1][ax] = epb * (1.f + (xb - xp) * ig) * ip - enb * (1.f - (xb - xn) * ig) * in;
+        wsum += xp - xn;
+        hsum += hi - lo;
+    }
+    put(j, q.x, g[0][0], g[0][1]);
+    put(j, q.y, g[1][0], g[1][1]);
+    wa = wsum;
+    hp = hsum;
+}
+
+// Short nets, one per lane: 32 consecutive nets [0, split) per warp item. With the class layout (three > 0) the
+// nets below `three` need no net_start: net i < two starts at pin 2 i, net i < three at 2 two + 3 (i - two). LONG: nets longer than WA_REG met there
 // (any order) are done by the whole warp in turn; without it every net below split is short (the ordered layout).
 // Blocks write float64 partials at bid0 + blockIdx.x of nblk.
 template <bool LONG>
@@ -217,12 +250,21 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
         const bool valid = i < j.split;
         int s = 0, d = 0;
         if (valid) {
-            s = j.net_start[i];
-            d = j.net_start[i + 1] - s;
+            if (i < j.two) {
+                s = 2 * i;
+                d = 2;
+            } else if (i < j.three) {
+                s = 2 * j.two + 3 * (i - j.two);
+                d = 3;
+            } else {
+                s = j.net_start[i];
+                d = j.net_start[i + 1] - s;
+            }
         }
         if (valid && d <= WA_REG) {
             float wa, hp;
-            if (d == 2) net_two(j, pos, ig, s, wa, hp);
+            if (i < j.two) net_two_pair(j, pos, ig, s, wa, hp);
+            else if (d == 2) net_two(j, pos, ig, s, wa, hp);
             else if (d == 3) net_thread<3>(j, pos, ig, s, d, wa, hp);
             else net_thread<WA_REG>(j, pos, ig, s, d, wa, hp);
             if (j.out) j.out[i] = make_float2(wa, hp);

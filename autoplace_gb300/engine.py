@@ -37,12 +37,12 @@ def net_order(net_start, cell32, cell_pin):
     nearby cells); the long nets after them (one warp each). Pins move with their nets.
     -> (pin permutation: new position -> old pin, new net_start, slot: new pin position -> its position in cell
     order (cell_pin order, which every cell sums in), index of the first net of more than SHORT_NET pins, index of
-    the first net of more than MID_NET pins)."""
+    the first net of more than MID_NET pins, number of 2-pin nets, number of nets of up to 3 pins)."""
     ns = np.asarray(net_start, np.int64)
     deg = np.diff(ns)
     n = len(deg)
     if n == 0:
-        return np.zeros(0, np.int64), np.zeros(1, np.int32), np.zeros(0, np.int32), 0, 0
+        return np.zeros(0, np.int64), np.zeros(1, np.int32), np.zeros(0, np.int32), 0, 0, 0, 0
     first = np.minimum.reduceat(np.asarray(cell32, np.int64), ns[:-1]) if len(cell32) else np.zeros(n, np.int64)
     cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, np.where(deg <= MID_NET, 3, 4))))
     order = np.lexsort((first, cls))
@@ -53,7 +53,8 @@ def net_order(net_start, cell32, cell_pin):
     newpos[perm] = np.arange(len(perm))
     slot = np.empty(len(perm), np.int64)
     slot[newpos[np.asarray(cell_pin, np.int64)]] = np.arange(len(perm))
-    return perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum()), int((cls < 4).sum())
+    return (perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum()), int((cls < 4).sum()),
+            int((cls < 1).sum()), int((cls < 2).sum()))
 
 
 def field_mode(mode, nbx, nby):
@@ -131,7 +132,7 @@ class Placer(object):
         self.cell_start = self._hold(up("cell_start", cs.cell_start, torch.int32))
         self.pin_cell, self.pin_off = z((max(P, 1),), torch.int32), z((max(P, 1), 2), torch.float32)
         self.net_start, self.pin_slot = z((N + 1,), torch.int32), z((max(P, 1),), torch.int32)
-        split = torch.zeros(2, dtype=torch.int32, device=dev)
+        split = torch.zeros(4, dtype=torch.int32, device=dev)
         scratch = torch.empty(int(native.lib().gp103_net_order_scratch(N, P, prob.num_mov)), dtype=torch.uint8,
                               device=dev)
         native.call("gp103_net_order", self._p(ns_in), self._p(cell_in), self._p(off_in), self._p(cp_in), N, P,
@@ -139,7 +140,7 @@ class Placer(object):
                     self._p(self.pin_off), self._p(self.pin_slot), self._p(split), self.stream.cuda_stream)
         pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
         pl.cell_start, pl.pin_slot = self._p(self.cell_start), self._p(self.pin_slot)
-        pl.net_split, pl.net_mid = (int(x) for x in split.cpu().tolist())
+        pl.net_split, pl.net_mid, pl.net_two, pl.net_three = (int(x) for x in split.cpu().tolist())
         del ns_in, cell_in, off_in, cp_in, scratch
         self.size = self._hold(up("size", f.size, torch.float32))
         self.ratio = self._hold(up("ratio", f.ratio, torch.float32))

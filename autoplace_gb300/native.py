@@ -36,7 +36,7 @@ class Plan(ctypes.Structure):
         ("pin_grad", _vp), ("map", _vp), ("jmap", _vp), ("red", _vp), ("counters", _vp),
         ("pin_slot", _vp), ("net_split", _i),
         ("order", _vp), ("order_counts", _vp), ("order_cursor", _vp),
-        ("net_mid", _i),
+        ("net_mid", _i), ("net_two", _i), ("net_three", _i),
     ]
 
 

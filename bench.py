@@ -9,7 +9,8 @@ first density weight, density phase until overflow < 0.07 + the settle iteration
 working set (pins, nodes, maps, field planes) is larger than the 129 MB L2, so no flush is needed between steps.
 
 Reported on one JSON line (rank 0): value = seconds per placement (lower is better), e2e = the same through the
-public API from host arrays (upload, run, download of the placement), the roofline of the dominant kernel (CUDA
+public API from the netlist's host arrays (upload, the problem's arrays built on the device, run, download of the
+placement), the roofline of the dominant kernel (CUDA
 events on its stream), a CPU baseline (the oracle's restatement of the reference's CPU iteration timed on a bounded
 sample of iterations of the same netlist, scaled by the iterations the GPU run needed), SM clocks during the timed
 region, and the number of libgp103 kernels launched.
@@ -328,24 +329,33 @@ def run_gb300(args):
     iters = last["iters"]
     hpwl_exact, overflow_exact = placer.evaluate(last["pos"])
 
-    # e2e: from pinned host arrays through the public API (upload, device set-up, run, download of the placement)
-    from autoplace_gb300.engine import pinned_inputs
-    host = pinned_inputs(prob)
-    host_pos = torch.from_numpy(np.ascontiguousarray(pos0, dtype=np.float32)).pin_memory()
+    # e2e: from the netlist's pinned host arrays through the public API: upload, the problem's arrays built on the
+    # device (net CSR, cell order, smoothed nodes), the device set-up of the Placer, the run, the download of the
+    # placement. The host part of the problem (grids, fixed fractions, fillers: the reader's and initializer's
+    # work) is made once, before.
+    from autoplace_gb300.problem import Problem, netlist_arrays
+    base = Problem(prob.nl, prob.opts, arrays=False)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    host = {k: pin(v) for k, v in netlist_arrays(base).items()}
+    maps = {"fixed": pin(base.force.fixed_map)}
+    if base.judge is not None:
+        maps["jfixed"] = pin(base.judge.fixed_map)
+    host_pos = pin(np.asarray(pos0, dtype=np.float32))
     out = torch.empty(host_pos.shape, dtype=torch.float32).pin_memory()
-    h2d = sum(x.numel() * x.element_size() for x in host.values()) + host_pos.numel() * 4 + \
-        len(prob.constants()) * 8
+    h2d = sum(x.numel() * x.element_size() for x in list(host.values()) + list(maps.values())) + \
+        host_pos.numel() * 4 + len(prob.constants()) * 8
     d2h = out.numel() * 4
     e2e_s = []
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.time()
-        pl2 = Placer(prob, field=args.field, stream=placer.stream, host=host)
+        dprob = base.on_device(stream=placer.stream, host=host)
+        pl2 = Placer(dprob, field=args.field, stream=placer.stream, host=maps)
         rr = pl2.run(host_pos)
         out.copy_(rr["pos"])
         torch.cuda.synchronize()
         e2e_s.append(time.time() - t)
-        del pl2
+        del pl2, dprob
     e2e = reduce_max(statistics.median(e2e_s), world)
 
     prof, _ = profile_pass(placer)

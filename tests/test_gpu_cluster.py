@@ -77,7 +77,7 @@ def test_coarse_problem_and_expand_match_reference(gold):
                            force_num_bin=int(g["force_num_bin"]), cluster_ratio=float(g["cluster_ratio"]),
                            seed=int(g["cluster_seed"]))
     prob = problem.Problem(nl, opts)
-    coarse = cluster.coarse_problem(prob)
+    coarse = cluster.coarse_problem(prob, build="host")
     cp = coarse.problem
     assert np.array_equal(coarse.cid, g["cid"]) and coarse.num == int(g["num"])
     assert np.array_equal(coarse.size.view(np.uint32), np.asarray(g["size"], np.float32).view(np.uint32))
@@ -91,3 +91,28 @@ def test_coarse_problem_and_expand_match_reference(gold):
     assert cp.total_pins == float(g["total_pins"]) and abs(cp.total_area - float(g["total_area"])) <= 1e-9 * cp.total_area
     pos = cluster.expand(g["cpos"], coarse, prob, int(g["cluster_seed"])).cpu().numpy()
     assert np.array_equal(pos.view(np.uint32), g["pos"].view(np.uint32))
+
+
+def test_coarse_problem_device_build_matches_host(gold):
+    """The clusters' problem built on the device from the selected pins (no download) and the host build: the same
+    arrays, bit for bit."""
+    from autoplace_gb300 import problem
+    g = gold("golden_coarse.npz")
+    nl = synth.make_netlist(int(g["cells"]), int(g["nets"]), window=int(g["window"]), macros=int(g["macros"]),
+                            cover=float(g["cover"]), fixed_pin_share=float(g["fixed_pin_share"]), seed=int(g["seed"]))
+    opts = problem.options(target_density=float(g["target_density"]), num_bin=int(g["num_bin"]),
+                           force_num_bin=int(g["force_num_bin"]), cluster_ratio=float(g["cluster_ratio"]),
+                           seed=int(g["cluster_seed"]))
+    prob = problem.Problem(nl, opts)
+    h = cluster.coarse_problem(prob, build="host").problem
+    d = cluster.coarse_problem(prob, build="device").problem
+    same = lambda a, b: np.array_equal(np.ascontiguousarray(a.cpu().numpy() if hasattr(a, "cpu") else a).view(np.uint8),
+                                       np.ascontiguousarray(b).view(np.uint8))
+    assert d.csr.num_nets == h.csr.num_nets and d.total_pins == h.total_pins
+    for k in ("net_start", "cell32", "off", "cell_start", "cell_pin"):
+        assert same(getattr(d.csr, k), getattr(h.csr, k)), k
+    for k in ("all_cell", "all_off", "all_net_start", "pins", "area"):
+        assert same(getattr(d, k), getattr(h, k)), k
+    for k in ("size", "ratio", "pos_lo", "pos_hi"):
+        assert same(getattr(d.force, k), getattr(h.force, k)), k
+    assert np.array_equal(d.constants(), h.constants())

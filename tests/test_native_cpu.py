@@ -64,10 +64,12 @@ def test_argument_errors_without_gpu():
 def test_net_order_keeps_nets_and_cell_sums():
     nl = synth.make_netlist(3000, 3100, window=60, macros=3, cover=0.1, fixed_pin_share=0.05, seed=4)
     cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
-    perm, ns, slot, split, mid = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    perm, ns, slot, split, mid, two, three = net_order(cs.net_start, cs.cell32, cs.cell_pin)
     deg = np.diff(ns)
     assert np.all(deg[:split] <= SHORT_NET) and np.all(deg[split:] > SHORT_NET)
     assert np.all(deg[split:mid] <= MID_NET) and np.all(deg[mid:] > MID_NET)
+    assert np.all(deg[:two] == 2) and np.all(deg[two:three] == 3) and np.all(deg[three:] > 3)
+    assert two > 0 and three > two
     cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, np.where(deg <= MID_NET, 3, 4))))
     assert np.all(np.diff(cls) >= 0)                       # classes in order
     assert sorted(perm.tolist()) == list(range(len(perm)))  # a permutation of the pins
