@@ -6,6 +6,7 @@
 // This file is built with -ftz=true, as the reference's kernels are (--use_fast_math), so that even denormal
 // intermediates round the same way.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "gp103.cuh"
 #include "kernels.cuh"
@@ -361,7 +362,25 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
             r[2] = __fadd_rn(mov[2], unfixed32(m1b.x));
             r[3] = __fadd_rn(mov[3], unfixed32(m1b.y));
             if (j.dens) *(float4*)(j.dens + b) = make_float4(r[0], r[1], r[2], r[3]);
-            if (j.t0) {
+            if (j.exps) {
+                // a 64-bin chunk of a row is 16 consecutive quads: half a warp (the loop keeps whole warps, since
+                // quads is a multiple of 32 on the tensor-core grids); its scale from its largest magnitude
+                float mx = fmaxf(fmaxf(fabsf(r[0]), fabsf(r[1])), fmaxf(fabsf(r[2]), fabsf(r[3])));
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                const int e = f16_chunk_exp(mx);
+                const float sc = __int_as_float((127 + e) << 23);
+                __align__(8) __half h[2][4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float x = r[k] * sc;
+                    h[0][k] = __float2half_rn(x);
+                    h[1][k] = __float2half_rn(__fsub_rn(x, __half2float(h[0][k])));
+                }
+                *(uint2*)(j.t0 + b) = *(const uint2*)h[0];
+                *(uint2*)(j.t1 + b) = *(const uint2*)h[1];
+                if ((threadIdx.x & 15) == 0) j.exps[(size_t)((b % j.nby) >> 6) * j.nbx + b / j.nby] = (signed char)e;
+            } else if (j.t0) {
                 __align__(8) __nv_bfloat16 t[3][4];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {

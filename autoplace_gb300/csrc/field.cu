@@ -21,6 +21,7 @@
 //   4b Ey[m][n]  = Cx^T . Q                                       A = CxT [nbx][nbx], B = Qt
 // This file has the constants and the float32 CUDA-core GEMM (any grid); field_tc.cu has the tensor-core form.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <math.h>
 
 #include "field.cuh"
@@ -36,9 +37,10 @@ __device__ __forceinline__ double trig(int kind, int p, int u, int n) {
     return kind == 0 ? cospi(t) : sinpi(t);
 }
 
-// what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]
+// what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]; f16: two float16 terms of
+// the value times 2^F16_CONST instead of three bf16 terms
 __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t0, __nv_bfloat16* t1,
-                                   __nv_bfloat16* t2, size_t plane) {
+                                   __nv_bfloat16* t2, size_t plane, int f16) {
     pdl_wait();
     const size_t total = (size_t)n * n;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -46,7 +48,13 @@ __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t
         const int kind = what & 1;
         const double v = what < 2 ? trig(kind, r, col, n) : trig(kind, col, r, n);
         if (f32) f32[e] = (float)v;
-        if (t0) {     // three bf16 terms of the float64 value
+        if (t0 && f16) {
+            const double w = ldexp(v, F16_CONST);
+            const __half a = __double2half(w);
+            const __half b = __double2half(w - (double)__half2float(a));
+            ((__half*)t0)[e] = a;
+            ((__half*)t1)[e] = b;
+        } else if (t0) {     // three bf16 terms of the float64 value
             const __nv_bfloat16 a = __double2bfloat16(v);
             const double r1 = v - (double)__bfloat162float(a);
             const __nv_bfloat16 b = __double2bfloat16(r1);
@@ -103,6 +111,8 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
     L.w_a = take(xy * es); L.w_tt = take(xy * es); L.w_kx = take(xy * es); L.w_ky = take(xy * es);
     L.w_pt = take(xy * es); L.w_qt = take(xy * es);
     L.w_err = take(1024);                                   // error flag of the tensor-core waits (int, zeroed)
+    const size_t ex = mode == GP103_FIELD_F16X3 ? xy / 64 : 0;   // one byte per row and 64-wide chunk
+    L.e_a = take(ex); L.e_tt = take(ex); L.e_kx = take(ex); L.e_ky = take(ex); L.e_pt = take(ex); L.e_qt = take(ex);
     L.work_bytes = o;
     return L;
 }
@@ -118,7 +128,8 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
         float* f = fp32 ? (float*)(c + m.off) : nullptr;
         __nv_bfloat16* t0 = fp32 ? nullptr : (__nv_bfloat16*)(c + m.off);
         if (launch_k(trig_matrix_kernel, dim3(grid_for(plane, 256, 8)), dim3(256), 0, s, m.what, m.n, f, t0, t0 ? t0 + plane : nullptr,
-                                                                      t0 ? t0 + 2 * plane : nullptr, plane) != cudaSuccess) return GP103_ERR_CUDA;
+                     t0 ? t0 + 2 * plane : nullptr, plane, (int)(L.mode == GP103_FIELD_F16X3)) != cudaSuccess)
+            return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
     if (launch_k(weight_kernel, dim3(grid_for((size_t)L.nbx * L.nby, 256, 8)), dim3(256), 0, s, L.nbx, L.nby, L.bx, L.by,

@@ -6,16 +6,23 @@
 namespace gp103 {
 
 // Byte offsets inside the plan's field_const / field_work buffers. Every operand is either one float32 plane
-// (GP103_FIELD_FP32) or three bf16 planes back to back (tensor-core modes; the bf16x3 mode reads two of them).
+// (GP103_FIELD_FP32) or up to three 16-bit planes back to back (tensor-core modes: bf16x6 three bf16 terms, bf16x3
+// two of them, f16x3 two float16 terms). In f16x3 every data operand also has a power-of-two scale per row and
+// 64-wide chunk of K: x_e[kb][n] = e, the terms hold x * 2^e (the constant matrices are scaled by 2^F16_CONST).
 struct FieldLayout {
     int nbx, nby, mode;
     double bx, by;
     size_t c_cx, c_cy, c_cyt, c_sxt, c_syt, c_cxt, c_wx, c_wy, c_wrow, c_wcol, const_bytes;
-    size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err, work_bytes;
+    size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err;
+    size_t e_a, e_tt, e_kx, e_ky, e_pt, e_qt, work_bytes;     // f16x3 chunk exponents (signed char)
 };
 
+constexpr int F16_CONST = 14;     // f16x3: the cosine / sine matrices (|c| <= 1) are stored times 2^14
+constexpr int F16_TOP = 14;       // f16x3: a chunk of data is scaled so that its largest magnitude is in [2^14, 2^15)
+constexpr int F16_EMAX = 100;     // f16x3: chunk exponents are clamped to [-100, 100] (all factors stay normal)
+
 // PLAIN: float32 [M][N]; TRANS: float32 [N][M] (CUDA-core GEMM); WEIGHT2: the two weighted products of the field;
-// SPLIT: the three bf16 terms of the product, [3][M][N] (tensor-core GEMM)
+// SPLIT: the 16-bit terms of the product, [terms][M][N] (tensor-core GEMM)
 enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3 };
 
 struct SGemm {

@@ -12,6 +12,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "field.cuh"
 #include "gp103.cuh"
@@ -34,6 +35,11 @@ struct TcProblem {
     float* out_f32;              // EPI_PLAIN: [M][N]
     const float4* wrow;          // EPI_WEIGHT2: per row p (kx^2, s kx / bin_x, w_p, 0)
     const float4* wcol;          //              per column q (ky^2, s ky / bin_x, w_q, 0)
+    // f16x3: exponents of the B operand's chunks, [K / 64][N] (B row n, k-block kb: its terms hold b * 2^e), and of
+    // the outputs' chunks, [N / 64][M] (written by the epilogue: the next GEMM reads the output as its B operand)
+    const signed char* b_exp;
+    signed char* o_exp;
+    signed char* o2_exp;
 };
 
 // A stage holds the k-block (64 of K) of every term of A and of B that the products read: na A tiles, then nb B
@@ -127,17 +133,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor: D float32, A and B bf16, both K-major, M = 128, N = BN.
-template <int BN>
+// Instruction descriptor: D float32, A and B both bf16 (F16 = false) or both float16, both K-major, M = 128, N.
+template <int N, bool F16>
 __device__ __forceinline__ constexpr uint32_t idesc() {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+    return (1u << 4) | (F16 ? 0u : (1u << 7) | (1u << 10)) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(TC_BM >> 4) << 24);
 }
 
-template <int N>
+template <int N, bool F16>
 __device__ __forceinline__ void mma_n(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N>()), "r"(accumulate));
+        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N, F16>()), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -168,6 +175,12 @@ __device__ __forceinline__ float recip(float t) {
     return fmaf(r, fmaf(-t, r, 1.f), r);
 }
 
+// f16x3: the two float16 terms of x (already scaled into the chunk's range)
+__device__ __forceinline__ void split2h(float x, __half& a, __half& b) {
+    a = __float2half_rn(x);
+    b = __float2half_rn(__fsub_rn(x, __half2float(a)));
+}
+
 __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16& b, __nv_bfloat16& c) {
     a = __float2bfloat16_rn(v);
     const float r1 = __fsub_rn(v, __bfloat162float(a));
@@ -184,7 +197,7 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& a, __nv_bfloat16&
 // then stays at float32 level (~2e-7) at every grid size.
 constexpr int TC_THREADS = 192;
 
-template <int BN, int EPI, int X6>
+template <int BN, int EPI, int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap a0, const __grid_constant__ CUtensorMap b0,
                    const __grid_constant__ CUtensorMap a1, const __grid_constant__ CUtensorMap b1,
@@ -192,6 +205,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                    const __grid_constant__ CUtensorMap o1a, const __grid_constant__ CUtensorMap o1b, TcArgs args) {
     // The set-up (barriers, tensor memory, tensor-map prefetch) reads nothing the previous kernel writes: it runs
     // before griddepcontrol.wait, overlapping the previous kernel's tail.
+    constexpr int X6 = MODE == 1 ? 1 : 0;                        // bf16x6 (MODE 0: bf16x3, MODE 2: f16x3)
+    constexpr bool F16 = MODE == 2;
     constexpr int B_TILE = BN * TC_BK * 2;
     constexpr int NA = X6 ? 3 : 2, NB = NA, NPROD = X6 ? 6 : 3;
     // BN = 64: the products are grouped by B term into NBLK column blocks of the accumulator (block j = the
@@ -205,6 +220,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // barriers: full[S], empty[S], acc_full[2], acc_empty[2]
     uint64_t* bars = (uint64_t*)(smem + TC_STAGE_SPACE);
     uint32_t* tmem_slot = (uint32_t*)(bars + 2 * TC_MAX_STAGES + 4);
+    // f16x3: the factors of B's chunks, [K / 64][BN], each the upper half of the float32 2^(-F16_CONST - e) that takes
+    // an accumulated product of a constant (times 2^F16_CONST) and a chunk scaled by 2^e back to its value (exact);
+    // the table sits behind the stages (4 x 48 KB or 3 x 64 KB leave 24 KB of the stage space; checked on the host)
+    constexpr int STAGE_BYTES = NA * TC_A_TILE + NB * B_TILE;
+    constexpr int STAGES = TC_STAGE_SPACE / STAGE_BYTES > TC_MAX_STAGES ? TC_MAX_STAGES : TC_STAGE_SPACE / STAGE_BYTES;
+    uint16_t* ftab = (uint16_t*)(smem + STAGES * STAGE_BYTES);   // (the host launches with args.stages = STAGES)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int z = blockIdx.z;
     const TcProblem& P = args.p[z];
@@ -283,29 +304,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     // product first, and each block starts fresh (accumulate = 0) with its first product.
                     if constexpr (X6) {
 #pragma unroll
-                        for (int kk = 0; kk < 4; kk++) mma_n<64>(acc, A(2, kk), Bd(0, kk), kk > 0);     // a2 b0
-                        mma_n<64>(acc + 64, A(1, 0), Bd(1, 0), 0);                                      // a1 b1
-                        mma_n<64>(acc, A(1, 0), Bd(0, 0), 1);                                           // a1 b0
+                        for (int kk = 0; kk < 4; kk++) mma_n<64, F16>(acc, A(2, kk), Bd(0, kk), kk > 0);     // a2 b0
+                        mma_n<64, F16>(acc + 64, A(1, 0), Bd(1, 0), 0);                                      // a1 b1
+                        mma_n<64, F16>(acc, A(1, 0), Bd(0, 0), 1);                                           // a1 b0
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<128>(acc, A(1, kk), Bd(0, kk), 1);         // a1 [b0 b1]
-                        mma_n<64>(acc + 128, A(0, 0), Bd(2, 0), 0);                                     // a0 b2
-                        mma_n<128>(acc, A(0, 0), Bd(0, 0), 1);                                          // a0 [b0 b1]
+                        for (int kk = 1; kk < 4; kk++) mma_n<128, F16>(acc, A(1, kk), Bd(0, kk), 1);         // a1 [b0 b1]
+                        mma_n<64, F16>(acc + 128, A(0, 0), Bd(2, 0), 0);                                     // a0 b2
+                        mma_n<128, F16>(acc, A(0, 0), Bd(0, 0), 1);                                          // a0 [b0 b1]
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<192>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1 b2]
+                        for (int kk = 1; kk < 4; kk++) mma_n<192, F16>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1 b2]
                     } else {
 #pragma unroll
-                        for (int kk = 0; kk < 4; kk++) mma_n<64>(acc, A(1, kk), Bd(0, kk), kk > 0);     // a1 b0
-                        mma_n<64>(acc + 64, A(0, 0), Bd(1, 0), 0);                                      // a0 b1
-                        mma_n<64>(acc, A(0, 0), Bd(0, 0), 1);                                           // a0 b0
+                        for (int kk = 0; kk < 4; kk++) mma_n<64, F16>(acc, A(1, kk), Bd(0, kk), kk > 0);     // a1 b0
+                        mma_n<64, F16>(acc + 64, A(0, 0), Bd(1, 0), 0);                                      // a0 b1
+                        mma_n<64, F16>(acc, A(0, 0), Bd(0, 0), 1);                                           // a0 b0
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<128>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1]
+                        for (int kk = 1; kk < 4; kk++) mma_n<128, F16>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1]
                     }
                 } else {
 #pragma unroll
                     for (int q = 0; q < NPROD; q++)
 #pragma unroll
                         for (int kk = 0; kk < TC_BK / 16; kk++)
-                            mma_n<BN>(acc, A(prod_a(X6, q), kk), Bd(prod_b(X6, q), kk), (q > 0 || kk > 0) ? 1u : 0u);
+                            mma_n<BN, F16>(acc, A(prod_a(X6, q), kk), Bd(prod_b(X6, q), kk), (q > 0 || kk > 0) ? 1u : 0u);
                 }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
@@ -315,6 +336,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int q4 = warp & 3;                                 // tensor-memory lane quarter
         const int row = m0 + q4 * 32 + lane;
         const float4 wr = EPI == EPI_WEIGHT2 ? P.wrow[row] : make_float4(0.f, 0.f, 0.f, 0.f);   // loaded early
+        if constexpr (F16) {                                     // this tile's factors of B, every k-block
+            constexpr int wpk = BN / 4;                          // 4 exponents per global word
+            const int rt = (int)threadIdx.x - 64, words = total * wpk;
+            for (int w = rt; w < words; w += 128) {
+                const int kb = w / wpk, c4 = w - kb * wpk;
+                const int e4 = __ldg((const int*)(P.b_exp + (size_t)kb * P.N + n0 + 4 * c4));
+                uint32_t f[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) f[i] = (uint32_t)(127 - F16_CONST - ((e4 << (24 - 8 * i)) >> 24)) << 7;
+                ((uint2*)ftab)[w] = make_uint2(f[0] | (f[1] << 16), f[2] | (f[3] << 16));
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+        }
         float r[BN];
 #pragma unroll
         for (int i = 0; i < BN; i++) r[i] = 0.f;
@@ -340,8 +374,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int i = 0; i < 32; i++) v[i] = __fadd_rn(w[i], v[i]);
                 }
+                if constexpr (F16) {                             // back to values: exact powers of two
+                    const uint32_t* tp = (const uint32_t*)(ftab + it * BN + c0);
 #pragma unroll
-                for (int i = 0; i < 32; i++) r[c0 + i] = __fadd_rn(r[c0 + i], v[i]);
+                    for (int h = 0; h < 16; h++) {               // two factors per 4-byte read
+                        const uint32_t w2 = tp[h];
+                        r[c0 + 2 * h] = fmaf(v[2 * h], __uint_as_float(__byte_perm(w2, 0u, 0x1044u)), r[c0 + 2 * h]);
+                        r[c0 + 2 * h + 1] =
+                            fmaf(v[2 * h + 1], __uint_as_float(__byte_perm(w2, 0u, 0x3244u)), r[c0 + 2 * h + 1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; i++) r[c0 + i] = __fadd_rn(r[c0 + i], v[i]);
+                }
             }
             tc_fence_before();
             __syncwarp();
@@ -370,6 +415,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int c = 0; c < BN / 4; c++)
                     st_shared_v4(sbase + chunk(c >> 3, c & 7), make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2],
                                                                           r[4 * c + 3]));
+            } else if (EPI == EPI_SPLIT && F16) {                // float16 terms of each 64-column chunk, scaled
+#pragma unroll
+                for (int g = 0; g < BN / 64; g++) {
+                    float mx = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 64; i++) mx = fmaxf(mx, fabsf(r[64 * g + i]));
+                    const int e = f16_chunk_exp(mx);
+                    const float sc = __int_as_float((127 + e) << 23);
+                    P.o_exp[(size_t)(n0 / 64 + g) * P.M + row] = (signed char)e;
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        __align__(16) __half ta[8], tb[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) split2h(r[64 * g + 8 * c + i] * sc, ta[i], tb[i]);
+                        st_shared_v4(sbase + chunk(0 * (BN / 64) + g, c), *(const float4*)ta);
+                        st_shared_v4(sbase + chunk(1 * (BN / 64) + g, c), *(const float4*)tb);
+                    }
+                }
             } else if (EPI == EPI_SPLIT) {                       // bf16 terms: boxes of 64 columns, term-major
 #pragma unroll
                 for (int c = 0; c < BN / 8; c++) {
@@ -380,6 +443,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     st_shared_v4(sbase + chunk(0 * (BN / 64) + g, c & 7), *(const float4*)ta);
                     st_shared_v4(sbase + chunk(1 * (BN / 64) + g, c & 7), *(const float4*)tb);
                     st_shared_v4(sbase + chunk(2 * (BN / 64) + g, c & 7), *(const float4*)tc);
+                }
+            } else if (F16) {
+                // Kx = K Wx, Ky = K Wy as below, each row's 64 columns scaled by its own power of two (the largest
+                // magnitude first, then the same products again, split); boxes 0-1: the terms of Kx, 2-3: of Ky
+                auto kxy = [&](int i, float& kx, float& ky) {
+                    const float4 wc = wsh[i];
+                    const float t = wr.x + wc.x;
+                    const float rr = t > 0.f ? recip(t) : 0.f;
+                    kx = r[i] * (wr.y * wc.z * rr);
+                    ky = r[i] * (wc.y * wr.z * rr);
+                };
+                float mxx = 0.f, mxy = 0.f;
+#pragma unroll
+                for (int i = 0; i < BN; i++) {
+                    float kx, ky;
+                    kxy(i, kx, ky);
+                    mxx = fmaxf(mxx, fabsf(kx));
+                    mxy = fmaxf(mxy, fabsf(ky));
+                }
+                const int exx = f16_chunk_exp(mxx), exy = f16_chunk_exp(mxy);
+                const float scx = __int_as_float((127 + exx) << 23), scy = __int_as_float((127 + exy) << 23);
+                P.o_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exx;
+                P.o2_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exy;
+#pragma unroll
+                for (int c = 0; c < BN / 8; c++) {
+                    __align__(16) __half xa[8], xb[8], ya[8], yb[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        float kx, ky;
+                        kxy(8 * c + i, kx, ky);
+                        split2h(kx * scx, xa[i], xb[i]);
+                        split2h(ky * scy, ya[i], yb[i]);
+                    }
+                    st_shared_v4(sbase + chunk(0, c), *(const float4*)xa);
+                    st_shared_v4(sbase + chunk(1, c), *(const float4*)xb);
+                    st_shared_v4(sbase + chunk(2, c), *(const float4*)ya);
+                    st_shared_v4(sbase + chunk(3, c), *(const float4*)yb);
                 }
             } else {
                 // Kx = K Wx, Ky = K Wy with Wx = (s kx_p / bin_x) w_q r, Wy = (s ky_q / bin_x) w_p r,
@@ -415,15 +515,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                 for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, m0);
             } else if (EPI == EPI_SPLIT) {
+                constexpr int OT = F16 ? 2 : 3;                  // output terms
 #pragma unroll
-                for (int t = 0; t < 3; t++)
+                for (int t = 0; t < OT; t++)
 #pragma unroll
                     for (int g = 0; g < BN / 64; g++) tma_store_3d(mo, sbase + (t * (BN / 64) + g) * EPI_BOX, n0 + 64 * g, m0, t);
             } else {
+                constexpr int OT = F16 ? 2 : 3;
 #pragma unroll
-                for (int t = 0; t < 3; t++) {
+                for (int t = 0; t < OT; t++) {
                     tma_store_3d(mo, sbase + t * EPI_BOX, n0, m0, t);
-                    tma_store_3d(mo2, sbase + (3 + t) * EPI_BOX, n0, m0, t);
+                    tma_store_3d(mo2, sbase + (OT + t) * EPI_BOX, n0, m0, t);
                 }
             }
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -456,15 +558,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// Three bf16 planes [3][rows][K] as a 3-D tensor (K, rows, term); box = 64 x box_rows x 1.
-static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows) {
+// 16-bit term planes [terms][rows][K] as a 3-D tensor (K, rows, term); box = 64 x box_rows x 1. Three bf16 planes
+// (the bf16 modes; bf16x3 reads two of them) or two float16 planes (f16x3).
+static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows, bool f16 = false) {
     auto fn = encode_fn();
     if (!fn) return false;
-    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, f16 ? 2u : 3u};
     cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
     cuuint32_t box[3] = {TC_BK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+    CUresult r = fn(m, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+                    const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -494,20 +598,28 @@ struct TcOp {
     TcProblem p;
 };
 
-template <int BN, int EPI, int X6>
+template <int BN, int EPI, int MODE>
 static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
+    constexpr bool F16 = MODE == 2;
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI, X6>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
+        if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
             cudaSuccess)
             return GP103_ERR_CUDA;
         attr = true;
     }
+    constexpr int terms = MODE == 1 ? 3 : 2;
+    constexpr int stage_bytes = terms * TC_A_TILE + terms * BN * TC_BK * 2;
+    constexpr int stages = TC_STAGE_SPACE / stage_bytes > TC_MAX_STAGES ? TC_MAX_STAGES : TC_STAGE_SPACE / stage_bytes;
     CUtensorMap maps[8];
     TcArgs args = {};
     for (int z = 0; z < 2; z++) {
         const TcOp& o = ops[z < nops ? z : 0];
-        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM) || !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, BN))
+        if (F16 && ((long long)(o.p.K / TC_BK) * BN * 2 > TC_STAGE_SPACE - (long long)stages * stage_bytes ||
+                    !o.p.b_exp || (EPI != EPI_PLAIN && !o.p.o_exp) || (EPI == EPI_WEIGHT2 && !o.p.o2_exp)))
+            return GP103_ERR_ARG;
+        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM, F16) ||
+            !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, BN, F16))
             return GP103_ERR_CUDA;
         // outputs (stored by TMA): bf16 terms [3][M][N] as (N, M, term) boxes of 64 x 128; float32 [M][N]
         CUtensorMap* oa = &maps[4 + 2 * z];
@@ -517,20 +629,18 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
             ok = make_map_f32(oa, o.p.out_f32, o.p.M, o.p.N);
             *ob = *oa;
         } else {
-            ok = make_map(oa, o.p.o_terms, o.p.M, o.p.N, TC_BM);
-            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M, o.p.N, TC_BM);
+            ok = make_map(oa, o.p.o_terms, o.p.M, o.p.N, TC_BM, F16);
+            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M, o.p.N, TC_BM, F16);
             else *ob = *oa;
         }
         if (!ok) return GP103_ERR_CUDA;
         args.p[z] = o.p;
     }
-    constexpr int terms = X6 ? 3 : 2;
-    args.stages = TC_STAGE_SPACE / (terms * TC_A_TILE + terms * BN * TC_BK * 2);
-    if (args.stages > TC_MAX_STAGES) args.stages = TC_MAX_STAGES;
+    args.stages = stages;
     args.err = err;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / BN, p.M / TC_BM, nops);
-    if (launch_k(tc_gemm_kernel<BN, EPI, X6>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2],
+    if (launch_k(tc_gemm_kernel<BN, EPI, MODE>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2],
                  maps[3], maps[4], maps[5], maps[6], maps[7], args) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
@@ -539,8 +649,9 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
 
 template <int BN, int EPI>
 static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
-    return mode == GP103_FIELD_BF16X3 ? launch_tc_mode<BN, EPI, 0>(ops, nops, err, s)
-                                      : launch_tc_mode<BN, EPI, 1>(ops, nops, err, s);
+    if (mode == GP103_FIELD_BF16X3) return launch_tc_mode<BN, EPI, 0>(ops, nops, err, s);
+    if (mode == GP103_FIELD_F16X3) return launch_tc_mode<BN, EPI, 2>(ops, nops, err, s);
+    return launch_tc_mode<BN, EPI, 1>(ops, nops, err, s);
 }
 
 // One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles. The epilogue is a
@@ -565,6 +676,32 @@ __global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t)
     }
 }
 
+// f16x3: a float32 density [nbx][nby] into two float16 terms, each row's 64-bin chunks scaled by their own power of
+// two (one warp per chunk, two bins per lane), the exponents in e[(y / 64) * nbx + x]
+__global__ void split_density_f16_kernel(const float* d, int nbx, int nby, __half* t, signed char* e) {
+    pdl_wait();
+    const int lane = threadIdx.x & 31;
+    const long long chunks = (long long)nbx * nby / 64, n = (long long)nbx * nby;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+        const float2 v = *(const float2*)(d + 64 * c + 2 * lane);
+        float mx = fmaxf(fabsf(v.x), fabsf(v.y));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const int ex = f16_chunk_exp(mx);
+        const float sc = __int_as_float((127 + ex) << 23);
+        __half a0, b0, a1, b1;
+        split2h(v.x * sc, a0, b0);
+        split2h(v.y * sc, a1, b1);
+        *(__half2*)(t + 64 * c + 2 * lane) = __halves2half2(a0, a1);
+        *(__half2*)(t + n + 64 * c + 2 * lane) = __halves2half2(b0, b1);
+        if (lane == 0) {
+            const long long x = (64 * c) / nby, y = (64 * c) % nby;
+            e[(y / 64) * nbx + x] = (signed char)ex;
+        }
+    }
+}
+
 int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* density, float* ex, float* ey,
              cudaStream_t s) {
     if (!field_tc_supported(L.nbx, L.nby)) return GP103_ERR_SHAPE;
@@ -574,7 +711,14 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     auto B = [](const char* base, size_t off) { return (__nv_bfloat16*)(base + off); };
     int* err = (int*)(w + L.w_err);
     int st;
-    if (density) {
+    const bool f16 = L.mode == GP103_FIELD_F16X3;
+    auto E = [&](size_t off) { return f16 ? (signed char*)(w + off) : (signed char*)nullptr; };
+    if (density && f16) {
+        if (launch_k(split_density_f16_kernel, dim3(grid_for((size_t)X * Y / 2, 256, 8)), dim3(256), 0, s, density, X,
+                     Y, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    } else if (density) {
         if (launch_k(split_density_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density, (size_t)X * Y, B(w, L.w_a)) != cudaSuccess) return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
@@ -587,11 +731,16 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     //    product comes out in rows (no transposing epilogue)
     TcOp o1 = {B(c, L.c_cy), Y, B(w, L.w_a), X, prob(Y, X, Y, EPI_SPLIT)};
     o1.p.o_terms = B(w, L.w_tt);
+    o1.p.b_exp = E(L.e_a);
+    o1.p.o_exp = E(L.e_tt);
     if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
     // 2: K = Cx T -> Kx, Ky
     TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
     o2.p.o_terms = B(w, L.w_kx);
     o2.p.o2_terms = B(w, L.w_ky);
+    o2.p.b_exp = E(L.e_tt);
+    o2.p.o_exp = E(L.e_kx);
+    o2.p.o2_exp = E(L.e_ky);
     o2.p.wrow = (const float4*)(c + L.c_wrow);
     o2.p.wcol = (const float4*)(c + L.c_wcol);
     if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
@@ -600,12 +749,18 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
                   {B(c, L.c_syt), Y, B(w, L.w_ky), X, prob(Y, X, Y, EPI_SPLIT)}};
     o3[0].p.o_terms = B(w, L.w_pt);
     o3[1].p.o_terms = B(w, L.w_qt);
+    o3[0].p.b_exp = E(L.e_kx);
+    o3[0].p.o_exp = E(L.e_pt);
+    o3[1].p.b_exp = E(L.e_ky);
+    o3[1].p.o_exp = E(L.e_qt);
     if ((st = launch_tc(o3, 2, L.mode, err, s))) return st;
     // 3b / 4b: Ex = Sx^T P, Ey = Cx^T Q
     TcOp o4[2] = {{B(c, L.c_sxt), X, B(w, L.w_pt), Y, prob(X, Y, X, EPI_PLAIN)},
                   {B(c, L.c_cxt), X, B(w, L.w_qt), Y, prob(X, Y, X, EPI_PLAIN)}};
     o4[0].p.out_f32 = ex;
     o4[1].p.out_f32 = ey;
+    o4[0].p.b_exp = E(L.e_pt);
+    o4[1].p.b_exp = E(L.e_qt);
     return launch_tc(o4, 2, L.mode, err, s);
 }
 

@@ -47,6 +47,15 @@ constexpr int SMS = 152;                           // GB300: 2 dies x 76 SMs
 
 __host__ __device__ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Field mode f16x3: the power-of-two exponent e that scales a chunk of largest magnitude mx into [2^14, 2^15)
+// (float16 terms with room to spare), clamped to [-100, 100] so that every factor 2^(+-e - 14) stays a normal
+// float32 (a chunk of zeros or of subnormals gets 100).
+__device__ __forceinline__ int f16_chunk_exp(float mx) {
+    const int be = (int)((__float_as_uint(mx) >> 23) & 0xFFu);
+    const int e = be == 0 ? 100 : 14 - (be - 127);
+    return min(max(e, -100), 100);
+}
+
 // Grid for a grid-stride loop over n items: at most `per_sm` blocks per SM, at least one block.
 inline int grid_for(long long n, int threads, int per_sm) {
     long long g = (n + threads - 1) / threads;

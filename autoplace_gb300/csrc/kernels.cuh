@@ -96,6 +96,8 @@ struct PostJob {
     float* dens;                // plain density, may be null
     __nv_bfloat16 *t0, *t1, *t2;  // bf16 split terms of the density, may be null
     int terms;
+    signed char* exps;          // non-null: float16 terms (t0, t1 hold __half) of each 64-bin chunk of a row scaled by
+                                // 2^e, e = exps[(y / 64) * nbx + x] (nby a multiple of 64)
     int exact;                  // float64 per-thread partials of the sum (evaluators); 0: float32 (hot path)
     Reduce red;                 // sum of the density above the target
 };

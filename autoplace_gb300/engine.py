@@ -89,12 +89,12 @@ def pinned_inputs(prob):
 
 
 class Placer(object):
-    def __init__(self, prob, field="bf16x6", device=None, check_every=16, use_graphs=True, stream=None,
+    def __init__(self, prob, field="f16x3", device=None, check_every=16, use_graphs=True, stream=None,
                  sort_every=None, host=None, handover_gamma=0.0):
         """host: optional {name: pinned CPU tensor} holding the problem's arrays (pinned_inputs), uploaded instead
         of the Problem's numpy arrays. handover_gamma: a run on clusters stops ("handover") once its smoothing is
         down to this (the smoothing the cells start with); 0 = never.
-        A tensor-core field (bf16x3, bf16x6) needs a grid of multiples of 128 bins per side: on a smaller grid
+        A tensor-core field (f16x3, bf16x6, bf16x3) needs a grid of multiples of 128 bins per side: on a smaller grid
         (clusters, small designs) the field runs in fp32."""
         self.p = prob
         self.dev = torch.device(device or "cuda")

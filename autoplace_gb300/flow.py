@@ -27,7 +27,7 @@ def _gamma(base_gamma, overflow):
     return base_gamma * 10 ** ((overflow - 0.1) * 20 / 9 - 1)
 
 
-def global_placement(prob, pos0, field="bf16x6", device="cuda", log=None, check_every=16, use_graphs=True,
+def global_placement(prob, pos0, field="f16x3", device="cuda", log=None, check_every=16, use_graphs=True,
                      stream=None):
     """Place prob from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
     (stop_reason, iters, start_iters, gp_time_s, per_iter_s, grad_calls; with two levels also clusters,

@@ -8,8 +8,8 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_ARG, ERR_CUDA, ERR_SHAPE = 0, 1, 2, 3
-FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6 = 0, 1, 2
-FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6}
+FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6, FIELD_F16X3 = 0, 1, 2, 3
+FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6, "f16x3": FIELD_F16X3}
 PHASE_START, PHASE_DENSITY = 0, 1
 PASS_SORT = 0x100
 T = dict(alpha=0, a=1, iter=2, loop_it=3, done=4, stop=5, accept=6, hpwl=7, wa=8, evals=9, nwa=10, start_tol=11,

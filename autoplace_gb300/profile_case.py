@@ -2,7 +2,7 @@
 inside an NVTX range "gp103_profile", so that a profiler can be limited to them with
 --nvtx --nvtx-include "gp103_profile/".
 
-    python -m autoplace_gb300.profile_case --config c2 --passes 8 [--field bf16x6]
+    python -m autoplace_gb300.profile_case --config c2 --passes 8 [--field f16x3]
 """
 import argparse
 import time
@@ -16,7 +16,7 @@ from .engine import Placer
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--field", default="bf16x6")
+    ap.add_argument("--field", default="f16x3")
     ap.add_argument("--passes", type=int, default=8)
     a = ap.parse_args(argv)
     nl, o = synth.preset(a.config)

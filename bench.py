@@ -1,6 +1,6 @@
 """Benchmark: time to overflow 0.07 of one global-placement level of the 1.2M-cell synthetic netlist on a GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2] [--field bf16x6]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2] [--field f16x3]
 
 Workload (config "c2"): 1,200,000 cells, 1,250,000 nets (5.2M pins, degree mix 2/3/4-10/11-100), 40 macros over 20 %
 of the region, target density 0.8, force grid 1024 x 1024, overflow grid 512 x 512; seeded synthetic data (the
@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2")
-    p.add_argument("--field", default="bf16x6", choices=["bf16x6", "bf16x3", "fp32"])
+    p.add_argument("--field", default="f16x3", choices=["f16x3", "bf16x6", "bf16x3", "fp32"])
     p.add_argument("--cpu-iters", type=int, default=4, help="density-phase iterations of the CPU sample")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
@@ -204,8 +204,10 @@ def cpu_baseline_dict(per, threads, iters, gpu_iters, source):
 
 
 # ------------------------------------------------------------------------------------------------ roofline
-def kernel_bytes(prob):
+def kernel_bytes(prob, field="f16x3"):
     """Algorithmic bytes (or flops) per launch of each kernel, by launcher name."""
+    terms = 3 if field in ("bf16x6", "bf16x3") else 2 if field == "f16x3" else 0     # 16-bit density terms out
+    dens = 2 * terms if terms else 4
     cs, n, c = prob.csr, prob.num_nodes, prob.num_mov
     P, N = len(cs.cell32), cs.num_nets
     nb = prob.force_bin * prob.force_bin
@@ -214,14 +216,14 @@ def kernel_bytes(prob):
         "launch_wa_net": 20 * P + 8 * c + 4 * N,                       # pins (cell, offset) in, pin gradient out
         "launch_gather": 44 * n + 12 * P + 4 * c + 8 * nb,             # node data, cell CSR gather, field planes
         "launch_scatter": 20 * n + 16 * nb,                            # node data in, map out (force grid); judge below
-        "launch_post_plain": 42 * nb,                                   # map in + zeroed, fixed in, bf16 terms out
+        "launch_post_plain": (36 + dens) * nb,                          # map in + zeroed, fixed in, density terms out
         "launch_step": 56 * n,                                          # u, v, g, lo, hi in; u', v' out
     }
 
 
 def tc_flops(prob, field):
     nb = prob.force_bin
-    terms = {"bf16x6": 6, "bf16x3": 3}.get(field, 0)
+    terms = {"bf16x6": 6, "bf16x3": 3, "f16x3": 3}.get(field, 0)
     return 2.0 * nb ** 3 * terms        # per GEMM
 
 
@@ -251,7 +253,7 @@ def roofline(prob, field, prof, peaks, config="c2"):
     traffic = measured_traffic(config, field)
     hbm = peaks.get("hbm_gbs")
     tc = peaks.get("bf16_tflops")
-    by = kernel_bytes(prob)
+    by = kernel_bytes(prob, field)
     dom = max(prof.items(), key=lambda kv: kv[1]["ms_per_pass"])
     name, d = dom
     ms_launch = d["ms_per_pass"] / max(d["launches_per_pass"], 1e-9)

@@ -246,7 +246,9 @@ def _density_plane(nb, seed=0):
 
 @pytest.mark.parametrize("nb,mode,tol", [(64, native.FIELD_FP32, 2e-6), (128, native.FIELD_FP32, 2e-6),
                                          (128, native.FIELD_BF16X6, 1e-6), (256, native.FIELD_BF16X6, 1e-6),
-                                         (256, native.FIELD_BF16X3, 3e-5)])
+                                         (256, native.FIELD_BF16X3, 3e-5), (128, native.FIELD_F16X3, 1e-6),
+                                         (256, native.FIELD_F16X3, 1e-6), (1024, native.FIELD_F16X3, 1e-6),
+                                         (1024, native.FIELD_BF16X6, 1e-6)])
 def test_field_matches_fp64(nb, mode, tol):
     pl, keep = _field_plan(nb, mode)
     a = _density_plane(nb)
