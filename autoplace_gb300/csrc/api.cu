@@ -369,7 +369,36 @@ static WaJob wa_job(const gp103_plan* p) {
     return w;
 }
 
+extern "C" int gp103_event_create(void** event) {
+    REQUIRE(event);
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GP103_ERR_CUDA;
+    *event = (void*)e;
+    return GP103_OK;
+}
+
+extern "C" int gp103_event_destroy(void* event) {
+    REQUIRE(event);
+    return cudaEventDestroy((cudaEvent_t)event) == cudaSuccess ? GP103_OK : GP103_ERR_CUDA;
+}
+
+static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream, cudaStream_t side,
+                    cudaEvent_t fork, cudaEvent_t join);
+
 extern "C" int gp103_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream) {
+    return run_pass(plan, phase_flags, stream, nullptr, nullptr, nullptr);
+}
+
+extern "C" int gp103_pass_split(const gp103_plan* plan, int phase_flags, cudaStream_t stream, cudaStream_t side,
+                                void* fork, void* join) {
+    REQUIRE(side != stream && fork && join && fork != join);
+    return run_pass(plan, phase_flags, stream, side, (cudaEvent_t)fork, (cudaEvent_t)join);
+}
+
+// One pass. With a side stream (density passes): the WA kernels run there, between a fork after the step and a
+// join before the gather, while `stream` runs the sort, the density map and the field; the results are the same.
+static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream, cudaStream_t side,
+                    cudaEvent_t fork, cudaEvent_t join) {
     TRY(check_plan(plan));
     const gp103_plan* p = plan;
     const int phase = phase_flags & ~GP103_PASS_SORT;
@@ -391,13 +420,19 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase_flags, cudaStream_t 
     const bool ordered = phase == GP103_PHASE_DENSITY && p->order != nullptr;
     if (sort) sj.ord = order_job(p);
     TRY(launch_step(sj, stream));
+    const bool split = side != nullptr && phase == GP103_PHASE_DENSITY;
+    if (split) {
+        if (cudaEventRecord(fork, stream) != cudaSuccess || cudaStreamWaitEvent(side, fork, 0) != cudaSuccess)
+            return GP103_ERR_CUDA;
+    }
     if (sort) TRY(launch_order(sj.ord, (const float2*)p->v[0], (const float2*)p->v[1], p->cur, true, stream));
 
     WaJob w = wa_job(p);
     w.pos_a = (const float2*)p->v[0];
     w.pos_b = (const float2*)p->v[1];
     w.sel = p->cur;
-    TRY(launch_wa_net(w, stream));
+    TRY(launch_wa_net(w, split ? side : stream));
+    if (split && cudaEventRecord(join, side) != cudaSuccess) return GP103_ERR_CUDA;
 
     GatherJob g = gather_job(p);
     g.pos_a = (const float2*)p->v[0];
@@ -416,6 +451,7 @@ extern "C" int gp103_pass(const gp103_plan* plan, int phase_flags, cudaStream_t 
         return launch_control_start(p->T, p->kp, r_moved, r_grad, r_wa, p->cur, stream);
     }
     TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream));
+    if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
     g.ex = p->ex;
     g.ey = p->ey;
     g.weight_p = p->kp + 1;

@@ -90,12 +90,16 @@ def pinned_inputs(prob):
 
 class Placer(object):
     def __init__(self, prob, field="f16x3", device=None, check_every=16, use_graphs=True, stream=None,
-                 sort_every=None, host=None, handover_gamma=0.0):
+                 sort_every=None, host=None, handover_gamma=0.0, split=False):
         """host: optional {name: pinned CPU tensor} holding the problem's arrays (pinned_inputs), uploaded instead
         of the Problem's numpy arrays. handover_gamma: a run on clusters stops ("handover") once its smoothing is
         down to this (the smoothing the cells start with); 0 = never.
         A tensor-core field (f16x3, bf16x6, bf16x3) needs a grid of multiples of 128 bins per side: on a smaller grid
-        (clusters, small designs) the field runs in fp32."""
+        (clusters, small designs) the field runs in fp32.
+        split: density passes with the WA kernels on a second stream, beside the density map and the field
+        (gp103_pass_split); the same results. Off by default: at c2 it measured 151.7 ms per placement against
+        146.8 ms in one stream (the fork and join replace programmatic launch edges; the two halves gain nothing
+        from sharing the GPU)."""
         self.p = prob
         self.dev = torch.device(device or "cuda")
         self.mode = field_mode(native.FIELD_MODES[field] if isinstance(field, str) else int(field),
@@ -106,6 +110,14 @@ class Placer(object):
         # density passes between refreshes of the scatter's spatial order (an order only speeds the scatter up)
         self.sort_every = max(int(sort_every or check_every), 1)
         self.stream = stream or torch.cuda.Stream(self.dev)
+        self.split = bool(split)
+        self.side = torch.cuda.Stream(self.dev) if self.split else None
+        self._events = []
+        if self.split:
+            for _ in range(2):
+                e = ctypes.c_void_p()
+                native.call("gp103_event_create", ctypes.byref(e))
+                self._events.append(e)
         self._graphs = {}
         self._captured = self._replayed = 0
         self._keep = []
@@ -197,6 +209,13 @@ class Placer(object):
         self._ref = ctypes.byref(pl)
         native.call("gp103_field_constants", self._ref, self.stream.cuda_stream)
 
+    def __del__(self):
+        try:
+            for e in getattr(self, "_events", []):
+                native.lib().gp103_event_destroy(e)
+        except Exception:
+            pass
+
     # ------------------------------------------------------------------ helpers
     def _hold(self, x):
         self._keep.append(x)
@@ -223,11 +242,17 @@ class Placer(object):
         self.sync()
         return float(self.scal[0].cpu())
 
-    def _passes(self, phase, k):
+    def _passes(self, phase, k, split=None):
         s = self.stream.cuda_stream
+        split = self.split if split is None else split
         for i in range(k):
             sort = phase == native.PHASE_DENSITY and i % self.sort_every == 0
-            native.call("gp103_pass", self._ref, phase | (native.PASS_SORT if sort else 0), s)
+            flags = phase | (native.PASS_SORT if sort else 0)
+            if split and phase == native.PHASE_DENSITY:
+                native.call("gp103_pass_split", self._ref, flags, s, self.side.cuda_stream, self._events[0],
+                            self._events[1])
+            else:
+                native.call("gp103_pass", self._ref, flags, s)
 
     def _replay(self, phase):
         if not self.use_graphs:

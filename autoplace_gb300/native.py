@@ -76,6 +76,9 @@ _SIGS = {
     "gp103_coarse_pins_scratch": ([_i], ctypes.c_size_t),
     "gp103_coarse_pins": ([_vp, _vp, _vp, _i, _i, _vp, _i, _vp, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_expand": ([_vp] * 5 + [_i, _vp, _vp], _i),
+    "gp103_pass_split": ([ctypes.POINTER(Plan), _i, _vp, _vp, _vp, _vp], _i),
+    "gp103_event_create": ([ctypes.POINTER(_vp)], _i),
+    "gp103_event_destroy": ([_vp], _i),
     "gp103_build_csr_scratch": ([_i, _i, _i], ctypes.c_size_t),
     "gp103_build_csr": ([_vp, _vp, _vp, _i, _i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 8 + [_vp], _i),
     "gp103_smooth_nodes": ([_vp, _i, _i, _d, _d, _f, _f] + [_vp] * 7 + [_vp], _i),

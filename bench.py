@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-pdl", action="store_true", help="plain stream order instead of programmatic dependent launch")
+    p.add_argument("--split", action="store_true", help="the WA kernels on a second stream, beside the density map")
     return p.parse_args()
 
 
@@ -160,6 +161,7 @@ def config_dict(prob, args, world):
             "cells": nl.num_mov, "nets": nl.num_nets, "pins": nl.num_pins, "nodes": prob.num_nodes,
             "force_grid": prob.force_bin, "overflow_grid": prob.num_bin, "target_density": prob.target,
             "field": args.field, "levels": 1, "start": "plain (wirelength-only)",
+            "streams": 2 if args.split else 1,
             "l2": "working set > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world}
 
 
@@ -230,7 +232,8 @@ def tc_flops(prob, field):
 def profile_pass(placer):
     """Per-launch durations of one density pass (eager, CUDA events on the engine's stream), averaged over 8."""
     from autoplace_gb300 import native
-    rec = native.profile(placer.stream.cuda_stream, lambda: placer._passes(native.PHASE_DENSITY, 8))
+    # one stream (the split pass runs the WA kernels beside the density map: per-launch events would overlap)
+    rec = native.profile(placer.stream.cuda_stream, lambda: placer._passes(native.PHASE_DENSITY, 8, split=False))
     agg = {}
     for name, ms in rec:
         a = agg.setdefault(name, [0, 0.0])
@@ -302,7 +305,7 @@ def run_gb300(args):
         from autoplace_gb300 import native
         native.call("gp103_set_option", 0, 0)
     prob, pos0 = workload(args.config, seed=rank)
-    placer = Placer(prob, field=args.field)
+    placer = Placer(prob, field=args.field, split=args.split)
     dpos = torch.tensor(pos0, device="cuda")
     r = None
     for _ in range(max(args.warmup, 0)):
@@ -352,7 +355,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         t = time.time()
         dprob = base.on_device(stream=placer.stream, host=host)
-        pl2 = Placer(dprob, field=args.field, stream=placer.stream, host=maps)
+        pl2 = Placer(dprob, field=args.field, stream=placer.stream, host=maps, split=args.split)
         rr = pl2.run(host_pos)
         out.copy_(rr["pos"])
         torch.cuda.synchronize()

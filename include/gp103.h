@@ -219,6 +219,17 @@ int gp103_probe(const gp103_plan* plan, const float* v, const float* g, double s
 /* The field of a plain density map a [nbx, nby] (float32) into ex, ey [nbx, nby] with the plan's field mode. */
 int gp103_field(const gp103_plan* plan, const float* density, float* ex, float* ey, cudaStream_t stream);
 
+/* gp103_pass with two streams (density passes; a wirelength-only pass runs on `stream` alone): the WA kernels run on
+ * `side`, which waits for the step (event `fork`, recorded on `stream`), while `stream` runs the spatial sort, the
+ * density map and the field; `stream` waits for them (event `join`, recorded on `side`) before the gather. The two
+ * halves of a pass share the GPU; the results are those of gp103_pass. Captured in a CUDA graph, the events become
+ * the graph's fork and join. fork, join: two distinct events (gp103_event_create), side != stream. */
+int gp103_pass_split(const gp103_plan* plan, int phase_flags, cudaStream_t stream, cudaStream_t side, void* fork,
+                     void* join);
+/* An event for gp103_pass_split (cudaEventDisableTiming), and its release. */
+int gp103_event_create(void** event);
+int gp103_event_destroy(void* event);
+
 /* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
 int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
 

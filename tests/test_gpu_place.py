@@ -65,6 +65,21 @@ def test_fused_pass_is_repeatable():
     assert np.array_equal(res[0][3], res[1][3])
 
 
+def test_split_pass_matches_single_stream():
+    """The WA kernels on a second stream beside the density map and the field (gp103_pass_split): the same run, bit
+    for bit, graphs or not."""
+    from autoplace_gb300.engine import Placer
+    prob = _problem(cells=6000, nb=128, judge=64, seed=3)
+    pos0 = synth.init_positions(prob.nl, prob.num_nodes, seed=1)
+    res = []
+    for split, graphs in ((False, True), (True, True), (True, False)):
+        r = Placer(prob, field="f16x3", check_every=8, split=split, use_graphs=graphs).run(pos0)
+        res.append((r["iters"], r["hpwl"], r["overflow"], r["pos"].cpu().numpy()))
+    for r in res[1:]:
+        assert r[:3] == res[0][:3]
+        assert np.array_equal(r[3], res[0][3])
+
+
 def test_level_matches_reference_run(gold):
     """The reference's own CPU run (golden_place.npz) and this GPU run of the same level: same stop, HPWL within
     0.5 %, iteration counts within 5 %."""
