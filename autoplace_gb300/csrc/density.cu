@@ -606,7 +606,9 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
 }
 
 int launch_gather(const GatherJob& j, cudaStream_t s) {
-    if (launch_k(gather_kernel, dim3(grid_for(j.num_nodes, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
+    static const int resident = resident_blocks(gather_kernel, 256);
+    if (launch_k(gather_kernel, dim3(min(grid_for(j.num_nodes, 256, 8), resident)), dim3(256), 0, s, j) != cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -47,6 +47,16 @@ constexpr int SMS = 152;                           // GB300: 2 dies x 76 SMs
 
 __host__ __device__ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// The blocks of `kernel` that are resident on the whole GPU at `threads` per block (its occupancy x the SMs): the
+// grid of a grid-stride loop in which every block stays busy to the end, with no second wave, and which writes as
+// few reduction partials as that allows. Callers keep it in a function-local static (one query per kernel).
+template <typename K>
+inline int resident_blocks(K kernel, int threads, size_t smem = 0) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
+    return per * SMS;
+}
+
 // Field mode f16x3: the power-of-two exponent e that scales a chunk of largest magnitude mx into [2^14, 2^15)
 // (float16 terms with room to spare), clamped to [-100, 100] so that every factor 2^(+-e - 14) stays a normal
 // float32 (a chunk of zeros or of subnormals gets 100).

@@ -204,7 +204,9 @@ __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ StepJ
 }
 
 int launch_step(const StepJob& j, cudaStream_t s) {
-    if (launch_k(step_kernel, dim3(grid_for(j.n, 256, 8)), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
+    static const int resident = resident_blocks(step_kernel, 256);
+    const int grid = min(grid_for(j.n, 256, 8), resident);
+    if (launch_k(step_kernel, dim3(grid), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

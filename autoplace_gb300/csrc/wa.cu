@@ -344,8 +344,10 @@ int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const long long chunks = (j.split + 31) / 32;
     const long long longs = (j.mid - j.split + 3) / 4 + (j.num_nets - j.mid);     // warp items of the long kernel
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
-    const int g1 = chunks > 0 || longs == 0 ? grid_for(chunks * 32, 256, 8) : 0;
-    const int g2 = longs > 0 ? grid_for(longs * 32, 256, 4) : 0;
+    static const int res_short = resident_blocks(wa_short_kernel<false>, 256);
+    static const int res_long = resident_blocks(wa_long_kernel, 256);
+    const int g1 = chunks > 0 || longs == 0 ? min(grid_for(chunks * 32, 256, 8), res_short) : 0;
+    const int g2 = longs > 0 ? min(grid_for(longs * 32, 256, 4), res_long) : 0;
     if (g1 > 0) {
         cudaError_t e = inline_long ? launch_k(wa_short_kernel<true>, dim3(g1), dim3(256), 0, s, j, 0, g1 + g2)
                                     : launch_k(wa_short_kernel<false>, dim3(g1), dim3(256), 0, s, j, 0, g1 + g2);
