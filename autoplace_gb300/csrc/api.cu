@@ -446,9 +446,16 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     const Reduce r_moved = reduce_slot(p->red, p->counters, R_MOVED);
     const Reduce r_grad = reduce_slot(p->red, p->counters, R_GRAD);
     const Reduce r_wa = reduce_slot(p->red, p->counters, R_WA);
+    // the step's, the WA kernels' and the post kernel's totals: summed by the gather's block 0 (TOT_* order)
+    double* pre = p->red + RED_TOTALS;
+    g.pre[TOT_MOVED] = r_moved; g.pre_k[TOT_MOVED] = 0;
+    g.pre[TOT_WA] = r_wa; g.pre_k[TOT_WA] = 0;
+    g.pre[TOT_HPWL] = r_wa; g.pre_k[TOT_HPWL] = 1;
+    g.npre = 3;
+    g.pre_out = pre;
     if (phase == GP103_PHASE_START) {
         TRY(launch_gather(g, stream));
-        return launch_control_start(p->T, p->kp, r_moved, r_grad, r_wa, p->cur, stream);
+        return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, stream);
     }
     TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream));
     if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
@@ -456,10 +463,12 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     g.ey = p->ey;
     g.weight_p = p->kp + 1;
     g.precond_p = p->kp + 2;
+    g.pre[TOT_OVF] = reduce_slot(p->red, p->counters, p->jnbx > 0 ? R_JOVF : R_OVF);
+    g.pre_k[TOT_OVF] = 0;
+    g.npre = 4;
     TRY(launch_gather(g, stream));
-    const Reduce ovf = reduce_slot(p->red, p->counters, p->jnbx > 0 ? R_JOVF : R_OVF);
     const double scale = p->jnbx > 0 ? p->jovf_scale : p->ovf_scale;
-    return launch_control_fused(p->S, p->kp, p->c, r_moved, r_grad, r_wa, ovf, scale, p->cur, stream);
+    return launch_control_fused(p->S, p->kp, p->c, r_grad, pre, scale, p->cur, stream);
 }
 
 extern "C" int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out, const float* g_ref, double weight,

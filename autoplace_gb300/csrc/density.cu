@@ -492,6 +492,15 @@ constexpr int GATHER_PINS = 8;
 
 __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     pdl_wait();
+    if (j.npre > 0 && blockIdx.x == 0) {                 // the earlier kernels' totals, off the critical path
+        for (int i = 0; i < j.npre; i++) {
+            const double t = block_total(j.pre[i], j.pre_k[i]);
+            if (threadIdx.x == 0) j.pre_out[i] = t;
+        }
+        return;
+    }
+    const int b0 = j.npre > 0 ? 1 : 0;                   // blocks b0 .. gridDim.x - 1 gather
+    const int bid = (int)blockIdx.x - b0, nblk = (int)gridDim.x - b0;
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     float2* gout = pick_mut(j.gout_a, j.gout_b, j.sel);
     const float2* gref = j.gref_a ? pick_ref(j.gref_a, j.gref_b, j.sel) : nullptr;
@@ -499,7 +508,7 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
     float precond = j.precond_p ? j.precond_p[0] : j.precond;
     const bool density = j.ex != nullptr;
     float d2 = 0.f, l1 = 0.f;                  // per-thread partials (a few nodes); float32 warp trees, float64 across warps and blocks
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j.num_nodes; i += gridDim.x * blockDim.x) {
+    for (int i = bid * blockDim.x + threadIdx.x; i < j.num_nodes; i += nblk * blockDim.x) {
         // wave 1: the node's own data
         const bool cell = i < j.num_mov;
         const bool wl = j.with_wl && cell;
@@ -602,13 +611,14 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
         if (cell) l1 += fabsf(g.x) + fabsf(g.y);
     }
     float v[2] = {d2, l1};
-    grid_sum<2>(v, j.red);
+    grid_sum<2>(v, j.red, nblk, bid);
 }
 
 int launch_gather(const GatherJob& j, cudaStream_t s) {
     static const int resident = resident_blocks(gather_kernel, 256);
-    if (launch_k(gather_kernel, dim3(min(grid_for(j.num_nodes, 256, 8), resident)), dim3(256), 0, s, j) != cudaSuccess)
-        return GP103_ERR_CUDA;
+    int grid = min(grid_for(j.num_nodes, 256, 8), resident);
+    if (j.npre > 0) grid = max(grid, 2);                 // block 0 sums, the others gather
+    if (launch_k(gather_kernel, dim3(grid), dim3(256), 0, s, j) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -31,7 +31,10 @@ inline Reduce reduce_slot(double* red, unsigned int* counters, int slot) {
     r.count = (int*)(counters + slot);
     return r;
 }
-constexpr size_t RED_DOUBLES = (size_t)R_COUNT * 4 * MAX_BLOCKS;
+// behind the partials: totals summed ahead of the control (GatherJob::pre), TOT_* order
+enum { TOT_MOVED = 0, TOT_WA, TOT_HPWL, TOT_OVF, TOT_COUNT };
+constexpr size_t RED_TOTALS = (size_t)R_COUNT * 4 * MAX_BLOCKS;
+constexpr size_t RED_DOUBLES = RED_TOTALS + 8;
 
 struct WaJob {
     const float2* pos_a; const float2* pos_b; const int* sel;
@@ -122,6 +125,12 @@ struct GatherJob {
     float2* gout_a; float2* gout_b;
     const float2* gref_a; const float2* gref_b;     // null: no distance
     Reduce red;                 // (|g - gref|^2, L1 of g over the cells)
+    // npre > 0: block 0 does no gathering: it sums the partials of earlier kernels, pre[i] value pre_k[i], in the
+    // order block_totals sums them (the same bits), into pre_out[i], while the other blocks gather
+    Reduce pre[4];
+    int pre_k[4];
+    int npre;
+    double* pre_out;
 };
 
 // Exclusive scan of n ints (build.cu): out[i] = in[0] + ... + in[i - 1], *total = the whole sum (device int);

@@ -238,12 +238,11 @@ int launch_probe(const float* v, const float* g, const float* lo, const float* h
 
 // The density phase's control: one block adds the pass's float64 partial sums (in block order), then one thread
 // runs the control; an accepted step flips the current buffers.
-__global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp, const double* c, Reduce moved2,
-                                                            Reduce grad, Reduce wa_hpwl, Reduce ovf_sum,
-                                                            double ovf_scale, int* cur) {
+// pre: the totals the gather's block 0 summed (TOT_MOVED, TOT_WA, TOT_HPWL, TOT_OVF); the gather's own partials
+// (the squared distance of the gradients) are summed here
+__global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp, const double* c, Reduce grad,
+                                                            const double* pre, double ovf_scale, int* cur) {
     pdl_wait();
-    const Reduce r[5] = {moved2, grad, wa_hpwl, wa_hpwl, ovf_sum};
-    const int k[5] = {0, 0, 0, 1, 0};
     // the state and the constants in registers first (one wave of loads): the control reads them one after another,
     // and through global memory every read after a write would wait a full memory latency
     double Sl[S_SIZE], cl[C_SIZE];
@@ -256,10 +255,10 @@ __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp
 #pragma unroll
         for (int i = 0; i < 5; i++) kpl[i] = kp[i];
     }
-    double t[5];
-    block_totals<5>(r, k, t);
+    const double turned2 = block_total(grad, 0);
     if (threadIdx.x == 0) {
-        const bool accepted = control_body(Sl, kpl, cl, sqrt(t[0]), sqrt(t[1]), t[3], t[4] * ovf_scale, t[2]);
+        const bool accepted = control_body(Sl, kpl, cl, sqrt(pre[TOT_MOVED]), sqrt(turned2), pre[TOT_HPWL],
+                                           pre[TOT_OVF] * ovf_scale, pre[TOT_WA]);
 #pragma unroll
         for (int i = 0; i < S_SIZE; i++) S[i] = Sl[i];
 #pragma unroll
@@ -268,10 +267,9 @@ __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp
     }
 }
 
-int launch_control_fused(double* S, float* kp, const double* c, Reduce moved2, Reduce grad, Reduce wa_hpwl,
-                         Reduce ovf_sum, double ovf_scale, int* cur, cudaStream_t s) {
-    if (launch_k(control_fused_kernel, dim3(1), dim3(256), 0, s, S, kp, c, moved2, grad, wa_hpwl, ovf_sum, ovf_scale,
-                 cur) != cudaSuccess)
+int launch_control_fused(double* S, float* kp, const double* c, Reduce grad, const double* pre, double ovf_scale,
+                         int* cur, cudaStream_t s) {
+    if (launch_k(control_fused_kernel, dim3(1), dim3(256), 0, s, S, kp, c, grad, pre, ovf_scale, cur) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
@@ -309,18 +307,16 @@ __device__ void control_start_body(double* T, float* kp, double moved, double tu
     kp[4] = (float)((an - 1) / ((1 + sqrt(4 * an * an + 1)) / 2));
 }
 
-__global__ void __launch_bounds__(256) control_start_kernel(double* T, float* kp, Reduce moved2, Reduce grad,
-                                                            Reduce wa_hpwl, int* cur) {
+__global__ void __launch_bounds__(256) control_start_kernel(double* T, float* kp, Reduce grad, const double* pre,
+                                                            int* cur) {
     pdl_wait();
-    const Reduce r[4] = {moved2, grad, wa_hpwl, wa_hpwl};
-    const int k[4] = {0, 0, 0, 1};
-    double t[4];
-    block_totals<4>(r, k, t);
-    if (threadIdx.x == 0) control_start_body(T, kp, sqrt(t[0]), sqrt(t[1]), t[2], t[3], cur);
+    const double turned2 = block_total(grad, 0);
+    if (threadIdx.x == 0)
+        control_start_body(T, kp, sqrt(pre[TOT_MOVED]), sqrt(turned2), pre[TOT_WA], pre[TOT_HPWL], cur);
 }
 
-int launch_control_start(double* T, float* kp, Reduce moved2, Reduce grad, Reduce wa_hpwl, int* cur, cudaStream_t s) {
-    if (launch_k(control_start_kernel, dim3(1), dim3(256), 0, s, T, kp, moved2, grad, wa_hpwl, cur) != cudaSuccess)
+int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, int* cur, cudaStream_t s) {
+    if (launch_k(control_start_kernel, dim3(1), dim3(256), 0, s, T, kp, grad, pre, cur) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
