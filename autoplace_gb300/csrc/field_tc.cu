@@ -529,7 +529,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             }
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+            // wait until the stores have read the staged boxes (the shared memory may then go); their writes are
+            // visible to the next kernel when this grid completes, which its griddepcontrol.wait waits for
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
         }
     }
     // Lane 0 of warps 0 and 1 leaves its role loop long after the other 31 lanes: reconverge every warp before the
