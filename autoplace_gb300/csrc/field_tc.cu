@@ -87,17 +87,18 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 // Bounded wait: false (and the error flag set) if the phase did not complete within TC_WAIT_NS, or if another
-// thread already gave up.
+// thread already gave up. The clock and the flag (a global load) are checked once every 64 tries (each try returns
+// within a bounded, system-dependent suspend time).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = gtime();
-    while (!mbar_try(bar, parity)) {
-        if (gtime() - t0 > TC_WAIT_NS || *(volatile int*)err != 0) {
+    for (unsigned i = 1;; i++) {
+        if (mbar_try(bar, parity)) return true;
+        if ((i & 63u) == 0u && (gtime() - t0 > TC_WAIT_NS || *(volatile int*)err != 0)) {
             atomicCAS(err, 0, code);
             return false;
         }
     }
-    return true;
 }
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y, int z) {
