@@ -126,3 +126,14 @@ def test_device_problem_build_rejects_bad_pins():
     bad["pin_cell"][17] = nl.num_mov + 5
     with pytest.raises(ValueError, match="cell out of range"):
         base.on_device(host=bad)
+
+
+@pytest.mark.parametrize("ignore", [1, 2, 3])
+def test_device_problem_build_filters(ignore):
+    """Degree filters that keep no net (1), only the 2-pin nets (2) or the 2- and 3-pin nets (3): the device build
+    equals the host build, empty CSR included."""
+    nl = synth.make_netlist(2000, 2100, window=100, macros=2, cover=0.1, fixed_pin_share=0.05, seed=8)
+    hp, dp = _check_device_problem(nl, problem.options(target_density=0.9, num_bin=64, force_num_bin=128,
+                                                       ignore_net_degree=ignore))
+    if ignore == 1:
+        assert dp.csr.num_nets == 0 and len(dp.csr.cell32) == 0
