@@ -319,6 +319,18 @@ class Placer(object):
             self.kp[0] = 10 * self.p.base_gamma
         return float(self.eval(pos, self.tmp[0], weight=0.0, with_wl=True)[2])
 
+    def _passes_left(self, Sh):
+        """Passes until the earliest stop the state makes certain, or None: once the run has settled (overflow under
+        the target after min_iter), the control stops ("converged") when settled exceeds settle_iter, at the earliest
+        after settle_iter + 1 - settled more passes; and at inner_iter passes in all. The host then runs exactly those
+        passes instead of a whole batch of check_every; passes after a stop change nothing, so the result is the
+        same, with fewer of them computed."""
+        o = self.p.opts
+        left = [int(o.inner_iter) - int(Sh[SK["loop_it"]])]
+        if Sh[SK["settled"]] > 0:
+            left.append(int(o.settle_iter) + 1 - int(Sh[SK["settled"]]))
+        return max(min(left), 1)
+
     # ------------------------------------------------------------------ one level
     def run(self, pos0, log=None, resume=None):
         """Place from pos0 ([num_nodes, 2], host or device) to the stop. -> dict (reason, iters, start_iters, hpwl,
@@ -399,10 +411,15 @@ class Placer(object):
             self.kp.copy_(torch.tensor([gam, lam, lam, alpha, coef], dtype=torch.float32))
             self.best.copy_(self.V[cur])
         logged = it0 // o.log_freq
+        left = None
         while True:
-            self._replay(native.PHASE_DENSITY)
+            if left is not None and left < self.check_every:
+                self._passes(native.PHASE_DENSITY, left)         # up to the predicted stop, eagerly
+            else:
+                self._replay(native.PHASE_DENSITY)
             self.sync()
             Sh = self.S.cpu().numpy()
+            left = self._passes_left(Sh)
             it = int(Sh[SK["loop_it"]])
             if log and it // o.log_freq > logged:
                 logged = it // o.log_freq
