@@ -187,6 +187,9 @@ class Placer(object):
         for k in range(2):
             pl.u[k], pl.v[k], pl.g[k] = self._p(self.U[k]), self._p(self.V[k]), self._p(self.G[k])
         self.best = z((n, 2), torch.float32)
+        # pinned host copies of the state (two, alternating) and their events, for the host's polls
+        self._s_host = [(torch.zeros(len(S_FIELDS), dtype=torch.float64).pin_memory(), torch.cuda.Event())
+                        for _ in range(2)]
         self.cur = z((1,), torch.int32)
         self.S = z((len(S_FIELDS),), torch.float64)
         self.T = z((T_SIZE,), torch.float64)
@@ -411,15 +414,34 @@ class Placer(object):
             self.kp.copy_(torch.tensor([gam, lam, lam, alpha, coef], dtype=torch.float32))
             self.best.copy_(self.V[cur])
         logged = it0 // o.log_freq
-        left = None
-        while True:
-            if left is not None and left < self.check_every:
-                self._passes(native.PHASE_DENSITY, left)         # up to the predicted stop, eagerly
-            else:
+        # Batches of passes, each followed by an asynchronous copy of the state into pinned memory. While no stop can
+        # come within two batches, the next batch is queued before the host waits for the state of the last one, so
+        # the GPU does not idle through the poll; near a predictable stop the host runs exactly the passes left.
+        inflight, launched = [], [0]
+
+        def launch(k):
+            if k is None:
                 self._replay(native.PHASE_DENSITY)
-            self.sync()
-            Sh = self.S.cpu().numpy()
+            else:
+                self._passes(native.PHASE_DENSITY, k)             # up to the predicted stop, eagerly
+            buf, ev = self._s_host[launched[0] % 2]               # (at most two batches are in flight)
+            launched[0] += 1
+            with torch.cuda.stream(self.stream):
+                buf.copy_(self.S, non_blocking=True)
+                ev.record(self.stream)
+            inflight.append((buf, ev))
+
+        left = None
+        launch(None)
+        while True:
+            if (left is None or left >= 2 * self.check_every) and len(inflight) < 2:
+                launch(None)
+            sbuf, ev = inflight.pop(0)
+            ev.synchronize()
+            Sh = sbuf.numpy().copy()
             left = self._passes_left(Sh)
+            if not Sh[SK["stop"]] and not inflight:
+                launch(None if left >= self.check_every else left)
             it = int(Sh[SK["loop_it"]])
             if log and it // o.log_freq > logged:
                 logged = it // o.log_freq
@@ -427,7 +449,7 @@ class Placer(object):
                     % (it, Sh[SK["res_hpwl"]], Sh[SK["res_ovf"]], Sh[SK["lam"]], Sh[SK["gam"]]))
             if Sh[SK["stop"]]:
                 break
-        native.call("gp103_finish", self._ref, self.stream.cuda_stream)
+        native.call("gp103_finish", self._ref, self.stream.cuda_stream)     # (after any batch still queued)
         self.sync()
         Sh = self.S.cpu().numpy()
         cur = int(self.cur.cpu())
