@@ -27,6 +27,7 @@ SK = {n: i for i, n in enumerate(S_FIELDS)}
 REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handover"}
 
 
+START_EVERY = 4        # passes per poll of the wirelength-only start
 SHORT_NET = 8          # nets of up to this many pins are done one per thread (WA_REG of the kernel)
 MID_NET = 32           # nets of up to this many pins (and more than SHORT_NET) are done by 8 lanes each
 
@@ -258,15 +259,18 @@ class Placer(object):
                 native.call("gp103_pass", self._ref, flags, s)
 
     def _replay(self, phase):
+        # the wirelength-only start ends after ~10 passes: it polls every START_EVERY passes, the density phase every
+        # check_every
+        k = self.check_every if phase == native.PHASE_DENSITY else min(START_EVERY, self.check_every)
         if not self.use_graphs:
-            self._passes(phase, self.check_every)
+            self._passes(phase, k)
             return
         g = self._graphs.get(phase)
         if g is None:
             g = torch.cuda.CUDAGraph()
             before = native.launch_count()
             with torch.cuda.graph(g, stream=self.stream):
-                self._passes(phase, self.check_every)
+                self._passes(phase, k)
             per = native.launch_count() - before
             self._captured += per
             self._graphs[phase] = (g, per)
