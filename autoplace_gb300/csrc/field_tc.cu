@@ -446,24 +446,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     st_shared_v4(sbase + chunk(2 * (BN / 64) + g, c & 7), *(const float4*)tc);
                 }
             } else if (F16) {
-                // Kx = K Wx, Ky = K Wy as below, each row's 64 columns scaled by its own power of two (the largest
-                // magnitude first, then the same products again, split); boxes 0-1: the terms of Kx, 2-3: of Ky
-                auto kxy = [&](int i, float& kx, float& ky) {
-                    const float4 wc = wsh[i];
-                    const float t = wr.x + wc.x;
-                    const float rr = t > 0.f ? recip(t) : 0.f;
-                    kx = r[i] * (wr.y * wc.z * rr);
-                    ky = r[i] * (wc.y * wr.z * rr);
-                };
-                float mxx = 0.f, mxy = 0.f;
-#pragma unroll
+                // Kx = K Wx, Ky = K Wy as below, each row's 64 columns scaled by a power of two taken from an upper
+                // bound of the row's magnitudes (a scale only has to keep the largest value under 2^15; a bound a
+                // few thousand times too large still leaves it above 2^2, where float16 loses nothing that matters),
+                // so that every product is formed once: |Kx| <= max|K| (s kx_p / bin_x) max w_q / t_min, |Ky| <=
+                // max|K| w_p max(s ky_q / bin_x) / t_min, t_min the smallest kx_p^2 + ky_q^2 > 0 of the row in this
+                // tile (the term with t = 0 is 0). Boxes 0-1: the terms of Kx, 2-3: of Ky.
+                float cmin = INFINITY, cminpos = INFINITY, zmax = 0.f, ymax = 0.f;
+#pragma unroll 8
                 for (int i = 0; i < BN; i++) {
-                    float kx, ky;
-                    kxy(i, kx, ky);
-                    mxx = fmaxf(mxx, fabsf(kx));
-                    mxy = fmaxf(mxy, fabsf(ky));
+                    const float4 wc = wsh[i];
+                    cmin = fminf(cmin, wc.x);
+                    if (wc.x > 0.f) cminpos = fminf(cminpos, wc.x);
+                    zmax = fmaxf(zmax, wc.z);
+                    ymax = fmaxf(ymax, wc.y);
                 }
-                const int exx = f16_chunk_exp(mxx), exy = f16_chunk_exp(mxy);
+                float mr = 0.f;
+#pragma unroll
+                for (int i = 0; i < BN; i++) mr = fmaxf(mr, fabsf(r[i]));
+                const float tmin = wr.x > 0.f ? wr.x + cmin : cminpos;
+                const float rt = tmin > 0.f && tmin < INFINITY ? recip(tmin) : 0.f;
+                const int exx = f16_chunk_exp(mr * (wr.y * zmax) * rt), exy = f16_chunk_exp(mr * (ymax * wr.z) * rt);
                 const float scx = __int_as_float((127 + exx) << 23), scy = __int_as_float((127 + exy) << 23);
                 P.o_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exx;
                 P.o2_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exy;
@@ -472,10 +475,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     __align__(16) __half xa[8], xb[8], ya[8], yb[8];
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
-                        float kx, ky;
-                        kxy(8 * c + i, kx, ky);
-                        split2h(kx * scx, xa[i], xb[i]);
-                        split2h(ky * scy, ya[i], yb[i]);
+                        const float4 wc = wsh[8 * c + i];
+                        const float t = wr.x + wc.x;
+                        const float rr = t > 0.f ? recip(t) : 0.f;
+                        split2h(r[8 * c + i] * (wr.y * wc.z * rr) * scx, xa[i], xb[i]);
+                        split2h(r[8 * c + i] * (wc.y * wr.z * rr) * scy, ya[i], yb[i]);
                     }
                     st_shared_v4(sbase + chunk(0, c), *(const float4*)xa);
                     st_shared_v4(sbase + chunk(1, c), *(const float4*)xb);
