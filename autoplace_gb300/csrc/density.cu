@@ -19,8 +19,9 @@ namespace gp103 {
 // charges there and then adds every non-zero bin to the global map once; otherwise it adds each charge to the global
 // map directly (64-bit atomics in L2).
 constexpr int SCAT_THREADS = 256;
-constexpr int SCAT_PER_THREAD = 2;
-constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;
+constexpr int SCAT_PER_THREAD = 3;
+constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;   // 768 nodes (measured: 512 and 1024 are slower)
+static_assert((long long)SCAT_CHUNK << 17 < (1LL << 32), "the shared-memory charge words could wrap");
 constexpr int SCAT_SMEM_BINS = 3072;      // 2 x 12 KB of 32-bit words
 constexpr float TWO32 = 4294967296.f, TWO33 = 8589934592.f, TWO_M32 = 2.3283064365386963e-10f;
 
@@ -31,7 +32,7 @@ __device__ __forceinline__ void red_shared(unsigned int* a, unsigned int v) {
 // Where a block's charges go. A charge is v = float(wx * oy) * 2^32 (the scaling is exact), truncated to an integer
 // q. In shared memory q < 2^33 is kept as two 32-bit sums: its low 16 bits in lo[b], the rest in hi[b], by adds
 // whose old values nobody reads. A block adds at most SCAT_CHUNK charges to a bin (one per node), so neither word
-// can wrap (1024 x 2^16, 1024 x 2^17 < 2^32) and the bin's sum is hi * 2^16 + lo exactly. Larger charges (only
+// can wrap (SCAT_CHUNK x 2^17 < 2^32, checked below) and the bin's sum is hi * 2^16 + lo exactly. Larger charges (only
 // from ratios above 1), infinities and NaNs take the exact 64-bit conversion and a global atomic.
 struct Tally {
     unsigned int* lo;
@@ -490,7 +491,7 @@ int launch_gather_mirror(const float* pos, const float* size, const float* ratio
 // memory latencies per node rather than one per bin and per pin.
 constexpr int GATHER_PINS = 8;
 
-__global__ void __launch_bounds__(256) gather_kernel(GatherJob j) {
+__global__ void __launch_bounds__(256, 5) gather_kernel(GatherJob j) {      // 48 registers: 5 blocks per SM
     pdl_wait();
     if (j.npre > 0 && blockIdx.x == 0) {                 // the earlier kernels' totals, off the critical path
         for (int i = 0; i < j.npre; i++) {
