@@ -18,9 +18,9 @@ namespace gp103 {
 // fillers. If the bins its nodes touch fit in shared memory (bounding box <= SCAT_SMEM_BINS), the block sums its
 // charges there and then adds every non-zero bin to the global map once; otherwise it adds each charge to the global
 // map directly (64-bit atomics in L2).
-constexpr int SCAT_THREADS = 256;
-constexpr int SCAT_PER_THREAD = 3;
-constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;   // 768 nodes (measured: 512 and 1024 are slower)
+constexpr int SCAT_THREADS = 384;
+constexpr int SCAT_PER_THREAD = 2;
+constexpr int SCAT_CHUNK = SCAT_THREADS * SCAT_PER_THREAD;   // 768 nodes (measured: 512 and 1024 nodes, and 256 x 3 or 128 x 6 threads x nodes, are slower)
 static_assert((long long)SCAT_CHUNK << 17 < (1LL << 32), "the shared-memory charge words could wrap");
 constexpr int SCAT_SMEM_BINS = 3072;      // 2 x 12 KB of 32-bit words
 constexpr float TWO32 = 4294967296.f, TWO33 = 8589934592.f, TWO_M32 = 2.3283064365386963e-10f;
