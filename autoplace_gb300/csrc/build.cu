@@ -3,7 +3,7 @@
 // Input: the optimised pin set as AutoPlace builds it (Wirelength._pin_set, src/core/wa_wirelength_hpwl.py:38-46):
 // pins grouped by net (net_start, cell per pin with num_mov for a fixed pin, offsets) and the pins in cell order
 // (cell_pin). Output: the same nets reordered for the WA kernels (short nets by class of degree 2 / 3 / 4-8, each
-// class by the net's lowest cell, then the nets of 9-32 pins and the longer ones, likewise), their pins moved with them, and for every pin its position
+// class by the net's lowest cell, then the nets of 9-16 pins and the longer ones, likewise), their pins moved with them, and for every pin its position
 // in cell order (pin_slot), where the WA kernels write its gradient. The order is exactly a stable sort of the nets
 // by (class, lowest cell): a counting sort over the keys, ties put back in net order, so the result is the same
 // on every run.
@@ -13,7 +13,7 @@
 namespace gp103 {
 
 constexpr int NO_SHORT = 8;               // nets of up to 8 pins are short (one thread each in the WA kernels)
-constexpr int NO_MID = 32;                // nets of 9 .. 32 pins: 8 lanes each; longer: a warp each
+constexpr int NO_MID = 16;                // nets of 9 .. 16 pins: 4 lanes each; longer: a warp each
 constexpr int NO_CLASSES = 5;
 // SCAN_TILE, SCAN_MAX_TILES: kernels.cuh
 
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) pin_slot_kernel(const int* cell_pin, cons
         slot[newpos[cell_pin[k]]] = k;
 }
 
-// split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 32 pins (class 4),
+// split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 16 pins (class 4),
 // split[2] = nets of 2 pins (class 0), split[3] = nets of up to 3 pins (class 1)
 __global__ void net_split_kernel(const int* start, int stride, int num_nets, int keys, int* split) {
     pdl_wait();

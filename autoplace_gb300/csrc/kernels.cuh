@@ -41,7 +41,7 @@ struct WaJob {
     const int* pin_cell; const float2* pin_off; const int* net_start;
     int num_nets, num_mov;
     int split;              // nets [split, num_nets): one warp each; below: 32 per warp (num_nets: any order)
-    int mid;                // nets [split, mid): 9 .. 32 pins, 8 lanes each (mid = split: none)
+    int mid;                // nets [split, mid): 9 .. 16 pins, 4 lanes each (mid = split: none)
     int two, three;         // nets [0, two): 2 pins, [two, three): 3 pins, pins from 0 in net order (three = 0: none)
     const int* slot;        // pin p's gradient goes to pin_grad[slot[p]] (null: pin_grad[p])
     const float* gamma;

@@ -293,9 +293,9 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
     }
 }
 
-// Long nets [split, num_nets): nets [split, mid) (9 .. 32 pins) by groups of 8 lanes, four per warp item; nets
+// Long nets [split, num_nets): nets [split, mid) (9 .. 16 pins) by groups of 4 lanes, eight per warp item; nets
 // [mid, num_nets) one per warp.
-constexpr int WA_GROUP = 8;
+constexpr int WA_GROUP = 4;
 
 __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
     pdl_wait();
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ Wa
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const long long chunks = (j.split + 31) / 32;
-    const long long longs = (j.mid - j.split + 3) / 4 + (j.num_nets - j.mid);     // warp items of the long kernel
+    const long long longs = (j.mid - j.split + 32 / WA_GROUP - 1) / (32 / WA_GROUP) + (j.num_nets - j.mid);   // warp items
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
     static const int res_short = resident_blocks(wa_short_kernel<false>, 256);
     static const int res_long = resident_blocks(wa_long_kernel, 256);

@@ -29,7 +29,7 @@ REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handov
 
 START_EVERY = 4        # passes per poll of the wirelength-only start
 SHORT_NET = 8          # nets of up to this many pins are done one per thread (WA_REG of the kernel)
-MID_NET = 32           # nets of up to this many pins (and more than SHORT_NET) are done by 8 lanes each
+MID_NET = 16           # nets of up to this many pins (and more than SHORT_NET) are done by 4 lanes each
 
 
 def net_order(net_start, cell32, cell_pin):

@@ -174,7 +174,7 @@ typedef struct {
      * it, the others only read it), order_counts [2048] (zero), order_cursor [2048]. Any permutation gives the same
      * density map; a recent spatial one gives a faster scatter. */
     int* order; int* order_counts; int* order_cursor;
-    /* nets [net_split, net_mid) have 9 to 32 pins: eight lanes each, four nets per warp (net_mid = 0: none, every
+    /* nets [net_split, net_mid) have 9 to 16 pins: four lanes each, eight nets per warp (net_mid = 0: none, every
      * long net takes a warp) */
     int net_mid;
     /* nets [0, net_two) have 2 pins and nets [net_two, net_three) 3 pins, their pins from 0 on in net order (the
@@ -236,11 +236,11 @@ int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
 /* Set-up of the fused path on the device: the nets of the optimised pin set (Wirelength._pin_set,
  * src/core/wa_wirelength_hpwl.py:38-46; net_start [num_nets + 1], pin_cell [num_pins] with num_mov for a fixed pin,
  * pin_off [num_pins, 2], cell_pin [num_pins] = the pins in cell order) reordered for the WA kernels: a stable sort
- * of the nets by (class, lowest cell), classes 2 pins / 3 pins / 4-8 pins / 9-32 pins / longer, pins moving with
+ * of the nets by (class, lowest cell), classes 2 pins / 3 pins / 4-8 pins / 9-16 pins / longer, pins moving with
  * their nets.
  * Writes net_start_out, pin_cell_out, pin_off_out (the plan's net_start, pin_cell, pin_off), pin_slot (each new
  * pin's position in cell order: the plan's pin_slot) and split (device int [4]: the plan's net_split, net_mid,
- * net_two and net_three = numbers of nets of up to 8, up to 32, 2 and up to 3 pins). scratch: gp103_net_order_scratch(...) bytes. No counterpart in the reference, whose kernel
+ * net_two and net_three = numbers of nets of up to 8, up to 16, 2 and up to 3 pins). scratch: gp103_net_order_scratch(...) bytes. No counterpart in the reference, whose kernel
  * reads the nets in their original order. GP103_ERR_TOO_LARGE beyond 5 (num_mov + 1) > 16,777,216. */
 size_t gp103_net_order_scratch(int num_nets, int num_pins, int num_mov);
 int gp103_net_order(const int* net_start, const int* pin_cell, const float* pin_off, const int* cell_pin,
