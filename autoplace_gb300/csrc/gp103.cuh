@@ -163,47 +163,6 @@ __device__ __forceinline__ void grid_sum(float (&v)[K], const Reduce& r) {
     grid_sum<K>(v, r, (int)gridDim.x, (int)blockIdx.x);
 }
 
-// Consumer side (every thread of the block calls it): N totals at once (value k[i] of reduction r[i]), returned to
-// every thread; one sweep over the partials and one block-wide tree.
-// A thread adds the partials b, b + T, b + 2T, ... (T = block size) of each reduction in that order; the loads of
-// four steps and of all N reductions are issued together (one memory latency per four steps, not one per partial).
-template <int N>
-__device__ __forceinline__ void block_totals(const Reduce (&r)[N], const int (&k)[N], double (&out)[N]) {
-    __shared__ double sh[N * 32];
-    __shared__ double tot[N];
-    constexpr int U = 4;
-    double v[N];
-    int n[N], nmax = 0;
-    const double* p[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        v[i] = 0.0;
-        n[i] = *r[i].count;
-        nmax = max(nmax, n[i]);
-        p[i] = r[i].partials + (size_t)k[i] * MAX_BLOCKS;
-    }
-    const int T = blockDim.x;
-    for (int b = threadIdx.x; b < nmax; b += U * T) {
-        double x[N][U];
-#pragma unroll
-        for (int i = 0; i < N; i++)
-#pragma unroll
-            for (int u = 0; u < U; u++) x[i][u] = b + u * T < n[i] ? p[i][b + u * T] : 0.0;
-#pragma unroll
-        for (int i = 0; i < N; i++)
-#pragma unroll
-            for (int u = 0; u < U; u++)
-                if (b + u * T < n[i]) v[i] += x[i][u];
-    }
-    block_sum<N>(v, sh);
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int i = 0; i < N; i++) tot[i] = v[i];
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < N; i++) out[i] = tot[i];
-    __syncthreads();
-}
 
 // Consumer side (every thread of the block calls it): value k of a reduction, returned to every thread.
 __device__ __forceinline__ double block_total(const Reduce& r, int k) {

@@ -126,7 +126,7 @@ struct GatherJob {
     const float2* gref_a; const float2* gref_b;     // null: no distance
     Reduce red;                 // (|g - gref|^2, L1 of g over the cells)
     // npre > 0: block 0 does no gathering: it sums the partials of earlier kernels, pre[i] value pre_k[i], in the
-    // order block_totals sums them (the same bits), into pre_out[i], while the other blocks gather
+    // order block_total sums them (the order of every consumer), into pre_out[i], while the other blocks gather
     Reduce pre[4];
     int pre_k[4];
     int npre;
