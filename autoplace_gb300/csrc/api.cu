@@ -314,6 +314,7 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
         if (p->field_mode == GP103_FIELD_F16X3) {
             pj.terms = 2;
             pj.exps = (signed char*)((char*)p->field_work + L.e_a);
+            pj.fold = L.fold ? 1 : 0;
         }
     }
     pj.red = reduce_slot(p->red, p->counters, R_OVF);

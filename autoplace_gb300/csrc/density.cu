@@ -325,6 +325,80 @@ __device__ __forceinline__ void split_bf16(float r, int terms, __nv_bfloat16* t0
     if (terms > 2) t2[at] = __float2bfloat16_rn(__fsub_rn(rem, __bfloat162float(b)));
 }
 
+// f16x3 folded (j.fold, with exps and the filler plane; nby a multiple of 128): as the float16 path below, but the
+// density goes out folded about the middle of y for the folded first transform of the field: s = rho(y) +
+// rho(nby-1-y) and t = rho(y) - rho(nby-1-y) for y < nby/2, each [nbx][nby/2] as two float16 terms with a
+// power-of-two scale per 64-value chunk of a row: planes s0, s1, t0, t1 of nbx * nby/2 values from j.t0 on; exponents
+// of s at exps[(y / 64) * nbx + x], of t behind them. A thread takes the quad y .. y+3 of a row's lower half and its
+// mirror nby-4-y .. nby-1-y (the mirror of y + k is the mirror quad's element 3 - k); a 64-value chunk is 16
+// consecutive threads, half a warp (the loop keeps whole warps: nbx * nby / 8 is a multiple of 32).
+__device__ __forceinline__ void post_fold(const PostJob& j, int bid, int nblk, float& ov) {
+    const int nb = j.nbx * j.nby, hq = j.nby / 8, hy = j.nby / 2;
+    const size_t hn = (size_t)j.nbx * hy;
+    __half* out = (__half*)j.t0;
+    ulonglong2* mov_map = (ulonglong2*)j.map;
+    ulonglong2* fill = (ulonglong2*)(j.map + nb);
+    for (int qp = bid * blockDim.x + threadIdx.x; qp < nb / 8; qp += nblk * blockDim.x) {
+        const int x = qp / hq, y = 4 * (qp - x * hq);
+        float r[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = (x * j.nby + (h ? j.nby - 4 - y : y)) >> 2;      // the quad (of 4 bins)
+            const ulonglong2 ma = mov_map[2 * q], mb = mov_map[2 * q + 1];
+            const ulonglong2 fa = fill[2 * q], fb = fill[2 * q + 1];
+            const float4 fx = *(const float4*)(j.fixed + 4 * q);
+            float mov[4];
+            mov[0] = __fadd_rn(unfixed32(ma.x), fx.x);
+            mov[1] = __fadd_rn(unfixed32(ma.y), fx.y);
+            mov[2] = __fadd_rn(unfixed32(mb.x), fx.z);
+            mov[3] = __fadd_rn(unfixed32(mb.y), fx.w);
+#pragma unroll
+            for (int k = 0; k < 4; k++) ov += fmaxf(__fsub_rn(mov[k], j.target), 0.f);
+            r[h][0] = __fadd_rn(mov[0], unfixed32(fa.x));
+            r[h][1] = __fadd_rn(mov[1], unfixed32(fa.y));
+            r[h][2] = __fadd_rn(mov[2], unfixed32(fb.x));
+            r[h][3] = __fadd_rn(mov[3], unfixed32(fb.y));
+            const ulonglong2 zero = make_ulonglong2(0ull, 0ull);
+            mov_map[2 * q] = zero;
+            mov_map[2 * q + 1] = zero;
+            fill[2 * q] = zero;
+            fill[2 * q + 1] = zero;
+        }
+        float sv[4], tv[4], ms = 0.f, mt = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            sv[k] = __fadd_rn(r[0][k], r[1][3 - k]);
+            tv[k] = __fsub_rn(r[0][k], r[1][3 - k]);
+            ms = fmaxf(ms, fabsf(sv[k]));
+            mt = fmaxf(mt, fabsf(tv[k]));
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            ms = fmaxf(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+            mt = fmaxf(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+        }
+        const int es = f16_chunk_exp(ms), et = f16_chunk_exp(mt);
+        const float scs = __int_as_float((127 + es) << 23), sct = __int_as_float((127 + et) << 23);
+        __align__(8) __half h[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float xs = sv[k] * scs, xt = tv[k] * sct;
+            h[0][k] = __float2half_rn(xs);
+            h[1][k] = __float2half_rn(__fsub_rn(xs, __half2float(h[0][k])));
+            h[2][k] = __float2half_rn(xt);
+            h[3][k] = __float2half_rn(__fsub_rn(xt, __half2float(h[2][k])));
+        }
+        const size_t at = (size_t)x * hy + y;
+#pragma unroll
+        for (int t = 0; t < 4; t++) *(uint2*)(out + t * hn + at) = *(const uint2*)h[t];
+        if ((threadIdx.x & 15) == 0) {
+            const size_t k = (size_t)(y >> 6) * j.nbx + x;
+            j.exps[k] = (signed char)es;
+            j.exps[(size_t)(hy >> 6) * j.nbx + k] = (signed char)et;
+        }
+    }
+}
+
 // EXACT: float64 per-thread partials of the overflow (the evaluators); a template argument, so that the hot path
 // carries no float64 instruction at all (a runtime flag gets both sides if-converted).
 template <bool EXACT>
@@ -337,9 +411,10 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
     const int nb = j.nbx * j.nby;
     float ov = 0.f;             // per-thread partial of the hot path (a few bins)
     double ovd = 0.0;           // the same in float64 for an exact evaluation (j.exact)
+    if (!EXACT && j.fold) post_fold(j, bid, nblk, ov);
     // four bins per thread and iteration: 32-byte map loads / stores, 8-byte stores of each bf16 term plane (a bin
     // count that is a multiple of 4 keeps every plane aligned; any other takes the scalar loop below for every bin)
-    const int quads = (nb & 3) ? 0 : nb >> 2;
+    const int quads = (nb & 3) || (!EXACT && j.fold) ? 0 : nb >> 2;
     for (int q = bid * blockDim.x + threadIdx.x; q < quads; q += nblk * blockDim.x) {
         const int b = 4 * q;
         const ulonglong2 m0a = ((const ulonglong2*)j.map)[2 * q], m0b = ((const ulonglong2*)j.map)[2 * q + 1];

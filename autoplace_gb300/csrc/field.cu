@@ -39,14 +39,25 @@ __device__ __forceinline__ double trig(int kind, int p, int u, int n) {
 
 // what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]; f16: two float16 terms of
 // the value times 2^F16_CONST instead of three bf16 terms
+// The frequency of position c in the folded order of the coefficients (f16x3): the even frequencies 0, 2, .. first,
+// then the odd ones 1, 3, ..
+__device__ __forceinline__ int folded_freq(int c, int n) { return c < n / 2 ? 2 * c : 2 * (c - n / 2) + 1; }
+
+// fold = 1 / 2: the (n/2) x (n/2) matrix of the even / odd frequencies of C over the lower half of the positions,
+// F[r][u] = C[2r (+1)][u], u < n/2 (the forward transform of a folded input, below); pcols (what 2, 3): the
+// frequency index of the transposed matrix in the folded order, T[m][c] = C[folded_freq(c)][m]
 __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t0, __nv_bfloat16* t1,
-                                   __nv_bfloat16* t2, size_t plane, int f16) {
+                                   __nv_bfloat16* t2, size_t plane, int f16, int fold, int pcols) {
     pdl_wait();
-    const size_t total = (size_t)n * n;
+    const int m = fold ? n / 2 : n;                      // the matrix is m x m
+    const size_t total = (size_t)m * m;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(e / n), col = (int)(e % n);
+        const int r = (int)(e / m), col = (int)(e % m);
         const int kind = what & 1;
-        const double v = what < 2 ? trig(kind, r, col, n) : trig(kind, col, r, n);
+        double v;
+        if (fold) v = trig(0, 2 * r + fold - 1, col, n);
+        else if (what < 2) v = trig(kind, r, col, n);
+        else v = trig(kind, pcols ? folded_freq(col, n) : col, r, n);
         if (f32) f32[e] = (float)v;
         if (t0 && f16) {
             const double w = ldexp(v, F16_CONST);
@@ -83,12 +94,14 @@ __global__ void weight_kernel(int nbx, int nby, double bx, double by, float* wx,
 
 // The separable parts of the weights, for epilogues that form them on the fly: per row p (kx^2, s kx / bin_x, w_p)
 // and per column q (ky^2, s ky / bin_x, w_q), s = 2 / (nbx nby); Wx = (s kx / bin_x) w_q / (kx^2 + ky^2).
-__global__ void weight_table_kernel(int n, int nbx, int nby, double bin, double bx, float4* tab) {
+// (perm: entry c for the frequency folded_freq(c), the column order of the folded coefficients)
+__global__ void weight_table_kernel(int n, int nbx, int nby, double bin, double bx, float4* tab, int perm) {
     pdl_wait();
     const double pi = 3.14159265358979323846;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int p = perm ? folded_freq(c, n) : c;
         const double k = pi * p / (n * bin), s = 2.0 / ((double)nbx * nby);
-        tab[p] = make_float4((float)(k * k), (float)(s * k / bx), p == 0 ? 1.f : 2.f, 0.f);
+        tab[c] = make_float4((float)(k * k), (float)(s * k / bx), p == 0 ? 1.f : 2.f, 0.f);
     }
 }
 
@@ -97,6 +110,7 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
     L.nbx = nbx;
     L.nby = nby;
     L.mode = mode;
+    L.fold = mode == GP103_FIELD_F16X3 && nby % 256 == 0;     // each half a whole number of 128-row tiles
     const size_t xx = (size_t)nbx * nbx, yy = (size_t)nby * nby, xy = (size_t)nbx * nby;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 1023) & ~(size_t)1023; return at; };
@@ -120,15 +134,20 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
 int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
     char* c = (char*)cbuf;
     const bool fp32 = L.mode == GP103_FIELD_FP32;
-    struct M { int what, n; size_t off; } mats[6] = {
-        {0, L.nbx, L.c_cx}, {0, L.nby, L.c_cy}, {2, L.nby, L.c_cyt}, {3, L.nbx, L.c_sxt}, {3, L.nby, L.c_syt},
-        {2, L.nbx, L.c_cxt}};
+    // folded (f16x3): Cy as its even- and odd-frequency halves over the lower half of the positions (two 2-term
+    // matrices of (nby/2)^2, one after the other), CyT and SyT with their frequency columns in the folded order
+    const int fold = L.fold ? 1 : 0;
+    const size_t half_cy = (size_t)(L.nby / 2) * (L.nby / 2) * 2 * 2;       // bytes of one folded half (2 terms)
+    struct M { int what, n; size_t off; int fold, pcols; } mats[7] = {
+        {0, L.nbx, L.c_cx, 0, 0}, {0, L.nby, L.c_cy, fold, 0}, {0, L.nby, L.c_cy + half_cy, 2, 0},
+        {2, L.nby, L.c_cyt, 0, fold}, {3, L.nbx, L.c_sxt, 0, 0}, {3, L.nby, L.c_syt, 0, fold}, {2, L.nbx, L.c_cxt, 0, 0}};
     for (auto& m : mats) {
-        const size_t plane = (size_t)m.n * m.n;
+        if (m.fold == 2 && !fold) continue;                  // the odd half exists only in the folded layout
+        const size_t plane = m.fold ? (size_t)(m.n / 2) * (m.n / 2) : (size_t)m.n * m.n;
         float* f = fp32 ? (float*)(c + m.off) : nullptr;
         __nv_bfloat16* t0 = fp32 ? nullptr : (__nv_bfloat16*)(c + m.off);
         if (launch_k(trig_matrix_kernel, dim3(grid_for(plane, 256, 8)), dim3(256), 0, s, m.what, m.n, f, t0, t0 ? t0 + plane : nullptr,
-                     t0 ? t0 + 2 * plane : nullptr, plane, (int)(L.mode == GP103_FIELD_F16X3)) != cudaSuccess)
+                     t0 ? t0 + 2 * plane : nullptr, plane, (int)(L.mode == GP103_FIELD_F16X3), m.fold, m.pcols) != cudaSuccess)
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
@@ -136,10 +155,10 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
                                                                             (float*)(c + L.c_wx), (float*)(c + L.c_wy)) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     if (launch_k(weight_table_kernel, dim3(grid_for(L.nbx, 256, 8)), dim3(256), 0, s, L.nbx, L.nbx, L.nby, L.bx, L.bx,
-                                                                 (float4*)(c + L.c_wrow)) != cudaSuccess) return GP103_ERR_CUDA;
+                                                                 (float4*)(c + L.c_wrow), 0) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     if (launch_k(weight_table_kernel, dim3(grid_for(L.nby, 256, 8)), dim3(256), 0, s, L.nby, L.nbx, L.nby, L.by, L.bx,
-                                                                 (float4*)(c + L.c_wcol)) != cudaSuccess) return GP103_ERR_CUDA;
+                                                                 (float4*)(c + L.c_wcol), fold) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

@@ -9,8 +9,13 @@ namespace gp103 {
 // (GP103_FIELD_FP32) or up to three 16-bit planes back to back (tensor-core modes: bf16x6 three bf16 terms, bf16x3
 // two of them, f16x3 two float16 terms). In f16x3 every data operand also has a power-of-two scale per row and
 // 64-wide chunk of K: x_e[kb][n] = e, the terms hold x * 2^e (the constant matrices are scaled by 2^F16_CONST).
+// fold (f16x3, nby a multiple of 256): the first transform (along y) takes the density folded about the middle of y, s = a(y) + a(nby-1-y)
+// and d = a(y) - a(nby-1-y) for y < nby/2, and gives the even and odd frequencies separately (C[p][nby-1-y] =
+// (-1)^p C[p][y]): half the products. Its output rows, and every later index of that frequency, are in the folded
+// order (even frequencies first, then odd), which the constants that meet them follow.
 struct FieldLayout {
     int nbx, nby, mode;
+    bool fold;
     double bx, by;
     size_t c_cx, c_cy, c_cyt, c_sxt, c_syt, c_cxt, c_wx, c_wy, c_wrow, c_wcol, const_bytes;
     size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err;

@@ -30,6 +30,8 @@ constexpr int EPI_BOX = 128 * 128;                               // an epilogue 
 struct TcProblem {
     int M, N, K;
     int epi;
+    int M_out, m_out;            // the outputs (terms, float32 plane, exponents) have M_out rows; this problem's start
+                                 // at row m_out (two problems of one launch can fill one output)
     __nv_bfloat16* o_terms;      // EPI_SPLIT: [3][M][N]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
     __nv_bfloat16* o2_terms;
     float* out_f32;              // EPI_PLAIN: [M][N]
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     for (int i = 0; i < 64; i++) mx = fmaxf(mx, fabsf(r[64 * g + i]));
                     const int e = f16_chunk_exp(mx);
                     const float sc = __int_as_float((127 + e) << 23);
-                    P.o_exp[(size_t)(n0 / 64 + g) * P.M + row] = (signed char)e;
+                    P.o_exp[(size_t)(n0 / 64 + g) * P.M_out + P.m_out + row] = (signed char)e;
 #pragma unroll
                     for (int c = 0; c < 8; c++) {
                         __align__(16) __half ta[8], tb[8];
@@ -468,8 +470,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const float rt = tmin > 0.f && tmin < INFINITY ? recip(tmin) : 0.f;
                 const int exx = f16_chunk_exp(mr * (wr.y * zmax) * rt), exy = f16_chunk_exp(mr * (ymax * wr.z) * rt);
                 const float scx = __int_as_float((127 + exx) << 23), scy = __int_as_float((127 + exy) << 23);
-                P.o_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exx;
-                P.o2_exp[(size_t)(n0 / 64) * P.M + row] = (signed char)exy;
+                P.o_exp[(size_t)(n0 / 64) * P.M_out + P.m_out + row] = (signed char)exx;
+                P.o2_exp[(size_t)(n0 / 64) * P.M_out + P.m_out + row] = (signed char)exy;
 #pragma unroll
                 for (int c = 0; c < BN / 8; c++) {
                     __align__(16) __half xa[8], xb[8], ya[8], yb[8];
@@ -514,23 +516,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (warp == 2 && lane == 0 && *(volatile int*)err == 0) {
+            const int om0 = m0 + P.m_out;         // the tile's first output row
             const CUtensorMap* mo = z ? &o1a : &o0a;
             const CUtensorMap* mo2 = z ? &o1b : &o0b;
             if (EPI == EPI_PLAIN) {
 #pragma unroll
-                for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, m0);
+                for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, om0);
             } else if (EPI == EPI_SPLIT) {
                 constexpr int OT = F16 ? 2 : 3;                  // output terms
 #pragma unroll
                 for (int t = 0; t < OT; t++)
 #pragma unroll
-                    for (int g = 0; g < BN / 64; g++) tma_store_3d(mo, sbase + (t * (BN / 64) + g) * EPI_BOX, n0 + 64 * g, m0, t);
+                    for (int g = 0; g < BN / 64; g++) tma_store_3d(mo, sbase + (t * (BN / 64) + g) * EPI_BOX, n0 + 64 * g, om0, t);
             } else {
                 constexpr int OT = F16 ? 2 : 3;
 #pragma unroll
                 for (int t = 0; t < OT; t++) {
-                    tma_store_3d(mo, sbase + t * EPI_BOX, n0, m0, t);
-                    tma_store_3d(mo2, sbase + (OT + t) * EPI_BOX, n0, m0, t);
+                    tma_store_3d(mo, sbase + t * EPI_BOX, n0, om0, t);
+                    tma_store_3d(mo2, sbase + (OT + t) * EPI_BOX, n0, om0, t);
                 }
             }
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
@@ -633,11 +636,11 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
         CUtensorMap* ob = &maps[5 + 2 * z];
         bool ok = true;
         if (EPI == EPI_PLAIN) {
-            ok = make_map_f32(oa, o.p.out_f32, o.p.M, o.p.N);
+            ok = make_map_f32(oa, o.p.out_f32, o.p.M_out, o.p.N);
             *ob = *oa;
         } else {
-            ok = make_map(oa, o.p.o_terms, o.p.M, o.p.N, TC_BM, F16);
-            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M, o.p.N, TC_BM, F16);
+            ok = make_map(oa, o.p.o_terms, o.p.M_out, o.p.N, TC_BM, F16);
+            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M_out, o.p.N, TC_BM, F16);
             else *ob = *oa;
         }
         if (!ok) return GP103_ERR_CUDA;
@@ -661,11 +664,12 @@ static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStrea
     return launch_tc_mode<BN, EPI, 1>(ops, nops, err, s);
 }
 
-// One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles. The epilogue is a
-// template argument (every problem of a launch has the same one).
-static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
+// One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles, or 64-column ones
+// (bn = 64: two half-height problems). The epilogue is a template argument (every problem of a launch has the same
+// one).
+static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int bn = 0) {
     const int epi = ops[0].p.epi;
-    if (nops == 1 && epi == EPI_SPLIT) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s);
+    if (epi == EPI_SPLIT && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 1 && epi == EPI_WEIGHT2) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
     if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
@@ -709,6 +713,49 @@ __global__ void split_density_f16_kernel(const float* d, int nbx, int nby, __hal
     }
 }
 
+// f16x3 folded: a float32 density [nbx][nby] folded about the middle of y, s = d(y) + d(nby-1-y) and
+// t = d(y) - d(nby-1-y) for y < nby/2, each [nbx][nby/2] as two float16 terms per 64-value chunk of a row scaled by
+// its own power of two (one warp per chunk of s and the same chunk of t, two values per lane): planes s0, s1, t0, t1
+// of nbx * nby/2 values from `out` on; exponents of s in e[(y / 64) * nbx + x] (y < nby/2), of t behind them.
+__global__ void split_density_fold_kernel(const float* d, int nbx, int nby, __half* out, signed char* e) {
+    pdl_wait();
+    const int lane = threadIdx.x & 31, hy = nby / 2;
+    const long long chunks = (long long)nbx * hy / 64, hn = (long long)nbx * hy;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+        const long long x = (64 * c) / hy;
+        const int y = (int)((64 * c) % hy) + 2 * lane;
+        const float* row = d + x * nby;
+        const float2 lo = *(const float2*)(row + y);
+        const float h0 = row[nby - 1 - y], h1 = row[nby - 2 - y];
+        const float s0 = __fadd_rn(lo.x, h0), s1 = __fadd_rn(lo.y, h1);
+        const float t0 = __fsub_rn(lo.x, h0), t1 = __fsub_rn(lo.y, h1);
+        float ms = fmaxf(fabsf(s0), fabsf(s1)), mt = fmaxf(fabsf(t0), fabsf(t1));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ms = fmaxf(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+            mt = fmaxf(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+        }
+        const int es = f16_chunk_exp(ms), et = f16_chunk_exp(mt);
+        const float scs = __int_as_float((127 + es) << 23), sct = __int_as_float((127 + et) << 23);
+        __half a0, b0, a1, b1;
+        const long long at = x * hy + y;
+        split2h(s0 * scs, a0, b0);
+        split2h(s1 * scs, a1, b1);
+        *(__half2*)(out + at) = __halves2half2(a0, a1);
+        *(__half2*)(out + hn + at) = __halves2half2(b0, b1);
+        split2h(t0 * sct, a0, b0);
+        split2h(t1 * sct, a1, b1);
+        *(__half2*)(out + 2 * hn + at) = __halves2half2(a0, a1);
+        *(__half2*)(out + 3 * hn + at) = __halves2half2(b0, b1);
+        if (lane == 0) {
+            const long long k = (long long)(y / 64) * nbx + x;
+            e[k] = (signed char)es;
+            e[(long long)(hy / 64) * nbx + k] = (signed char)et;
+        }
+    }
+}
+
 int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* density, float* ex, float* ey,
              cudaStream_t s) {
     if (!field_tc_supported(L.nbx, L.nby)) return GP103_ERR_SHAPE;
@@ -720,7 +767,12 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     int st;
     const bool f16 = L.mode == GP103_FIELD_F16X3;
     auto E = [&](size_t off) { return f16 ? (signed char*)(w + off) : (signed char*)nullptr; };
-    if (density && f16) {
+    if (density && L.fold) {
+        if (launch_k(split_density_fold_kernel, dim3(grid_for((size_t)X * Y / 4, 256, 8)), dim3(256), 0, s, density,
+                     X, Y, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    } else if (density && f16) {
         if (launch_k(split_density_f16_kernel, dim3(grid_for((size_t)X * Y / 2, 256, 8)), dim3(256), 0, s, density, X,
                      Y, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
             return GP103_ERR_CUDA;
@@ -732,15 +784,34 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     auto prob = [](int M, int N, int K, int epi) {
         TcProblem p = {};
         p.M = M; p.N = N; p.K = K; p.epi = epi;
+        p.M_out = M;
         return p;
     };
     // 1: Tt = (A Cy^T)^T = Cy A^T: Cy as the row operand, the density as the column operand, so the transposed
-    //    product comes out in rows (no transposing epilogue)
-    TcOp o1 = {B(c, L.c_cy), Y, B(w, L.w_a), X, prob(Y, X, Y, EPI_SPLIT)};
-    o1.p.o_terms = B(w, L.w_tt);
-    o1.p.b_exp = E(L.e_a);
-    o1.p.o_exp = E(L.e_tt);
-    if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
+    //    product comes out in rows (no transposing epilogue); folded (f16x3): rows in the folded frequency order, which
+    //    K's columns, the column weights and the A operands CyT / SyT of step 3 follow
+    if (L.fold) {
+        // folded (f16x3): the even frequencies of the folded sum, rows [0, Y/2) of Tt, and the odd ones of the
+        // folded difference, rows [Y/2, Y): two GEMMs of half the height and half the depth in one launch
+        const int H = Y / 2;
+        const size_t cy_half = (size_t)H * H * 2, a_half = (size_t)X * H * 2;      // elements (2 terms)
+        TcOp o1[2] = {{B(c, L.c_cy), H, B(w, L.w_a), X, prob(H, X, H, EPI_SPLIT)},
+                      {B(c, L.c_cy) + cy_half, H, B(w, L.w_a) + a_half, X, prob(H, X, H, EPI_SPLIT)}};
+        for (int z = 0; z < 2; z++) {
+            o1[z].p.o_terms = B(w, L.w_tt);
+            o1[z].p.M_out = Y;
+            o1[z].p.m_out = z * H;
+            o1[z].p.b_exp = E(L.e_a) + (size_t)z * (H / 64) * X;
+            o1[z].p.o_exp = E(L.e_tt);
+        }
+        if ((st = launch_tc(o1, 2, L.mode, err, s, 64))) return st;
+    } else {
+        TcOp o1 = {B(c, L.c_cy), Y, B(w, L.w_a), X, prob(Y, X, Y, EPI_SPLIT)};
+        o1.p.o_terms = B(w, L.w_tt);
+        o1.p.b_exp = E(L.e_a);
+        o1.p.o_exp = E(L.e_tt);
+        if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
+    }
     // 2: K = Cx T -> Kx, Ky
     TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
     o2.p.o_terms = B(w, L.w_kx);

@@ -101,6 +101,8 @@ struct PostJob {
     int terms;
     signed char* exps;          // non-null: float16 terms (t0, t1 hold __half) of each 64-bin chunk of a row scaled by
                                 // 2^e, e = exps[(y / 64) * nbx + x] (nby a multiple of 64)
+    int fold;                   // with exps (nby a multiple of 128): the terms of the density folded about the middle
+                                // of y (post_fold), for the folded first transform of the field
     int exact;                  // float64 per-thread partials of the sum (evaluators); 0: float32 (hot path)
     Reduce red;                 // sum of the density above the target
 };
