@@ -224,9 +224,13 @@ def kernel_bytes(prob, field="f16x3"):
 
 
 def tc_flops(prob, field):
+    """Tensor-core FLOPs of the field per density pass: six GEMMs of nb^3 (2 nb^3 per product, the mode's products
+    each); f16x3 on a grid of a multiple of 256 bins folds the first transform into two GEMMs of half the height and
+    half the depth, half a GEMM less."""
     nb = prob.force_bin
     terms = {"bf16x6": 6, "bf16x3": 3, "f16x3": 3}.get(field, 0)
-    return 2.0 * nb ** 3 * terms        # per GEMM
+    gemms = 5.5 if field == "f16x3" and nb % 256 == 0 else 6.0
+    return 2.0 * nb ** 3 * terms * gemms
 
 
 def profile_pass(placer):
@@ -268,11 +272,11 @@ def roofline(prob, field, prof, peaks, config="c2"):
         if k in by:     # algorithmic bytes of the whole pass over the kernel's time per pass (all its launches)
             row["gbs"] = round(by[k] / (v["ms_per_pass"] * 1e-3) / 1e9, 1)
         if k == "launch_tc_mode":
-            f = tc_flops(prob, field) * (6.0 / v["launches_per_pass"])
+            f = tc_flops(prob, field) / v["launches_per_pass"]
             row["tflops"] = round(f / (ml * 1e-3) / 1e12, 1)
         table[k] = row
     if name == "launch_tc_mode":
-        f = tc_flops(prob, field) * (6.0 / d["launches_per_pass"])
+        f = tc_flops(prob, field) / d["launches_per_pass"]
         ach = f / (ms_launch * 1e-3) / 1e12
         r = {"kernel": "tc_gemm_kernel", "bound": "tensor", "achieved": round(ach, 1), "peak": tc,
              "unit": "TFLOP/s", "frac": round(ach / tc, 4) if tc else None, "traffic": traffic.get(name),
