@@ -110,7 +110,7 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
     L.nbx = nbx;
     L.nby = nby;
     L.mode = mode;
-    L.fold = mode == GP103_FIELD_F16X3 && nby % 256 == 0;     // each half a whole number of 128-row tiles
+    L.fold = mode == GP103_FIELD_F16X3 && nbx % 256 == 0 && nby % 256 == 0;   // halves of whole 128-row tiles
     const size_t xx = (size_t)nbx * nbx, yy = (size_t)nby * nby, xy = (size_t)nbx * nby;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 1023) & ~(size_t)1023; return at; };
@@ -134,13 +134,16 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
 int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
     char* c = (char*)cbuf;
     const bool fp32 = L.mode == GP103_FIELD_FP32;
-    // folded (f16x3): Cy as its even- and odd-frequency halves over the lower half of the positions (two 2-term
-    // matrices of (nby/2)^2, one after the other), CyT and SyT with their frequency columns in the folded order
+    // folded (f16x3): Cx and Cy as their even- and odd-frequency halves over the lower half of the positions (two
+    // 2-term matrices of (n/2)^2 each, one after the other), the transposed matrices with their frequency columns in
+    // the folded order
     const int fold = L.fold ? 1 : 0;
-    const size_t half_cy = (size_t)(L.nby / 2) * (L.nby / 2) * 2 * 2;       // bytes of one folded half (2 terms)
-    struct M { int what, n; size_t off; int fold, pcols; } mats[7] = {
-        {0, L.nbx, L.c_cx, 0, 0}, {0, L.nby, L.c_cy, fold, 0}, {0, L.nby, L.c_cy + half_cy, 2, 0},
-        {2, L.nby, L.c_cyt, 0, fold}, {3, L.nbx, L.c_sxt, 0, 0}, {3, L.nby, L.c_syt, 0, fold}, {2, L.nbx, L.c_cxt, 0, 0}};
+    const size_t half_cx = (size_t)(L.nbx / 2) * (L.nbx / 2) * 2 * 2;       // bytes of one folded half (2 terms)
+    const size_t half_cy = (size_t)(L.nby / 2) * (L.nby / 2) * 2 * 2;
+    struct M { int what, n; size_t off; int fold, pcols; } mats[8] = {
+        {0, L.nbx, L.c_cx, fold, 0}, {0, L.nbx, L.c_cx + half_cx, 2, 0}, {0, L.nby, L.c_cy, fold, 0},
+        {0, L.nby, L.c_cy + half_cy, 2, 0}, {2, L.nby, L.c_cyt, 0, fold}, {3, L.nbx, L.c_sxt, 0, fold},
+        {3, L.nby, L.c_syt, 0, fold}, {2, L.nbx, L.c_cxt, 0, fold}};
     for (auto& m : mats) {
         if (m.fold == 2 && !fold) continue;                  // the odd half exists only in the folded layout
         const size_t plane = m.fold ? (size_t)(m.n / 2) * (m.n / 2) : (size_t)m.n * m.n;
@@ -155,7 +158,7 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
                                                                             (float*)(c + L.c_wx), (float*)(c + L.c_wy)) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     if (launch_k(weight_table_kernel, dim3(grid_for(L.nbx, 256, 8)), dim3(256), 0, s, L.nbx, L.nbx, L.nby, L.bx, L.bx,
-                                                                 (float4*)(c + L.c_wrow), 0) != cudaSuccess) return GP103_ERR_CUDA;
+                                                                 (float4*)(c + L.c_wrow), fold) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     if (launch_k(weight_table_kernel, dim3(grid_for(L.nby, 256, 8)), dim3(256), 0, s, L.nby, L.nbx, L.nby, L.by, L.bx,
                                                                  (float4*)(c + L.c_wcol), fold) != cudaSuccess) return GP103_ERR_CUDA;

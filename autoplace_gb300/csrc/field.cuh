@@ -9,10 +9,11 @@ namespace gp103 {
 // (GP103_FIELD_FP32) or up to three 16-bit planes back to back (tensor-core modes: bf16x6 three bf16 terms, bf16x3
 // two of them, f16x3 two float16 terms). In f16x3 every data operand also has a power-of-two scale per row and
 // 64-wide chunk of K: x_e[kb][n] = e, the terms hold x * 2^e (the constant matrices are scaled by 2^F16_CONST).
-// fold (f16x3, nby a multiple of 256): the first transform (along y) takes the density folded about the middle of y, s = a(y) + a(nby-1-y)
-// and d = a(y) - a(nby-1-y) for y < nby/2, and gives the even and odd frequencies separately (C[p][nby-1-y] =
-// (-1)^p C[p][y]): half the products. Its output rows, and every later index of that frequency, are in the folded
-// order (even frequencies first, then odd), which the constants that meet them follow.
+// fold (f16x3, nbx and nby multiples of 256): both forward transforms take their input folded about its middle and
+// give the even and odd frequencies separately (C[p][n-1-u] = (-1)^p C[p][u]): half the products of each. The first
+// (along y) takes the density folded about the middle of y, s = a(y) + a(nby-1-y) and d = a(y) - a(nby-1-y) for
+// y < nby/2; its epilogue folds its output about the middle of x for the second. Both frequencies then run in the
+// folded order (even ones first, then odd), which the constants that meet them follow.
 struct FieldLayout {
     int nbx, nby, mode;
     bool fold;
@@ -27,8 +28,9 @@ constexpr int F16_TOP = 14;       // f16x3: a chunk of data is scaled so that it
 constexpr int F16_EMAX = 100;     // f16x3: chunk exponents are clamped to [-100, 100] (all factors stay normal)
 
 // PLAIN: float32 [M][N]; TRANS: float32 [N][M] (CUDA-core GEMM); WEIGHT2: the two weighted products of the field;
-// SPLIT: the 16-bit terms of the product, [terms][M][N] (tensor-core GEMM)
-enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3 };
+// SPLIT: the 16-bit terms of the product, [terms][M][N] (tensor-core GEMM); FOLD (f16x3): the product's columns in
+// mirrored pairs (B rows n and N-1-n), the float16 terms of their sums and of their differences, [terms][M][N/2] each
+enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3, EPI_FOLD = 4 };
 
 struct SGemm {
     int M, N, K;

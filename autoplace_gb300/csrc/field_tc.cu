@@ -282,8 +282,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int t = 0; t < NA; t++)
                     tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
 #pragma unroll
-                for (int t = 0; t < NB; t++)
-                    tma_load_3d(smem_u32(st + NA * TC_A_TILE + t * B_TILE), mb, full_bar(s), it * TC_BK, n0, t);
+                for (int t = 0; t < NB; t++) {
+                    const uint32_t dst = smem_u32(st + NA * TC_A_TILE + t * B_TILE);
+                    if (EPI == EPI_FOLD) {                       // B rows [64j, 64j + 64) and their mirror
+                        tma_load_3d(dst, mb, full_bar(s), it * TC_BK, 64 * (int)blockIdx.x, t);
+                        tma_load_3d(dst + 64 * 128, mb, full_bar(s), it * TC_BK, P.N - 64 - 64 * (int)blockIdx.x, t);
+                    } else {
+                        tma_load_3d(dst, mb, full_bar(s), it * TC_BK, n0, t);
+                    }
+                }
             }
         }
     } else if (warp == 1) {
@@ -338,13 +345,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else {                                                     // readers + epilogue
         const int q4 = warp & 3;                                 // tensor-memory lane quarter
         const int row = m0 + q4 * 32 + lane;
-        const float4 wr = EPI == EPI_WEIGHT2 ? P.wrow[row] : make_float4(0.f, 0.f, 0.f, 0.f);   // loaded early
+        const float4 wr = EPI == EPI_WEIGHT2 ? P.wrow[P.m_out + row] : make_float4(0.f, 0.f, 0.f, 0.f);   // early
         if constexpr (F16) {                                     // this tile's factors of B, every k-block
             constexpr int wpk = BN / 4;                          // 4 exponents per global word
             const int rt = (int)threadIdx.x - 64, words = total * wpk;
             for (int w = rt; w < words; w += 128) {
                 const int kb = w / wpk, c4 = w - kb * wpk;
-                const int e4 = __ldg((const int*)(P.b_exp + (size_t)kb * P.N + n0 + 4 * c4));
+                // (FOLD: columns 64 .. 127 are B rows N - 64j - 64 .. N - 64j - 1)
+                const int n = EPI != EPI_FOLD ? n0 + 4 * c4
+                              : 4 * c4 < 64 ? 64 * (int)blockIdx.x + 4 * c4 : P.N - 128 - 64 * (int)blockIdx.x + 4 * c4;
+                const int e4 = __ldg((const int*)(P.b_exp + (size_t)kb * P.N + n));
                 uint32_t f[4];
 #pragma unroll
                 for (int i = 0; i < 4; i++) f[i] = (uint32_t)(127 - F16_CONST - ((e4 << (24 - 8 * i)) >> 24)) << 7;
@@ -418,6 +428,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int c = 0; c < BN / 4; c++)
                     st_shared_v4(sbase + chunk(c >> 3, c & 7), make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2],
                                                                           r[4 * c + 3]));
+            } else if (EPI == EPI_FOLD) {
+                // column c < 64 is B row 64j + c, column 127 - c its mirror N - 1 - (64j + c): sums into r[c],
+                // differences into r[127 - c]; boxes 0-1: the terms of the sums, 2-3: of the differences, each the
+                // output's 64-column chunk j with its own scale
+#pragma unroll
+                for (int c = 0; c < 64; c++) {
+                    const float a = r[c], b = r[127 - c];
+                    r[c] = __fadd_rn(a, b);
+                    r[127 - c] = __fsub_rn(a, b);
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    float mx = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 64; i++) mx = fmaxf(mx, fabsf(r[64 * h + i]));
+                    const int e = f16_chunk_exp(mx);
+                    const float sc = __int_as_float((127 + e) << 23);
+                    (h ? P.o2_exp : P.o_exp)[(size_t)blockIdx.x * P.M_out + P.m_out + row] = (signed char)e;
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        __align__(16) __half ta[8], tb[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) split2h(r[h ? 127 - (8 * c + i) : 8 * c + i] * sc, ta[i], tb[i]);
+                        st_shared_v4(sbase + chunk(2 * h, c), *(const float4*)ta);
+                        st_shared_v4(sbase + chunk(2 * h + 1, c), *(const float4*)tb);
+                    }
+                }
             } else if (EPI == EPI_SPLIT && F16) {                // float16 terms of each 64-column chunk, scaled
 #pragma unroll
                 for (int g = 0; g < BN / 64; g++) {
@@ -522,6 +559,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (EPI == EPI_PLAIN) {
 #pragma unroll
                 for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, om0);
+            } else if (EPI == EPI_FOLD) {
+#pragma unroll
+                for (int t = 0; t < 2; t++) {
+                    tma_store_3d(mo, sbase + t * EPI_BOX, 64 * (int)blockIdx.x, om0, t);
+                    tma_store_3d(mo2, sbase + (2 + t) * EPI_BOX, 64 * (int)blockIdx.x, om0, t);
+                }
             } else if (EPI == EPI_SPLIT) {
                 constexpr int OT = F16 ? 2 : 3;                  // output terms
 #pragma unroll
@@ -626,10 +669,11 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     for (int z = 0; z < 2; z++) {
         const TcOp& o = ops[z < nops ? z : 0];
         if (F16 && ((long long)(o.p.K / TC_BK) * BN * 2 > TC_STAGE_SPACE - (long long)stages * stage_bytes ||
-                    !o.p.b_exp || (EPI != EPI_PLAIN && !o.p.o_exp) || (EPI == EPI_WEIGHT2 && !o.p.o2_exp)))
+                    !o.p.b_exp || (EPI != EPI_PLAIN && !o.p.o_exp) ||
+                    ((EPI == EPI_WEIGHT2 || EPI == EPI_FOLD) && !o.p.o2_exp)))
             return GP103_ERR_ARG;
         if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM, F16) ||
-            !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, BN, F16))
+            !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, EPI == EPI_FOLD ? 64 : BN, F16))
             return GP103_ERR_CUDA;
         // outputs (stored by TMA): bf16 terms [3][M][N] as (N, M, term) boxes of 64 x 128; float32 [M][N]
         CUtensorMap* oa = &maps[4 + 2 * z];
@@ -639,8 +683,9 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
             ok = make_map_f32(oa, o.p.out_f32, o.p.M_out, o.p.N);
             *ob = *oa;
         } else {
-            ok = make_map(oa, o.p.o_terms, o.p.M_out, o.p.N, TC_BM, F16);
-            if (ok && EPI == EPI_WEIGHT2) ok = make_map(ob, o.p.o2_terms, o.p.M_out, o.p.N, TC_BM, F16);
+            const int ncols = EPI == EPI_FOLD ? o.p.N / 2 : o.p.N;
+            ok = make_map(oa, o.p.o_terms, o.p.M_out, ncols, TC_BM, F16);
+            if (ok && (EPI == EPI_WEIGHT2 || EPI == EPI_FOLD)) ok = make_map(ob, o.p.o2_terms, o.p.M_out, ncols, TC_BM, F16);
             else *ob = *oa;
         }
         if (!ok) return GP103_ERR_CUDA;
@@ -670,7 +715,9 @@ static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStrea
 static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int bn = 0) {
     const int epi = ops[0].p.epi;
     if (epi == EPI_SPLIT && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s);
-    if (nops == 1 && epi == EPI_WEIGHT2) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
+    if (epi == EPI_WEIGHT2 && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
+    if (epi == EPI_FOLD)                                         // 128 columns: 64 and their mirror (f16x3 only)
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<128, EPI_FOLD, 2>(ops, nops, err, s) : GP103_ERR_ARG;
     if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
     return GP103_ERR_ARG;                                        // no other combination is used
@@ -791,37 +838,56 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     //    product comes out in rows (no transposing epilogue); folded (f16x3): rows in the folded frequency order, which
     //    K's columns, the column weights and the A operands CyT / SyT of step 3 follow
     if (L.fold) {
-        // folded (f16x3): the even frequencies of the folded sum, rows [0, Y/2) of Tt, and the odd ones of the
-        // folded difference, rows [Y/2, Y): two GEMMs of half the height and half the depth in one launch
-        const int H = Y / 2;
-        const size_t cy_half = (size_t)H * H * 2, a_half = (size_t)X * H * 2;      // elements (2 terms)
-        TcOp o1[2] = {{B(c, L.c_cy), H, B(w, L.w_a), X, prob(H, X, H, EPI_SPLIT)},
-                      {B(c, L.c_cy) + cy_half, H, B(w, L.w_a) + a_half, X, prob(H, X, H, EPI_SPLIT)}};
+        // folded (f16x3). 1: the even frequencies of the density's folded sum and the odd ones of its folded
+        // difference (two GEMMs of half the height and half the depth in one launch), rows [0, Y/2) / [Y/2, Y) of Tt,
+        // the epilogue folding Tt about the middle of x: sums Ts and differences Td, [2 terms][Y][X/2] each
+        const int H = Y / 2, G = X / 2;
+        const size_t cy_half = (size_t)H * H * 2, a_half = (size_t)X * H * 2, t_half = (size_t)Y * G * 2;
+        TcOp o1[2] = {{B(c, L.c_cy), H, B(w, L.w_a), X, prob(H, X, H, EPI_FOLD)},
+                      {B(c, L.c_cy) + cy_half, H, B(w, L.w_a) + a_half, X, prob(H, X, H, EPI_FOLD)}};
         for (int z = 0; z < 2; z++) {
             o1[z].p.o_terms = B(w, L.w_tt);
+            o1[z].p.o2_terms = B(w, L.w_tt) + t_half;
             o1[z].p.M_out = Y;
             o1[z].p.m_out = z * H;
             o1[z].p.b_exp = E(L.e_a) + (size_t)z * (H / 64) * X;
             o1[z].p.o_exp = E(L.e_tt);
+            o1[z].p.o2_exp = E(L.e_tt) + (size_t)(G / 64) * Y;
         }
-        if ((st = launch_tc(o1, 2, L.mode, err, s, 64))) return st;
+        if ((st = launch_tc(o1, 2, L.mode, err, s))) return st;
+        // 2: the even frequencies along x from Ts and the odd ones from Td, rows [0, X/2) / [X/2, X) of K, weighted
+        const size_t cx_half = (size_t)G * G * 2;
+        TcOp o2[2] = {{B(c, L.c_cx), G, B(w, L.w_tt), Y, prob(G, Y, G, EPI_WEIGHT2)},
+                      {B(c, L.c_cx) + cx_half, G, B(w, L.w_tt) + t_half, Y, prob(G, Y, G, EPI_WEIGHT2)}};
+        for (int z = 0; z < 2; z++) {
+            o2[z].p.o_terms = B(w, L.w_kx);
+            o2[z].p.o2_terms = B(w, L.w_ky);
+            o2[z].p.M_out = X;
+            o2[z].p.m_out = z * G;
+            o2[z].p.b_exp = E(L.e_tt) + (size_t)z * (G / 64) * Y;
+            o2[z].p.o_exp = E(L.e_kx);
+            o2[z].p.o2_exp = E(L.e_ky);
+            o2[z].p.wrow = (const float4*)(c + L.c_wrow);
+            o2[z].p.wcol = (const float4*)(c + L.c_wcol);
+        }
+        if ((st = launch_tc(o2, 2, L.mode, err, s, 64))) return st;
     } else {
         TcOp o1 = {B(c, L.c_cy), Y, B(w, L.w_a), X, prob(Y, X, Y, EPI_SPLIT)};
         o1.p.o_terms = B(w, L.w_tt);
         o1.p.b_exp = E(L.e_a);
         o1.p.o_exp = E(L.e_tt);
         if ((st = launch_tc(&o1, 1, L.mode, err, s))) return st;
+        // 2: K = Cx T -> Kx, Ky
+        TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
+        o2.p.o_terms = B(w, L.w_kx);
+        o2.p.o2_terms = B(w, L.w_ky);
+        o2.p.b_exp = E(L.e_tt);
+        o2.p.o_exp = E(L.e_kx);
+        o2.p.o2_exp = E(L.e_ky);
+        o2.p.wrow = (const float4*)(c + L.c_wrow);
+        o2.p.wcol = (const float4*)(c + L.c_wcol);
+        if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
     }
-    // 2: K = Cx T -> Kx, Ky
-    TcOp o2 = {B(c, L.c_cx), X, B(w, L.w_tt), Y, prob(X, Y, X, EPI_WEIGHT2)};
-    o2.p.o_terms = B(w, L.w_kx);
-    o2.p.o2_terms = B(w, L.w_ky);
-    o2.p.b_exp = E(L.e_tt);
-    o2.p.o_exp = E(L.e_kx);
-    o2.p.o2_exp = E(L.e_ky);
-    o2.p.wrow = (const float4*)(c + L.c_wrow);
-    o2.p.wcol = (const float4*)(c + L.c_wcol);
-    if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
     // 3a / 4a: Pt = (Kx Cy)^T = Cy^T Kx^T, Qt = (Ky Sy)^T = Sy^T Ky^T (row operand Cy^T / Sy^T, column operand Kx / Ky)
     TcOp o3[2] = {{B(c, L.c_cyt), Y, B(w, L.w_kx), X, prob(Y, X, Y, EPI_SPLIT)},
                   {B(c, L.c_syt), Y, B(w, L.w_ky), X, prob(Y, X, Y, EPI_SPLIT)}};
