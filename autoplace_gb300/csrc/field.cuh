@@ -29,8 +29,11 @@ constexpr int F16_EMAX = 100;     // f16x3: chunk exponents are clamped to [-100
 
 // PLAIN: float32 [M][N]; TRANS: float32 [N][M] (CUDA-core GEMM); WEIGHT2: the two weighted products of the field;
 // SPLIT: the 16-bit terms of the product, [terms][M][N] (tensor-core GEMM); FOLD (f16x3): the product's columns in
-// mirrored pairs (B rows n and N-1-n), the float16 terms of their sums and of their differences, [terms][M][N/2] each
-enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3, EPI_FOLD = 4 };
+// mirrored pairs (B rows n and N-1-n), the float16 terms of their sums and of their differences, [terms][M][N/2] each;
+// MSPLIT / MPLAIN (f16x3): an inverse transform over a depth in the folded frequency order, rows m < M_out/2 computed
+// as E (the even frequencies, the first half of K) and O (the odd ones): row m = E + O, row M_out-1-m = msign (E - O),
+// out as SPLIT / PLAIN
+enum { EPI_PLAIN = 0, EPI_TRANS = 1, EPI_WEIGHT2 = 2, EPI_SPLIT = 3, EPI_FOLD = 4, EPI_MSPLIT = 5, EPI_MPLAIN = 6 };
 
 struct SGemm {
     int M, N, K;

@@ -32,6 +32,7 @@ struct TcProblem {
     int epi;
     int M_out, m_out;            // the outputs (terms, float32 plane, exponents) have M_out rows; this problem's start
                                  // at row m_out (two problems of one launch can fill one output)
+    int msign;                   // MSPLIT / MPLAIN: +1 for a cosine row operand (mirror row E - O), -1 for a sine one
     __nv_bfloat16* o_terms;      // EPI_SPLIT: [3][M][N]; EPI_WEIGHT2: [3][M][N] (Kx), o2: Ky
     __nv_bfloat16* o2_terms;
     float* out_f32;              // EPI_PLAIN: [M][N]
@@ -362,12 +363,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             asm volatile("bar.sync 1, 128;" ::: "memory");
         }
+        constexpr bool MIRROR = EPI == EPI_MSPLIT || EPI == EPI_MPLAIN;
         float r[BN];
+        float e[MIRROR ? BN : 1];                                // MIRROR: E, the sum over the first half of K
 #pragma unroll
         for (int i = 0; i < BN; i++) r[i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < (MIRROR ? BN : 1); i++) e[i] = 0.f;
         bool ok = true;
         for (int it = 0; it < total && ok; it++) {
             const int b = it & 1;
+            if (MIRROR && it == total / 2) {                     // the even frequencies are summed: E aside, O next
+#pragma unroll
+                for (int i = 0; i < BN; i++) {
+                    e[i] = r[i];
+                    r[i] = 0.f;
+                }
+            }
             if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4)) { ok = false; break; }
             tc_fence_after();
             const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)b * ACC_COLS;
@@ -422,8 +434,53 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (r_in < BN) ((float4*)(smem + 6 * EPI_BOX))[r_in] = P.wcol[n0 + r_in];
             asm volatile("bar.sync 1, 128;" ::: "memory");
         }
+        // MIRROR: box row of this thread's row of the mirror tile (stored upside down: tile row r_in is output row
+        // M_out - 1 - (om0 + r_in), box row 127 - r_in of a tile stored at M_out - om0 - 128)
+        auto chunk_at = [&](int box, int c, bool mirror) {
+            const int rr = mirror ? 127 - r_in : r_in;
+            return (uint32_t)(box * EPI_BOX + rr * 128 + ((c ^ (rr & 7)) << 4));
+        };
         if (ok) {
-            if (EPI == EPI_PLAIN) {                              // float32: boxes of 32 columns
+            if constexpr (MIRROR) {
+                // row m = E + O (into e), its mirror msign (E - O) (into r); boxes from 0: the rows, behind them:
+                // the mirror rows (float32: BN / 32 boxes each; float16: the 2 terms of the one 64-column chunk)
+                const float sg = (float)P.msign;
+#pragma unroll
+                for (int i = 0; i < BN; i++) {
+                    const float a = e[i], b = r[i];
+                    e[i] = __fadd_rn(a, b);
+                    r[i] = sg * __fsub_rn(a, b);
+                }
+                if (EPI == EPI_MPLAIN) {
+#pragma unroll
+                    for (int c = 0; c < BN / 4; c++) {
+                        st_shared_v4(sbase + chunk_at(c >> 3, c & 7, false),
+                                     make_float4(e[4 * c], e[4 * c + 1], e[4 * c + 2], e[4 * c + 3]));
+                        st_shared_v4(sbase + chunk_at(BN / 32 + (c >> 3), c & 7, true),
+                                     make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]));
+                    }
+                } else {
+                    auto put = [&](float (&v)[BN], int box0, bool mirror) {
+                        float mx = 0.f;
+#pragma unroll
+                        for (int i = 0; i < BN; i++) mx = fmaxf(mx, fabsf(v[i]));
+                        const int ex = f16_chunk_exp(mx);
+                        const float sc = __int_as_float((127 + ex) << 23);
+                        const int orow = mirror ? P.M_out - 1 - (P.m_out + row) : P.m_out + row;
+                        P.o_exp[(size_t)(n0 / 64) * P.M_out + orow] = (signed char)ex;
+#pragma unroll
+                        for (int c = 0; c < 8; c++) {
+                            __align__(16) __half ta[8], tb[8];
+#pragma unroll
+                            for (int i = 0; i < 8; i++) split2h(v[8 * c + i] * sc, ta[i], tb[i]);
+                            st_shared_v4(sbase + chunk_at(box0, c, mirror), *(const float4*)ta);
+                            st_shared_v4(sbase + chunk_at(box0 + 1, c, mirror), *(const float4*)tb);
+                        }
+                    };
+                    put(e, 0, false);
+                    put(r, 2, true);
+                }
+            } else if (EPI == EPI_PLAIN) {                       // float32: boxes of 32 columns
 #pragma unroll
                 for (int c = 0; c < BN / 4; c++)
                     st_shared_v4(sbase + chunk(c >> 3, c & 7), make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2],
@@ -556,7 +613,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int om0 = m0 + P.m_out;         // the tile's first output row
             const CUtensorMap* mo = z ? &o1a : &o0a;
             const CUtensorMap* mo2 = z ? &o1b : &o0b;
-            if (EPI == EPI_PLAIN) {
+            if (EPI == EPI_MPLAIN || EPI == EPI_MSPLIT) {
+                const int mm0 = P.M_out - om0 - TC_BM;          // the mirror tile (rows upside down in its boxes)
+                if (EPI == EPI_MPLAIN) {
+#pragma unroll
+                    for (int b = 0; b < BN / 32; b++) {
+                        tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, om0);
+                        tma_store_2d(mo, sbase + (BN / 32 + b) * EPI_BOX, n0 + 32 * b, mm0);
+                    }
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 2; t++) {
+                        tma_store_3d(mo, sbase + t * EPI_BOX, n0, om0, t);
+                        tma_store_3d(mo, sbase + (2 + t) * EPI_BOX, n0, mm0, t);
+                    }
+                }
+            } else if (EPI == EPI_PLAIN) {
 #pragma unroll
                 for (int b = 0; b < BN / 32; b++) tma_store_2d(mo, sbase + b * EPI_BOX, n0 + 32 * b, om0);
             } else if (EPI == EPI_FOLD) {
@@ -669,7 +741,7 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     for (int z = 0; z < 2; z++) {
         const TcOp& o = ops[z < nops ? z : 0];
         if (F16 && ((long long)(o.p.K / TC_BK) * BN * 2 > TC_STAGE_SPACE - (long long)stages * stage_bytes ||
-                    !o.p.b_exp || (EPI != EPI_PLAIN && !o.p.o_exp) ||
+                    !o.p.b_exp || (EPI != EPI_PLAIN && EPI != EPI_MPLAIN && !o.p.o_exp) ||
                     ((EPI == EPI_WEIGHT2 || EPI == EPI_FOLD) && !o.p.o2_exp)))
             return GP103_ERR_ARG;
         if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM, F16) ||
@@ -679,7 +751,7 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
         CUtensorMap* oa = &maps[4 + 2 * z];
         CUtensorMap* ob = &maps[5 + 2 * z];
         bool ok = true;
-        if (EPI == EPI_PLAIN) {
+        if (EPI == EPI_PLAIN || EPI == EPI_MPLAIN) {
             ok = make_map_f32(oa, o.p.out_f32, o.p.M_out, o.p.N);
             *ob = *oa;
         } else {
@@ -718,6 +790,10 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     if (epi == EPI_WEIGHT2 && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
     if (epi == EPI_FOLD)                                         // 128 columns: 64 and their mirror (f16x3 only)
         return mode == GP103_FIELD_F16X3 ? launch_tc_mode<128, EPI_FOLD, 2>(ops, nops, err, s) : GP103_ERR_ARG;
+    if (epi == EPI_MSPLIT)                                       // half-height tiles, each with its mirror (f16x3)
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MSPLIT, 2>(ops, nops, err, s) : GP103_ERR_ARG;
+    if (epi == EPI_MPLAIN)
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MPLAIN, 2>(ops, nops, err, s) : GP103_ERR_ARG;
     if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s);
     if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
     return GP103_ERR_ARG;                                        // no other combination is used
@@ -888,9 +964,14 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
         o2.p.wcol = (const float4*)(c + L.c_wcol);
         if ((st = launch_tc(&o2, 1, L.mode, err, s))) return st;
     }
-    // 3a / 4a: Pt = (Kx Cy)^T = Cy^T Kx^T, Qt = (Ky Sy)^T = Sy^T Ky^T (row operand Cy^T / Sy^T, column operand Kx / Ky)
-    TcOp o3[2] = {{B(c, L.c_cyt), Y, B(w, L.w_kx), X, prob(Y, X, Y, EPI_SPLIT)},
-                  {B(c, L.c_syt), Y, B(w, L.w_ky), X, prob(Y, X, Y, EPI_SPLIT)}};
+    // 3a / 4a: Pt = (Kx Cy)^T = Cy^T Kx^T, Qt = (Ky Sy)^T = Sy^T Ky^T (row operand Cy^T / Sy^T, column operand Kx / Ky);
+    // folded: rows n < Y/2 and their mirrors Y-1-n from the even and odd frequencies (cosine: E - O, sine: O - E)
+    const int e3 = L.fold ? EPI_MSPLIT : EPI_SPLIT, M3 = L.fold ? Y / 2 : Y;
+    TcOp o3[2] = {{B(c, L.c_cyt), Y, B(w, L.w_kx), X, prob(M3, X, Y, e3)},
+                  {B(c, L.c_syt), Y, B(w, L.w_ky), X, prob(M3, X, Y, e3)}};
+    o3[0].p.M_out = o3[1].p.M_out = Y;
+    o3[0].p.msign = 1;
+    o3[1].p.msign = -1;
     o3[0].p.o_terms = B(w, L.w_pt);
     o3[1].p.o_terms = B(w, L.w_qt);
     o3[0].p.b_exp = E(L.e_kx);
@@ -898,9 +979,13 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     o3[1].p.b_exp = E(L.e_ky);
     o3[1].p.o_exp = E(L.e_qt);
     if ((st = launch_tc(o3, 2, L.mode, err, s))) return st;
-    // 3b / 4b: Ex = Sx^T P, Ey = Cx^T Q
-    TcOp o4[2] = {{B(c, L.c_sxt), X, B(w, L.w_pt), Y, prob(X, Y, X, EPI_PLAIN)},
-                  {B(c, L.c_cxt), X, B(w, L.w_qt), Y, prob(X, Y, X, EPI_PLAIN)}};
+    // 3b / 4b: Ex = Sx^T P, Ey = Cx^T Q (folded: as step 3, rows m < X/2 and their mirrors)
+    const int e4 = L.fold ? EPI_MPLAIN : EPI_PLAIN, M4 = L.fold ? X / 2 : X;
+    TcOp o4[2] = {{B(c, L.c_sxt), X, B(w, L.w_pt), Y, prob(M4, Y, X, e4)},
+                  {B(c, L.c_cxt), X, B(w, L.w_qt), Y, prob(M4, Y, X, e4)}};
+    o4[0].p.M_out = o4[1].p.M_out = X;
+    o4[0].p.msign = -1;
+    o4[1].p.msign = 1;
     o4[0].p.out_f32 = ex;
     o4[1].p.out_f32 = ey;
     o4[0].p.b_exp = E(L.e_pt);

@@ -225,11 +225,12 @@ def kernel_bytes(prob, field="f16x3"):
 
 def tc_flops(prob, field):
     """Tensor-core FLOPs of the field per density pass: six GEMMs of nb^3 (2 nb^3 per product, the mode's products
-    each); f16x3 on a grid of a multiple of 256 bins folds both forward transforms, each into two GEMMs of half the
-    height and half the depth: one GEMM less."""
+    each); f16x3 on a grid of a multiple of 256 bins folds the transforms: each forward one into two GEMMs of half
+    the height and half the depth, each inverse one into half-height products that also give the mirror rows -- half
+    the products in all."""
     nb = prob.force_bin
     terms = {"bf16x6": 6, "bf16x3": 3, "f16x3": 3}.get(field, 0)
-    gemms = 5.0 if field == "f16x3" and nb % 256 == 0 else 6.0
+    gemms = 3.0 if field == "f16x3" and nb % 256 == 0 else 6.0
     return 2.0 * nb ** 3 * terms * gemms
 
 
