@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--config", default="c2")
     p.add_argument("--field", default="f16x3", choices=["f16x3", "bf16x6", "bf16x3", "fp32"])
     p.add_argument("--cpu-iters", type=int, default=4, help="density-phase iterations of the CPU sample")
-    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-pdl", action="store_true", help="plain stream order instead of programmatic dependent launch")
     p.add_argument("--split", action="store_true", help="the WA kernels on a second stream, beside the density map")
@@ -355,8 +355,10 @@ def run_gb300(args):
     h2d = sum(x.numel() * x.element_size() for x in list(host.values()) + list(maps.values())) + \
         host_pos.numel() * 4 + len(prob.constants()) * 8
     d2h = out.numel() * 4
+    # one untimed step first: it loads the device-build kernels, which only this path uses (a one-time cost per
+    # process, like the warm-up placements of the device-timed loop)
     e2e_s = []
-    for _ in range(args.e2e_steps):
+    for i in range(1 + args.e2e_steps):
         torch.cuda.synchronize()
         t = time.time()
         dprob = base.on_device(stream=placer.stream, host=host)
@@ -364,7 +366,8 @@ def run_gb300(args):
         rr = pl2.run(host_pos)
         out.copy_(rr["pos"])
         torch.cuda.synchronize()
-        e2e_s.append(time.time() - t)
+        if i > 0:
+            e2e_s.append(time.time() - t)
         del pl2, dprob
     e2e = reduce_max(statistics.median(e2e_s), world)
 
