@@ -19,6 +19,8 @@
 //   3b Ex[m][n]  = Sx^T . P                                       A = SxT [nbx][nbx], B = Pt
 //   4a Qt[n][p]  = (Ky . Sy)^T                                    A = Ky, B = SyT [nby][nby]
 //   4b Ey[m][n]  = Cx^T . Q                                       A = CxT [nbx][nbx], B = Qt
+// With f16x3 on grids of multiples of 256 the tensor-core form folds the transforms (FieldLayout::fold): half the
+// products, the frequencies in the folded order (even ones first), which the constants below follow.
 // This file has the constants and the float32 CUDA-core GEMM (any grid); field_tc.cu has the tensor-core form.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>

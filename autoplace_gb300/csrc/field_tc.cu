@@ -7,7 +7,11 @@
 // same staged k-block (each term's tile is loaded once per k-block) into one accumulator:
 //   bf16x3: (1,0) (0,1) (0,0)                          ~1e-5 of the max
 //   bf16x6: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)        ~2e-7 of the max (float32-level)
+// f16x3 instead keeps two float16 terms per operand, data chunks scaled by powers of two (below), 3 products.
 // Tiles are 128 rows x BN columns: BN = 64 when a launch has one GEMM (twice the blocks), 128 when it has two.
+// Folded transforms (f16x3, grids of multiples of 256; field.cuh): the forward ones as two half-size GEMMs per launch
+// (64-column tiles; the first with EPI_FOLD, 64-row B tiles and their mirrors), the inverse ones as half-height
+// tiles that also write their mirror rows (EPI_MSPLIT, EPI_MPLAIN).
 // Shapes: M, N multiples of 128, K a multiple of 64 (force grids of 128 .. 4096 bins per side).
 #include <cuda.h>
 #include <cudaTypedefs.h>
