@@ -215,18 +215,19 @@ def test_control_divergence():
 
 # ------------------------------------------------------------------------------------------------ field
 def _field_plan(nb, mode, bx=7.3, by=6.1):
-    """A minimal plan with only the field buffers filled (gp103_field needs no netlist)."""
+    """A minimal plan with only the field buffers filled (gp103_field needs no netlist); nb: n or (nbx, nby)."""
+    nbx, nby = nb if isinstance(nb, tuple) else (nb, nb)
     s = native.Sizes()
-    native.call("gp103_plan_sizes", nb, nb, mode, ctypes.byref(s))
+    native.call("gp103_plan_sizes", nbx, nby, mode, ctypes.byref(s))
     keep = dict(c=torch.zeros(s.field_const, dtype=torch.uint8, device=DEV),
                 w=torch.zeros(s.field_work, dtype=torch.uint8, device=DEV),
                 red=torch.zeros(s.red, dtype=torch.float64, device=DEV),
                 cnt=torch.zeros(16, dtype=torch.int32, device=DEV),
-                map=torch.zeros((2, nb, nb), dtype=torch.int64, device=DEV),
-                ex=torch.zeros((nb, nb), device=DEV), ey=torch.zeros((nb, nb), device=DEV),
+                map=torch.zeros((2, nbx, nby), dtype=torch.int64, device=DEV),
+                ex=torch.zeros((nbx, nby), device=DEV), ey=torch.zeros((nbx, nby), device=DEV),
                 kp=torch.zeros(5, device=DEV))
     pl = native.Plan()
-    pl.nbx = pl.nby = nb
+    pl.nbx, pl.nby = nbx, nby
     pl.bx, pl.by = bx, by
     pl.field_mode = mode
     pl.field_const, pl.field_work = keep["c"].data_ptr(), keep["w"].data_ptr()
@@ -237,10 +238,11 @@ def _field_plan(nb, mode, bx=7.3, by=6.1):
 
 
 def _density_plane(nb, seed=0):
+    nbx, nby = nb if isinstance(nb, tuple) else (nb, nb)
     rng = np.random.default_rng(seed)
-    a = rng.random((nb, nb)) * 0.3 + 0.6
-    a[nb // 3: nb // 3 + 5, nb // 2: nb // 2 + 7] += 40.0          # a clump
-    a[: nb // 4, -nb // 5:] = 0.9                                   # a blocked corner
+    a = rng.random((nbx, nby)) * 0.3 + 0.6
+    a[nbx // 3: nbx // 3 + 5, nby // 2: nby // 2 + 7] += 40.0      # a clump
+    a[: nbx // 4, -nby // 5:] = 0.9                                 # a blocked corner
     return a.astype(np.float32)
 
 
@@ -248,11 +250,17 @@ def _density_plane(nb, seed=0):
                                          (128, native.FIELD_BF16X6, 1e-6), (256, native.FIELD_BF16X6, 1e-6),
                                          (256, native.FIELD_BF16X3, 3e-5), (128, native.FIELD_F16X3, 1e-6),
                                          (256, native.FIELD_F16X3, 1e-6), (1024, native.FIELD_F16X3, 1e-6),
-                                         (1024, native.FIELD_BF16X6, 1e-6)])
+                                         (1024, native.FIELD_BF16X6, 1e-6), ((256, 512), native.FIELD_F16X3, 1e-6),
+                                         ((512, 256), native.FIELD_F16X3, 1e-6),
+                                         ((256, 384), native.FIELD_F16X3, 1e-6)])
 def test_field_matches_fp64(nb, mode, tol):
+    """The field against its float64 statement and the reference's mirrored FFT. f16x3 folds the transforms on grids
+    whose sides are multiples of 256 (256, 1024, 256 x 512, 512 x 256: the x and y folds each on a grid where the
+    other side differs), not on 128 or 256 x 384."""
+    nbx, nby = nb if isinstance(nb, tuple) else (nb, nb)
     pl, keep = _field_plan(nb, mode)
     a = _density_plane(nb)
-    ex, ey = torch.zeros((nb, nb), device=DEV), torch.zeros((nb, nb), device=DEV)
+    ex, ey = torch.zeros((nbx, nby), device=DEV), torch.zeros((nbx, nby), device=DEV)
     d = cu(a)
     native.call("gp103_field", ctypes.byref(pl), d.data_ptr(), ex.data_ptr(), ey.data_ptr(),
                 torch.cuda.current_stream().cuda_stream)
@@ -262,5 +270,5 @@ def test_field_matches_fp64(nb, mode, tol):
     err = max(np.abs(ex.cpu().numpy() - fx).max(), np.abs(ey.cpu().numpy() - fy).max()) / scale
     assert err <= tol, err
     # the same as the first quadrant of the reference's mirrored FFT field
-    f64 = O.field_fft(O.mirror(a), nb, nb, np.array([7.3, 6.1]))
-    assert np.abs(ex.cpu().numpy() - f64[0, :nb, :nb]).max() <= 2 * tol * scale
+    f64 = O.field_fft(O.mirror(a), nbx, nby, np.array([7.3, 6.1]))
+    assert np.abs(ex.cpu().numpy() - f64[0, :nbx, :nby]).max() <= 2 * tol * scale
