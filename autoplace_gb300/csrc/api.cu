@@ -432,7 +432,10 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     w.pos_a = (const float2*)p->v[0];
     w.pos_b = (const float2*)p->v[1];
     w.sel = p->cur;
-    TRY(launch_wa_net(w, split ? side : stream));
+    // density passes in one stream: the WA kernels go after the field, right before the gather, which reads their pin
+    // gradients (42 MB at 1.2M cells) while they are still in L2; nothing between depends on them
+    const bool wa_late = phase == GP103_PHASE_DENSITY && !split;
+    if (!wa_late) TRY(launch_wa_net(w, split ? side : stream));
     if (split && cudaEventRecord(join, side) != cudaSuccess) return GP103_ERR_CUDA;
 
     GatherJob g = gather_job(p);
@@ -459,6 +462,7 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
         return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, stream);
     }
     TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream));
+    if (wa_late) TRY(launch_wa_net(w, stream));
     if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
     g.ex = p->ex;
     g.ey = p->ey;
