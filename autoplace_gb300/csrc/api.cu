@@ -264,7 +264,7 @@ static OrderJob order_job(const gp103_plan* p) {
 }
 
 static int density_and_field(const gp103_plan* p, const float* pos_a, const float* pos_b, const int* sel,
-                             const int* order, cudaStream_t s) {
+                             const int* order, cudaStream_t s, const WaJob* wa = nullptr) {
     const size_t nb = (size_t)p->nbx * p->nby;
     ScatterJob sj = {};
     sj.pos_a = (const float2*)pos_a;
@@ -330,6 +330,7 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
         jp.red = reduce_slot(p->red, p->counters, R_JOVF);
     }
     TRY(launch_post_plain(posts, p->jnbx > 0 ? 2 : 1, s));
+    if (wa) TRY(launch_wa_net(*wa, s));                     // (see run_pass)
     return run_field(p, nullptr, s);
 }
 
@@ -432,8 +433,9 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     w.pos_a = (const float2*)p->v[0];
     w.pos_b = (const float2*)p->v[1];
     w.sel = p->cur;
-    // density passes in one stream: the WA kernels go after the field, right before the gather, which reads their pin
-    // gradients (42 MB at 1.2M cells) while they are still in L2; nothing between depends on them
+    // density passes in one stream: the WA kernels go between the density map and the field, so that the gather
+    // reads their pin gradients (42 MB at 1.2M cells) from L2 behind only the field's small working set, and the
+    // field planes it reads are the last thing written; nothing between depends on them
     const bool wa_late = phase == GP103_PHASE_DENSITY && !split;
     if (!wa_late) TRY(launch_wa_net(w, split ? side : stream));
     if (split && cudaEventRecord(join, side) != cudaSuccess) return GP103_ERR_CUDA;
@@ -461,8 +463,7 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
         TRY(launch_gather(g, stream));
         return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, stream);
     }
-    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream));
-    if (wa_late) TRY(launch_wa_net(w, stream));
+    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream, wa_late ? &w : nullptr));
     if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
     g.ex = p->ex;
     g.ey = p->ey;
