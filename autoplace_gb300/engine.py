@@ -153,7 +153,8 @@ class Placer(object):
                     self._p(self.pin_off), self._p(self.pin_slot), self._p(split), self.stream.cuda_stream)
         pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
         pl.cell_start, pl.pin_slot = self._p(self.cell_start), self._p(self.pin_slot)
-        pl.net_split, pl.net_mid, pl.net_two, pl.net_three = (int(x) for x in split.cpu().tolist())
+        # (the stream-ordered allocator may hand these blocks to the allocations below: their kernels run after
+        # gp103_net_order on the same stream; the split counts are read back at the end, after the other set-up)
         del ns_in, cell_in, off_in, cp_in, scratch
         self.size = self._hold(up("size", f.size, torch.float32))
         self.ratio = self._hold(up("ratio", f.ratio, torch.float32))
@@ -209,9 +210,11 @@ class Placer(object):
         self.tmp = [z((n, 2), torch.float32) for _ in range(2)]
         for k in ("best", "cur", "S", "T", "kp", "c", "pin_grad", "map", "red", "counters"):
             setattr(pl, k, self._p(getattr(self, k)))
+        native.call("gp103_field_constants", ctypes.byref(pl), self.stream.cuda_stream)
+        # the one host synchronisation of the set-up: the net classes of the WA order (launch sizes of the passes)
+        pl.net_split, pl.net_mid, pl.net_two, pl.net_three = (int(x) for x in split.cpu().tolist())
         self.plan = pl
         self._ref = ctypes.byref(pl)
-        native.call("gp103_field_constants", self._ref, self.stream.cuda_stream)
 
     def __del__(self):
         try:
