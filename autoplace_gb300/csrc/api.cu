@@ -20,11 +20,20 @@ using namespace gp103;
 
 // ------------------------------------------------------------------------------------------------ options
 static int g_pdl = 1;
+static int g_wait_ms = 2000;
+static int g_stall = 0;
 bool gp103::pdl_enabled() { return g_pdl != 0; }
+long long gp103::tc_wait_ns() { return (long long)g_wait_ms * 1000000LL; }
+bool gp103::tc_test_stall() { return g_stall != 0; }
 
 extern "C" int gp103_set_option(int option, int value) {
     switch (option) {
         case GP103_OPT_PDL: g_pdl = value != 0; return GP103_OK;
+        case GP103_OPT_WAIT_MS:
+            REQUIRE(value >= 1 && value <= 60000);
+            g_wait_ms = value;
+            return GP103_OK;
+        case GP103_OPT_TEST_STALL_FIELD: g_stall = value != 0; return GP103_OK;
         default: return GP103_ERR_ARG;
     }
 }
@@ -81,7 +90,8 @@ extern "C" const char* gp103_status_string(int status) {
         case GP103_ERR_CUDA: return "a CUDA launch failed";
         case GP103_ERR_SHAPE: return "grid not supported by the tensor-core field (multiples of 128 bins per side)";
         case GP103_ERR_TOO_LARGE:
-            return "grid larger than the fixed scratch of gp103_density_map_noalloc (nbx * nby <= 262144)";
+            return "size beyond a fixed limit (gp103_density_map_noalloc: nbx * nby <= 262144 bins; device problem "
+                   "build and net order: <= 16,777,215 pins, nets or cells)";
         default: return "unknown status";
     }
 }
@@ -222,9 +232,29 @@ static int check_plan(const gp103_plan* p) {
     return GP103_OK;
 }
 
+// The device error flag of the tensor-core field's waits (inside the field work buffer), or null (fp32 field).
+static int* field_error_flag(const gp103_plan* p) {
+    if (p->field_mode == GP103_FIELD_FP32) return nullptr;
+    return (int*)((char*)p->field_work + layout_of(p).w_err);
+}
+
 extern "C" int gp103_field_constants(const gp103_plan* plan, cudaStream_t stream) {
     TRY(check_plan(plan));
+    if (int* f = field_error_flag(plan))
+        if (cudaMemsetAsync(f, 0, sizeof(int), stream) != cudaSuccess) return GP103_ERR_CUDA;
     return field_constants(layout_of(plan), plan->field_const, stream);
+}
+
+extern "C" int gp103_device_error(const gp103_plan* plan, int clear, int* code, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    REQUIRE(code);
+    *code = 0;
+    int* f = field_error_flag(plan);
+    if (!f) return GP103_OK;
+    if (cudaMemcpyAsync(code, f, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return GP103_ERR_CUDA;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return GP103_ERR_CUDA;
+    if (clear && *code != 0 && cudaMemsetAsync(f, 0, sizeof(int), stream) != cudaSuccess) return GP103_ERR_CUDA;
+    return GP103_OK;
 }
 
 static int run_field(const gp103_plan* p, const float* density, cudaStream_t s) {
@@ -461,7 +491,7 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     g.pre_out = pre;
     if (phase == GP103_PHASE_START) {
         TRY(launch_gather(g, stream));
-        return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, stream);
+        return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, field_error_flag(p), stream);
     }
     TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream, wa_late ? &w : nullptr));
     if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
@@ -474,7 +504,7 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
     g.npre = 4;
     TRY(launch_gather(g, stream));
     const double scale = p->jnbx > 0 ? p->jovf_scale : p->ovf_scale;
-    return launch_control_fused(p->S, p->kp, p->c, r_grad, pre, scale, p->cur, stream);
+    return launch_control_fused(p->S, p->kp, p->c, r_grad, pre, scale, p->cur, field_error_flag(p), stream);
 }
 
 extern "C" int gp103_eval(const gp103_plan* plan, const float* pos, float* g_out, const float* g_ref, double weight,

@@ -28,7 +28,7 @@ constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                     // 16 KB per A 
 constexpr int TC_STAGE_SPACE = 216 * 1024;                       // room for the stages
 constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_SMEM = TC_STAGE_SPACE + 1024 + 256;
-constexpr long long TC_WAIT_NS = 2000000000LL;                  // a wait that takes 2 s has failed
+constexpr long long TC_DRAIN_NS = 2000000000LL;                 // limit of the waits for work already in flight
 constexpr int EPI_BOX = 128 * 128;                               // an epilogue box: 128 rows x 128 bytes
 
 struct TcProblem {
@@ -56,6 +56,8 @@ struct TcArgs {
     TcProblem p[2];
     int stages;
     int* err;
+    long long wait_ns;           // limit of one wait (GP103_OPT_WAIT_MS)
+    int stall;                   // GP103_OPT_TEST_STALL_FIELD: the producer issues no load (every wait runs out)
 };
 
 // The products of a mode, smallest first: bf16x6 (X6 = 1) has 3 terms per operand and 6 products, bf16x3 2 and 3.
@@ -93,18 +95,28 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false (and the error flag set) if the phase did not complete within TC_WAIT_NS, or if another
+// Bounded wait: false (and the error flag set) if the phase did not complete within `limit` ns, or if another
 // thread already gave up. The clock and the flag (a global load) are checked once every 64 tries (each try returns
 // within a bounded, system-dependent suspend time).
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code, long long limit) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = gtime();
     for (unsigned i = 1;; i++) {
         if (mbar_try(bar, parity)) return true;
-        if ((i & 63u) == 0u && (gtime() - t0 > TC_WAIT_NS || *(volatile int*)err != 0)) {
+        if ((i & 63u) == 0u && (gtime() - t0 > limit || *(volatile int*)err != 0)) {
             atomicCAS(err, 0, code);
             return false;
         }
+    }
+}
+// After a wait gave up: wait (at most TC_DRAIN_NS, whatever the error flag says) for work this thread already
+// started to land -- TMA loads into this block's shared memory, MMAs into its tensor memory -- so that the block
+// neither exits nor frees its tensor memory with them in flight.
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+    const long long t0 = gtime();
+    for (unsigned i = 0;; i++) {
+        if (mbar_try(bar, parity)) return;
+        if ((i & 63u) == 63u && gtime() - t0 > TC_DRAIN_NS) return;
     }
 }
 
@@ -243,6 +255,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int total = P.K / TC_BK, stages = args.stages;
     constexpr int stage_bytes = NA * TC_A_TILE + NB * B_TILE;
     int* err = args.err;
+    const long long limit = args.wait_ns;
     auto full_bar = [&](int s) { return smem_u32(&bars[s]); };
     auto empty_bar = [&](int s) { return smem_u32(&bars[TC_MAX_STAGES + s]); };
     auto accf_bar = [&](int b) { return smem_u32(&bars[2 * TC_MAX_STAGES + b]); };
@@ -277,10 +290,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {                                         // TMA producer
-            for (int it = 0; it < total; it++) {
+            int issued = 0;
+            for (int it = 0; it < total && !args.stall; it++) {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
-                if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1)) break;
+                if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1, limit)) break;
                 mbar_expect_tx(full_bar(s), stage_bytes);
                 uint8_t* st = smem + s * stage_bytes;
 #pragma unroll
@@ -296,15 +310,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         tma_load_3d(dst, mb, full_bar(s), it * TC_BK, n0, t);
                     }
                 }
+                issued = it + 1;
             }
+            // a wait gave up (here or anywhere in the grid): the last load of each stage may still be in flight
+            if (*(volatile int*)err != 0)
+                for (int it = issued > stages ? issued - stages : 0; it < issued; it++)
+                    mbar_drain(full_bar(it % stages), (uint32_t)(it / stages) & 1u);
         }
     } else if (warp == 1) {
         if (lane == 0) {                                         // MMA issuer: one k-block per accumulator
+            int committed = 0;
             for (int it = 0; it < total; it++) {
                 const int s = it % stages, b = it & 1;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u, use = (uint32_t)(it >> 1) & 1u;
-                if (!mbar_wait(acce_bar(b), use ^ 1u, err, 2)) break;
-                if (!mbar_wait(full_bar(s), ph, err, 3)) break;
+                if (!mbar_wait(acce_bar(b), use ^ 1u, err, 2, limit)) break;
+                if (!mbar_wait(full_bar(s), ph, err, 3, limit)) break;
                 tc_fence_after();
                 // descriptors of the stage's first A and B tiles; a tile or a 16-wide K step further on is the
                 // same descriptor with its start-address field (address / 16) advanced (no carry: smem < 256 KB)
@@ -345,7 +365,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
+                committed = it + 1;
             }
+            // a wait gave up: the last commit tracks every MMA this thread issued; wait for it before the tensor
+            // memory is freed
+            if (*(volatile int*)err != 0 && committed > 0)
+                mbar_drain(accf_bar((committed - 1) & 1), (uint32_t)((committed - 1) >> 1) & 1u);
         }
     } else {                                                     // readers + epilogue
         const int q4 = warp & 3;                                 // tensor-memory lane quarter
@@ -384,7 +409,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     r[i] = 0.f;
                 }
             }
-            if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4)) { ok = false; break; }
+            if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4, limit)) { ok = false; break; }
             tc_fence_after();
             const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)b * ACC_COLS;
 #pragma unroll
@@ -730,12 +755,17 @@ struct TcOp {
 template <int BN, int EPI, int MODE>
 static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     constexpr bool F16 = MODE == 2;
-    static bool attr = false;
-    if (!attr) {
+    // the shared-memory attribute is a property of the function on each device: set once per device (a race of two
+    // host threads sets it twice, which is harmless)
+    static unsigned long long attr_set[4] = {0, 0, 0, 0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return GP103_ERR_CUDA;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(__atomic_load_n(&attr_set[dev >> 6], __ATOMIC_ACQUIRE) & bit)) {
         if (cudaFuncSetAttribute(tc_gemm_kernel<BN, EPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM) !=
             cudaSuccess)
             return GP103_ERR_CUDA;
-        attr = true;
+        __atomic_fetch_or(&attr_set[dev >> 6], bit, __ATOMIC_ACQ_REL);
     }
     constexpr int terms = MODE == 1 ? 3 : 2;
     constexpr int stage_bytes = terms * TC_A_TILE + terms * BN * TC_BK * 2;
@@ -769,6 +799,8 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     }
     args.stages = stages;
     args.err = err;
+    args.wait_ns = tc_wait_ns();
+    args.stall = tc_test_stall() ? 1 : 0;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / BN, p.M / TC_BM, nops);
     if (launch_k(tc_gemm_kernel<BN, EPI, MODE>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2],

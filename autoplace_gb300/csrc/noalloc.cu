@@ -11,7 +11,10 @@
 //     2 x 262,144 x 8 bytes = 4 MiB, held on every GPU that loads the library until the process exits;
 //     larger grids are rejected with GP103_ERR_TOO_LARGE before any work;
 //   * the array's device address is looked up once per device (cudaGetSymbolAddress, with that device current) by
-//     the first call on that device; make that first call before any stream capture;
+//     the first call on that device; make that first call before any stream capture. The address is kept for the
+//     life of the process: after a cudaDeviceReset of a device it is stale (the reset destroys the context it
+//     belongs to), so do not call this entry point on that device again in the same process;
+//   * `stream` must belong to the current device (checked: GP103_ERR_ARG otherwise), whose array the call uses;
 //   * every call shares the one array and leaves its contents behind: each call clears the part it uses before
 //     adding to it, and calls whose work overlaps on the GPU (other streams, other host threads) race on it.
 #include <mutex>
@@ -57,6 +60,9 @@ extern "C" int gp103_density_map_noalloc(const float* pos, const float* size, co
     if (num_nodes > 0 && !(pos && size && ratio)) return GP103_ERR_ARG;
     if (!(bx > 0.f && by > 0.f)) return GP103_ERR_ARG;
     if ((long long)nbx * nby > NOALLOC_MAX_BINS) return GP103_ERR_TOO_LARGE;
+    int cur = -1, sdev = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(stream, &sdev) != cudaSuccess) return GP103_ERR_CUDA;
+    if (sdev != cur) return GP103_ERR_ARG;                    // the array of another device than the stream's
     unsigned long long* map = nullptr;
     int st = noalloc_map(&map);
     if (st) return st;

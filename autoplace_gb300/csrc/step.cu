@@ -241,8 +241,20 @@ int launch_probe(const float* v, const float* g, const float* lo, const float* h
 // pre: the totals the gather's block 0 summed (TOT_MOVED, TOT_WA, TOT_HPWL, TOT_OVF); the gather's own partials
 // (the squared distance of the gradients) are summed here
 __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp, const double* c, Reduce grad,
-                                                            const double* pre, double ovf_scale, int* cur) {
+                                                            const double* pre, double ovf_scale, int* cur,
+                                                            const int* ferr) {
     pdl_wait();
+    __shared__ int failed;                                  // the field gave up a wait: this pass's field is stale
+    if (threadIdx.x == 0) failed = ferr ? *(volatile const int*)ferr : 0;
+    __syncthreads();
+    if (failed) {
+        if (threadIdx.x == 0) {
+            S[S_ACCEPT] = 0;
+            S[S_IS_BEST] = 0;
+            if (S[S_STOP] == 0) S[S_STOP] = STOP_DEVICE_ERROR;
+        }
+        return;
+    }
     // the state and the constants in registers first (one wave of loads): the control reads them one after another,
     // and through global memory every read after a write would wait a full memory latency
     double Sl[S_SIZE], cl[C_SIZE];
@@ -268,8 +280,9 @@ __global__ void __launch_bounds__(256) control_fused_kernel(double* S, float* kp
 }
 
 int launch_control_fused(double* S, float* kp, const double* c, Reduce grad, const double* pre, double ovf_scale,
-                         int* cur, cudaStream_t s) {
-    if (launch_k(control_fused_kernel, dim3(1), dim3(256), 0, s, S, kp, c, grad, pre, ovf_scale, cur) != cudaSuccess)
+                         int* cur, const int* ferr, cudaStream_t s) {
+    if (launch_k(control_fused_kernel, dim3(1), dim3(256), 0, s, S, kp, c, grad, pre, ovf_scale, cur, ferr) !=
+        cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
@@ -308,15 +321,26 @@ __device__ void control_start_body(double* T, float* kp, double moved, double tu
 }
 
 __global__ void __launch_bounds__(256) control_start_kernel(double* T, float* kp, Reduce grad, const double* pre,
-                                                            int* cur) {
+                                                            int* cur, const int* ferr) {
     pdl_wait();
+    __shared__ int failed;
+    if (threadIdx.x == 0) failed = ferr ? *(volatile const int*)ferr : 0;
+    __syncthreads();
+    if (failed) {
+        if (threadIdx.x == 0) {
+            T[GP103_T_ACCEPT] = 0;
+            if (T[GP103_T_STOP] == 0) T[GP103_T_STOP] = STOP_DEVICE_ERROR;
+        }
+        return;
+    }
     const double turned2 = block_total(grad, 0);
     if (threadIdx.x == 0)
         control_start_body(T, kp, sqrt(pre[TOT_MOVED]), sqrt(turned2), pre[TOT_WA], pre[TOT_HPWL], cur);
 }
 
-int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, int* cur, cudaStream_t s) {
-    if (launch_k(control_start_kernel, dim3(1), dim3(256), 0, s, T, kp, grad, pre, cur) != cudaSuccess)
+int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, int* cur, const int* ferr,
+                         cudaStream_t s) {
+    if (launch_k(control_start_kernel, dim3(1), dim3(256), 0, s, T, kp, grad, pre, cur, ferr) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;

@@ -37,9 +37,13 @@ int launch_select(const double* S, float* u, float* v, float* g, const float* u_
 int launch_step(const StepJob& j, cudaStream_t s);
 int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
                  Reduce red, cudaStream_t s);
+// ferr: the tensor-core field's device error flag (or null): when set, the control stops the run with reason
+// STOP_DEVICE_ERROR and changes nothing else.
+constexpr int STOP_DEVICE_ERROR = 6;
 int launch_control_fused(double* S, float* kp, const double* c, Reduce grad, const double* pre, double ovf_scale,
-                         int* cur, cudaStream_t s);
-int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, int* cur, cudaStream_t s);
+                         int* cur, const int* ferr, cudaStream_t s);
+int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, int* cur, const int* ferr,
+                         cudaStream_t s);
 int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
                   cudaStream_t s);
 int launch_totals(const Reduce* r, const int* k, int n, double* out, cudaStream_t s);

@@ -24,7 +24,8 @@ from .native import Plan, Sizes, T as TI, T_SIZE
 S_FIELDS = ("lam gam alpha a iter hpwl_prev motion ww mu settled best_hpwl best_ovf is_best improved stop accept "
             "loop_it evals res_hpwl res_ovf has_best").split()
 SK = {n: i for i, n in enumerate(S_FIELDS)}
-REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handover"}
+REASON = {1: "converged", 2: "stalled", 3: "diverged", 4: "max_iter", 5: "handover", 6: "device_error"}
+STOP_DEVICE_ERROR = 6
 
 
 START_EVERY = 4        # passes per poll of the wirelength-only start
@@ -235,11 +236,24 @@ class Placer(object):
     def sync(self):
         self.stream.synchronize()
 
+    def check_device(self, what="gp103"):
+        """Raise RuntimeError if a wait of the tensor-core field ran out (the plan's device error flag), after the
+        work queued so far. The flag stays set: a later run stops at once with reason device_error."""
+        code = native.device_error(self._ref, self.stream.cuda_stream)
+        if code:
+            native.raise_device_error(code, what)
+
+    def clear_device_error(self):
+        """Reset the device error flag (after a failure was handled), -> the code it held."""
+        return native.device_error(self._ref, self.stream.cuda_stream, clear=True)
+
     def eval(self, pos, g_out, g_ref=None, weight=0.0, precond=-1.0, with_wl=True):
         """-> (|g - g_ref|^2, WA, HPWL, overflow sum, L1 of g over the cells), after a host sync."""
         native.call("gp103_eval", self._ref, self._p(pos), self._p(g_out),
                     None if g_ref is None else self._p(g_ref), float(weight), float(precond), int(bool(with_wl)),
                     self._p(self.scal), self.stream.cuda_stream)
+        if weight != 0.0:
+            self.check_device("gp103_eval")                  # (synchronises the stream)
         self.sync()
         return self.scal[:5].cpu().numpy()
 
@@ -397,6 +411,8 @@ class Placer(object):
                     break
             evals += int(Th[TI["evals"]])
             start_iters = int(Th[TI["loop_it"]])
+            if Th[TI["stop"]] == STOP_DEVICE_ERROR:
+                self.check_device("wirelength-only start")
             if Th[TI["stop"]]:
                 reason = REASON[int(Th[TI["stop"]])]
                 cur = int(self.cur.cpu())
@@ -459,6 +475,8 @@ class Placer(object):
         native.call("gp103_finish", self._ref, self.stream.cuda_stream)     # (after any batch still queued)
         self.sync()
         Sh = self.S.cpu().numpy()
+        if Sh[SK["stop"]] == STOP_DEVICE_ERROR:
+            self.check_device("density phase")
         cur = int(self.cur.cpu())
         pos = self.best if Sh[SK["has_best"]] else self.V[cur]
         return dict(reason=REASON[int(Sh[SK["stop"]])], iters=int(Sh[SK["loop_it"]]), start_iters=start_iters,

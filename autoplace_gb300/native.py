@@ -8,6 +8,10 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_ARG, ERR_CUDA, ERR_SHAPE = 0, 1, 2, 3
+OPT_PDL, OPT_WAIT_MS, OPT_TEST_STALL_FIELD = 0, 1, 2
+# the waits of the tensor-core field (gp103_device_error codes)
+DEVICE_ERRORS = {1: "a TMA stage's slot", 2: "an accumulator's buffer", 3: "a TMA stage's data",
+                 4: "an accumulator's result"}
 FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6, FIELD_F16X3 = 0, 1, 2, 3
 FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6, "f16x3": FIELD_F16X3}
 PHASE_START, PHASE_DENSITY = 0, 1
@@ -66,6 +70,7 @@ _SIGS = {
     "gp103_probe": ([ctypes.POINTER(Plan), _vp, _vp, _d, _vp, _vp, _vp], _i),
     "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
+    "gp103_device_error": ([ctypes.POINTER(Plan), _i, ctypes.POINTER(_i), _vp], _i),
     "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
     "gp103_net_order_scratch": ([_i, _i, _i], ctypes.c_size_t),
     "gp103_cluster_scratch": ([_i, _i, _i], ctypes.c_size_t),
@@ -118,6 +123,19 @@ def check(status, what):
 
 def call(name, *args):
     check(getattr(lib(), name)(*args), name)
+
+
+def device_error(plan_ref, stream_handle, clear=False):
+    """The plan's device error flag (0: none; else the tensor-core field wait that ran out, DEVICE_ERRORS), read after
+    the work queued on the stream; clear=True resets it."""
+    code = _i(0)
+    call("gp103_device_error", plan_ref, int(bool(clear)), ctypes.byref(code), stream_handle)
+    return int(code.value)
+
+
+def raise_device_error(code, what):
+    raise RuntimeError("%s: the tensor-core field gave up waiting for %s (device error %d); its outputs were not "
+                       "written" % (what, DEVICE_ERRORS.get(code, "?"), code))
 
 
 def exported_symbols():

@@ -67,11 +67,14 @@ class Netlist:
 
 
 PRESETS = {
-    # name: cells, nets, window, macros, macro cover, target density, overflow grid, force grid (0 = rule)
-    "c0": dict(cells=10_000, nets=10_500, window=200, macros=0, cover=0.0, target=1.0, num_bin=128, force_bin=0),
-    "c1": dict(cells=200_000, nets=210_000, window=200, macros=20, cover=0.15, target=0.9, num_bin=0, force_bin=512),
+    # name: cells, nets, window, macros, macro cover, target density, overflow grid, force grid (0 = rule), cluster
+    # ratio (5: two levels, the reference's default, main.py:44)
+    "c0": dict(cells=10_000, nets=10_500, window=200, macros=0, cover=0.0, target=1.0, num_bin=128, force_bin=0,
+               cluster_ratio=5.0),
+    "c1": dict(cells=200_000, nets=210_000, window=200, macros=20, cover=0.15, target=0.9, num_bin=0, force_bin=512,
+               cluster_ratio=5.0),
     "c2": dict(cells=1_200_000, nets=1_250_000, window=2000, macros=40, cover=0.20, target=0.8, num_bin=512,
-               force_bin=1024),
+               force_bin=1024, cluster_ratio=5.0),
 }
 
 
@@ -158,11 +161,12 @@ def make_netlist(cells, nets, window=200, macros=0, cover=0.0, util=0.7, fixed_p
 
 def preset(name, seed=0, **over):
     """Netlist of a preset (c0: 10k cells, c1: 200k cells + 20 macros, c2: 1.2M cells + 40 macros) and its run
-    options: -> (netlist, options dict with target, num_bin, force_bin)."""
+    options: -> (netlist, options dict with target_density, num_bin, force_num_bin, cluster_ratio)."""
     p = dict(PRESETS[name])
     p.update(over)
     nl = make_netlist(seed=seed, name="%s_s%d" % (name, seed), **p)
-    return nl, {"target_density": p["target"], "num_bin": p["num_bin"], "force_num_bin": p["force_bin"]}
+    return nl, {"target_density": p["target"], "num_bin": p["num_bin"], "force_num_bin": p["force_bin"],
+                "cluster_ratio": p["cluster_ratio"]}
 
 
 def init_positions(nl, num_nodes, seed=0):

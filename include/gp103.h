@@ -25,17 +25,26 @@ enum {
     GP103_ERR_ARG = 1,       /* a size or pointer the kernels cannot take */
     GP103_ERR_CUDA = 2,      /* a launch failed (cudaGetLastError) */
     GP103_ERR_SHAPE = 3,     /* a grid the tensor-core field does not support */
-    GP103_ERR_TOO_LARGE = 4  /* a grid larger than the fixed scratch of gp103_density_map_noalloc */
+    GP103_ERR_TOO_LARGE = 4  /* a size beyond a fixed limit of the library: the grid of gp103_density_map_noalloc
+                              * (nbx * nby <= 262,144 bins), the 16,777,215 pins, nets or cells of the device
+                              * problem build and of the net order */
 };
 
 /* Library version and the status text of an error code. */
 int gp103_version(void);
 const char* gp103_status_string(int status);
 
-/* Process-wide options. GP103_OPT_PDL (default 1): launch with programmatic dependent launch, so that each kernel of
- * a pass is launched while the previous one finishes (and graph edges become programmatic edges); 0 = plain
- * stream order. */
-enum { GP103_OPT_PDL = 0 };
+/* Process-wide options, read when a kernel is launched (a CUDA graph keeps the values of its capture).
+ * GP103_OPT_PDL (default 1): launch with programmatic dependent launch, so that each kernel of a pass is launched
+ *   while the previous one finishes (and graph edges become programmatic edges); 0 = plain stream order.
+ * GP103_OPT_WAIT_MS (default 2000, 1 .. 60000): how long a wait of the tensor-core field (a TMA stage, an MMA, an
+ *   accumulator) may take before the kernel gives it up: it then records the failure in the plan's device error
+ *   flag (gp103_device_error), waits (at most 2 s) for its own copies and MMAs already in flight, frees its tensor
+ *   memory and returns; later waits of the same launch give up at once, and no output is stored.
+ * GP103_OPT_TEST_STALL_FIELD (default 0): a test hook. 1 = the field's TMA producer issues no load, so that every
+ *   wait of the tensor-core field runs out (after GP103_OPT_WAIT_MS) with nothing in flight; it exists to test how
+ *   a failure reaches the caller without faulting the GPU. */
+enum { GP103_OPT_PDL = 0, GP103_OPT_WAIT_MS = 1, GP103_OPT_TEST_STALL_FIELD = 2 };
 int gp103_set_option(int option, int value);
 
 /* Kernel launches issued through this library so far (a launch captured into a CUDA graph counts once). */
@@ -74,7 +83,9 @@ int gp103_density_map(const float* pos, const float* size, const float* ratio, i
  * limited to nbx * nby <= 262,144 bins (GP103_ERR_TOO_LARGE beyond, before any work). It allocates nothing: no
  * cudaMalloc, cudaFree or allocating library call. The first call on a device looks up the array's address
  * (make it before any stream capture); every call clears the part of the array it uses, all calls share the array,
- * and calls whose work overlaps on the GPU race on it. */
+ * and calls whose work overlaps on the GPU race on it. `stream` must belong to the current device (GP103_ERR_ARG
+ * otherwise). The address stays cached for the process: after cudaDeviceReset of a device, do not call this entry
+ * point on that device again. */
 int gp103_density_map_noalloc(const float* pos, const float* size, const float* ratio, int num_nodes, int num_mov,
                               float bx, float by, int nbx, int nby, const float* fixed, float target, float* rho,
                               float* over, cudaStream_t stream);
@@ -232,6 +243,14 @@ int gp103_event_destroy(void* event);
 
 /* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
 int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
+
+/* The plan's device error flag: 0, or the wait of the tensor-core field that ran out first (1 = a TMA stage's
+ * slot, 2 = an accumulator's buffer, 3 = a TMA stage's data, 4 = an accumulator's result). The flag is set by the
+ * field's kernels (the outputs of that launch are not written), cleared by gp103_field_constants and, with
+ * clear != 0, here. The control kernel of every pass reads it: a set flag stops the run with stop reason 6 (S[14]
+ * in the density phase, T[GP103_T_STOP] in the start phase). Copies the flag to *code after the work queued on
+ * `stream` (a host synchronisation of the stream). Always 0 in field mode GP103_FIELD_FP32 (no bounded waits). */
+int gp103_device_error(const gp103_plan* plan, int clear, int* code, cudaStream_t stream);
 
 /* Set-up of the fused path on the device: the nets of the optimised pin set (Wirelength._pin_set,
  * src/core/wa_wirelength_hpwl.py:38-46; net_start [num_nets + 1], pin_cell [num_pins] with num_mov for a fixed pin,

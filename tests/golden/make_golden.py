@@ -1,8 +1,8 @@
 """Generate the golden fixtures of tests/golden/ from AutoPlace's own PyTorch operators (its CPU path).
 
-Run in a checkout that has the AutoPlace sources (default: /root/reference, or $AUTOPLACE_REF):
+Run with the path of a checkout of the AutoPlace sources (an argument, or $AUTOPLACE_REF):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <autoplace checkout>
 
 It imports the reference with its compiled modules absent (gp_cuda = None), i.e. exactly the `--gpu -1` code path,
 feeds it seeded synthetic inputs from autoplace_gb300.synth, and stores inputs and outputs as small .npz files. The
@@ -26,7 +26,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("AUTOPLACE_REF", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AUTOPLACE_REF")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("usage: python tests/golden/make_golden.py <path of the AutoPlace sources> (or set AUTOPLACE_REF)")
 sys.path.insert(0, REPO)
 sys.path.insert(0, REF)
 

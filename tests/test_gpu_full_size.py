@@ -138,3 +138,53 @@ def test_full_size_placement_is_deterministic_and_judged_exactly(c2):
     r3 = Placer(dp).run(pos0)
     assert r3["iters"] == r1["iters"]
     assert np.array_equal(r3["pos"].cpu().numpy().view(np.uint32), p1.view(np.uint32))
+
+
+# ------------------------------------------------------------------------------------------------ field precision
+def _states(nl, prob, pos0):
+    """Density states of a real placement of this netlist: the start (every cell in a cloud of 0.1 % of the region's
+    side, its hottest bins far above the target), a state mid-run (the run cut at 150 iterations, overflow still
+    high), and the final placement."""
+    import copy
+    from autoplace_gb300.engine import Placer
+    gr = prob.force
+    out = {"start": np.clip(pos0, gr.pos_lo, gr.pos_hi).astype(np.float32)}
+    mid = copy.copy(prob)
+    mid.opts = problem.options(**dict(vars(prob.opts), inner_iter=150))
+    r = Placer(mid).run(pos0)
+    assert r["reason"] == "max_iter"
+    out["mid"] = r["pos"].cpu().numpy()
+    out["final"] = Placer(prob).run(pos0)["pos"].cpu().numpy()
+    return out
+
+
+@pytest.fixture(scope="module")
+def c2_states(c2):
+    nl, prob, pos0 = c2
+    return _states(nl, prob, pos0)
+
+
+@pytest.mark.parametrize("state", ["start", "mid", "final"])
+@pytest.mark.parametrize("mode,tol", [(native.FIELD_F16X3, 1e-6), (native.FIELD_BF16X6, 1e-6)])
+def test_full_size_field_error_on_real_states(c2, c2_states, state, mode, tol):
+    """The tensor-core field of the 1024 x 1024 force grid against float64 (the cosine-transform statement of the
+    reference's mirrored FFT) on the densities of a real run: max |E - E64| / max |E64| <= 1e-6. The density plane
+    is the run's own (the float32 total density of the fixed-point map)."""
+    import ctypes
+    from tests.test_gpu_ops import _field_plan
+    nl, prob, _ = c2
+    gr = prob.force
+    pos = c2_states[state]
+    _, rho, _ = _native_map(pos, gr.size, gr.ratio, prob.num_mov, gr)
+    a = np.ascontiguousarray(rho[:gr.nbx, :gr.nby])
+    pl, keep = _field_plan(gr.nbx, mode, bx=gr.bx, by=gr.by)
+    ex, ey = torch.zeros((gr.nbx, gr.nby), device=DEV), torch.zeros((gr.nbx, gr.nby), device=DEV)
+    d = cu(a)
+    native.call("gp103_field", ctypes.byref(pl), d.data_ptr(), ex.data_ptr(), ey.data_ptr(),
+                torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    fx, fy = O.field_dct(a, gr.bin_np)
+    scale = max(np.abs(fx).max(), np.abs(fy).max())
+    err = max(np.abs(ex.cpu().numpy() - fx).max(), np.abs(ey.cpu().numpy() - fy).max()) / scale
+    print("field error %s mode %d: %.3e (peak density %.4g)" % (state, mode, err, a.max()))
+    assert err <= tol, err

@@ -4,7 +4,7 @@ import math
 import numpy as np
 import pytest
 
-from autoplace_gb300 import problem, synth
+from autoplace_gb300 import native, problem, synth
 from oracle import gp_oracle as O
 
 torch = pytest.importorskip("torch")
@@ -174,3 +174,25 @@ def test_two_levels_single_level_when_ratio_is_one(gold):
     r = Placer(prob, field="fp32").run(g["pos0"])
     assert "clusters" not in st and st["iters"] == r["iters"] and st["stop_reason"] == r["reason"]
     assert np.array_equal(st["pos"].cpu().numpy(), r["pos"].cpu().numpy())
+
+
+def test_c0_two_levels_match_oracle_with_tensor_core_field():
+    """The 10,000-cell netlist as its configuration states it: cluster_ratio 5 (the reference's default, two levels),
+    the cells' 128 x 128 force grid in f16x3 on the tensor cores (the clusters' smaller grid in fp32), against the
+    oracle's two-level CPU run (float64, the field as cosine transforms): the same clusters and cluster grid, the
+    same stop, HPWL within 0.5 %, and the control's overflow under the stop target."""
+    from autoplace_gb300.flow import global_placement
+    nl, o = synth.preset("c0")
+    prob = problem.Problem(nl, problem.options(**o))
+    assert prob.opts.cluster_ratio == 5.0
+    pos0 = synth.init_positions(nl, prob.num_nodes, seed=0)
+    st = global_placement(prob, pos0, field="f16x3")
+    assert st["placer"].mode == native.FIELD_F16X3
+    ref = O.two_level(prob, pos0)
+    assert st["clusters"] == ref["clusters"] and st["coarse_num_bin"] == ref["coarse_num_bin"]
+    assert st["stop_reason"] == ref["reason"] == "converged"
+    h = O.hpwl_all(st["pos"].cpu().numpy(), prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
+    hr = O.hpwl_all(ref["pos"], prob.all_cell, prob.all_off, prob.all_net_start, prob.num_mov)
+    assert abs(h - hr) <= 0.005 * hr, (h, hr)
+    assert st["overflow"] < prob.opts.stop_overflow
+    assert abs(st["iters"] - ref["iters"]) <= 0.1 * ref["iters"], (st["iters"], ref["iters"])

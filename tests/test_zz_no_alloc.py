@@ -72,3 +72,25 @@ def test_no_alloc_rejects_grids_beyond_its_scratch():
                                                 rho.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert st == 4
     assert "262144" in native.lib().gp103_status_string(st).decode()
+
+
+def test_no_alloc_at_the_limit_and_with_no_nodes():
+    """A grid of exactly 262,144 bins (512 x 512, the array's size) is bit-identical to gp103_density_map; then a call
+    with no nodes after it gives the fixed map alone (the array's leftover sums are cleared)."""
+    prob, gr, pos = _case(6, 30000, 512)
+    assert gr.nbx * gr.nby == 262144
+    args = _inputs(prob, gr, pos)
+    want_rho, want_over = _with_scratch(prob, gr, args)
+    got_rho, got_over = _no_alloc(prob, gr, args)
+    torch.cuda.synchronize()
+    assert torch.equal(got_rho, want_rho) and torch.equal(got_over, want_over)
+    p, s, r, f = args
+    empty = (p[:0], s[:0], r[:0], f)
+    want_rho, want_over = _with_scratch(prob, gr, empty)
+    got_rho, got_over = _no_alloc(prob, gr, empty)
+    torch.cuda.synchronize()
+    assert torch.equal(got_rho, want_rho) and torch.equal(got_over, want_over)
+    fixed = f.cpu().numpy()
+    half = got_rho.cpu().numpy()[:gr.nbx, :gr.nby]
+    assert np.array_equal(half, fixed)                           # no charge: the density is the fixed map
+    assert np.array_equal(got_over.cpu().numpy(), np.maximum(fixed - np.float32(gr.target), 0).astype(np.float32))
