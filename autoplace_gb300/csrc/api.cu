@@ -184,6 +184,7 @@ static FieldLayout layout_of(const gp103_plan* p) {
     FieldLayout L = field_layout(p->nbx, p->nby, p->field_mode);
     L.bx = p->bx;
     L.by = p->by;
+    L.shift = p->field_shift;
     return L;
 }
 
@@ -196,7 +197,8 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(ovf_scale), OFF(jsize), OFF(jratio), OFF(jfixed), OFF(jbx), OFF(jby), OFF(jovf_scale), OFF(field_const),
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
         OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
-        OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid), OFF(net_two), OFF(net_three)};
+        OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid), OFF(net_two), OFF(net_three),
+        OFF(field_shift)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -333,6 +335,7 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
     pj.nbx = p->nbx;
     pj.nby = p->nby;
     pj.with_fill = 1;
+    pj.shift = p->field_shift;
     if (p->field_mode == GP103_FIELD_FP32) {
         pj.dens = (float*)((char*)p->field_work + L.w_a);
     } else {

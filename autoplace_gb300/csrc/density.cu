@@ -367,7 +367,7 @@ __device__ __forceinline__ void post_fold(const PostJob& j, int bid, int nblk, f
         float sv[4], tv[4], ms = 0.f, mt = 0.f;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            sv[k] = __fadd_rn(r[0][k], r[1][3 - k]);
+            sv[k] = __fadd_rn(__fsub_rn(r[0][k], j.shift), __fsub_rn(r[1][3 - k], j.shift));
             tv[k] = __fsub_rn(r[0][k], r[1][3 - k]);
             ms = fmaxf(ms, fabsf(sv[k]));
             mt = fmaxf(mt, fabsf(tv[k]));
@@ -437,6 +437,8 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
             r[1] = __fadd_rn(mov[1], unfixed32(m1a.y));
             r[2] = __fadd_rn(mov[2], unfixed32(m1b.x));
             r[3] = __fadd_rn(mov[3], unfixed32(m1b.y));
+#pragma unroll
+            for (int k = 0; k < 4; k++) r[k] = __fsub_rn(r[k], j.shift);
             if (j.dens) *(float4*)(j.dens + b) = make_float4(r[0], r[1], r[2], r[3]);
             if (j.exps) {
                 // a 64-bin chunk of a row is 16 consecutive quads: half a warp (the loop keeps whole warps, since
@@ -480,7 +482,7 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
         const float o = fmaxf(__fsub_rn(mov, j.target), 0.f);
         if (EXACT) ovd += (double)o; else ov += o;
         if (j.with_fill) {
-            const float r = __fadd_rn(mov, unfixed32(j.map[nb + b]));
+            const float r = __fsub_rn(__fadd_rn(mov, unfixed32(j.map[nb + b])), j.shift);
             if (j.dens) j.dens[b] = r;
             if (j.t0) split_bf16(r, j.terms, j.t0, j.t1, j.t2, b);
             j.map[nb + b] = 0ull;

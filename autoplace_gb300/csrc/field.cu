@@ -108,7 +108,7 @@ __global__ void weight_table_kernel(int n, int nbx, int nby, double bin, double 
 }
 
 FieldLayout field_layout(int nbx, int nby, int mode) {
-    FieldLayout L;
+    FieldLayout L = {};
     L.nbx = nbx;
     L.nby = nby;
     L.mode = mode;

@@ -18,6 +18,7 @@ struct FieldLayout {
     int nbx, nby, mode;
     bool fold;
     double bx, by;
+    float shift;                // subtracted from a float32 density before the transforms (the same field)
     size_t c_cx, c_cy, c_cyt, c_sxt, c_syt, c_cxt, c_wx, c_wy, c_wrow, c_wcol, const_bytes;
     size_t w_a, w_tt, w_kx, w_ky, w_pt, w_qt, w_err;
     size_t e_a, e_tt, e_kx, e_ky, e_pt, e_qt, work_bytes;     // f16x3 chunk exponents (signed char)

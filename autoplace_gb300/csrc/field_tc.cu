@@ -835,11 +835,11 @@ static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t
     return GP103_ERR_ARG;                                        // no other combination is used
 }
 
-__global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t) {
+__global__ void split_density_kernel(const float* d, size_t n, float shift, __nv_bfloat16* t) {
     pdl_wait();
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
         __nv_bfloat16 a, b, c;
-        split3(d[e], a, b, c);
+        split3(__fsub_rn(d[e], shift), a, b, c);
         t[e] = a;
         t[n + e] = b;
         t[2 * n + e] = c;
@@ -848,13 +848,15 @@ __global__ void split_density_kernel(const float* d, size_t n, __nv_bfloat16* t)
 
 // f16x3: a float32 density [nbx][nby] into two float16 terms, each row's 64-bin chunks scaled by their own power of
 // two (one warp per chunk, two bins per lane), the exponents in e[(y / 64) * nbx + x]
-__global__ void split_density_f16_kernel(const float* d, int nbx, int nby, __half* t, signed char* e) {
+__global__ void split_density_f16_kernel(const float* d, int nbx, int nby, float shift, __half* t, signed char* e) {
     pdl_wait();
     const int lane = threadIdx.x & 31;
     const long long chunks = (long long)nbx * nby / 64, n = (long long)nbx * nby;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long c = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
-        const float2 v = *(const float2*)(d + 64 * c + 2 * lane);
+        float2 v = *(const float2*)(d + 64 * c + 2 * lane);
+        v.x = __fsub_rn(v.x, shift);
+        v.y = __fsub_rn(v.y, shift);
         float mx = fmaxf(fabsf(v.x), fabsf(v.y));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -876,7 +878,8 @@ __global__ void split_density_f16_kernel(const float* d, int nbx, int nby, __hal
 // t = d(y) - d(nby-1-y) for y < nby/2, each [nbx][nby/2] as two float16 terms per 64-value chunk of a row scaled by
 // its own power of two (one warp per chunk of s and the same chunk of t, two values per lane): planes s0, s1, t0, t1
 // of nbx * nby/2 values from `out` on; exponents of s in e[(y / 64) * nbx + x] (y < nby/2), of t behind them.
-__global__ void split_density_fold_kernel(const float* d, int nbx, int nby, __half* out, signed char* e) {
+__global__ void split_density_fold_kernel(const float* d, int nbx, int nby, float shift, __half* out,
+                                          signed char* e) {
     pdl_wait();
     const int lane = threadIdx.x & 31, hy = nby / 2;
     const long long chunks = (long long)nbx * hy / 64, hn = (long long)nbx * hy;
@@ -887,7 +890,8 @@ __global__ void split_density_fold_kernel(const float* d, int nbx, int nby, __ha
         const float* row = d + x * nby;
         const float2 lo = *(const float2*)(row + y);
         const float h0 = row[nby - 1 - y], h1 = row[nby - 2 - y];
-        const float s0 = __fadd_rn(lo.x, h0), s1 = __fadd_rn(lo.y, h1);
+        const float s0 = __fadd_rn(__fsub_rn(lo.x, shift), __fsub_rn(h0, shift));
+        const float s1 = __fadd_rn(__fsub_rn(lo.y, shift), __fsub_rn(h1, shift));
         const float t0 = __fsub_rn(lo.x, h0), t1 = __fsub_rn(lo.y, h1);
         float ms = fmaxf(fabsf(s0), fabsf(s1)), mt = fmaxf(fabsf(t0), fabsf(t1));
 #pragma unroll
@@ -928,16 +932,18 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     auto E = [&](size_t off) { return f16 ? (signed char*)(w + off) : (signed char*)nullptr; };
     if (density && L.fold) {
         if (launch_k(split_density_fold_kernel, dim3(grid_for((size_t)X * Y / 4, 256, 8)), dim3(256), 0, s, density,
-                     X, Y, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
+                     X, Y, L.shift, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     } else if (density && f16) {
         if (launch_k(split_density_f16_kernel, dim3(grid_for((size_t)X * Y / 2, 256, 8)), dim3(256), 0, s, density, X,
-                     Y, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
+                     Y, L.shift, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     } else if (density) {
-        if (launch_k(split_density_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density, (size_t)X * Y, B(w, L.w_a)) != cudaSuccess) return GP103_ERR_CUDA;
+        if (launch_k(split_density_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density,
+                     (size_t)X * Y, L.shift, B(w, L.w_a)) != cudaSuccess)
+            return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
     auto prob = [](int M, int N, int K, int epi) {

@@ -105,6 +105,10 @@ struct PostJob {
                                 // of y (post_fold), for the folded first transform of the field
     int exact;                  // float64 per-thread partials of the sum (evaluators); 0: float32 (hot path)
     Reduce red;                 // sum of the density above the target
+    float shift;                // subtracted from the density that goes to the field (dens / terms): the field of a
+                                // density and of the density minus a constant are the same (only the zero frequency
+                                // changes, and the field drops it); with the mean density, the transforms' rounding
+                                // follows the density's variation instead of its mean
 };
 
 struct PostPair {

@@ -29,6 +29,7 @@ STOP_DEVICE_ERROR = 6
 
 
 START_EVERY = 4        # passes per poll of the wirelength-only start
+_GRAPH_LAUNCHES = {"captured": 0, "replayed": 0}        # libgp103 launches inside CUDA graphs, all Placers
 SHORT_NET = 8          # nets of up to this many pins are done one per thread (WA_REG of the kernel)
 MID_NET = 16           # nets of up to this many pins (and more than SHORT_NET) are done by 4 lanes each
 
@@ -59,6 +60,12 @@ def net_order(net_start, cell32, cell_pin):
             int((cls < 1).sum()), int((cls < 2).sum()))
 
 
+def launches():
+    """Kernels of libgp103 executed so far by this process, every Placer's graph replays counted launch by launch
+    (a captured launch counts when its graph replays, not when it is captured)."""
+    return native.launch_count() - _GRAPH_LAUNCHES["captured"] + _GRAPH_LAUNCHES["replayed"]
+
+
 def field_mode(mode, nbx, nby):
     """The field mode a grid of nbx x nby bins runs in: `mode`, or fp32 where the tensor-core field cannot tile the
     grid (gp103_plan_sizes answers GP103_ERR_SHAPE)."""
@@ -69,6 +76,17 @@ def field_mode(mode, nbx, nby):
         return native.FIELD_FP32
     native.check(rc, "gp103_plan_sizes")
     return mode
+
+
+def mean_density(prob):
+    """The force grid's mean density: the nodes' area over the bin area plus the fixed map, over the bins. Every node
+    stays inside the region (positions are clamped), so this is the mean of every pass's density map; it is the
+    field's shift (gp103_plan.field_shift)."""
+    f = prob.force
+    area = prob.area
+    total = float(area.double().sum()) if torch.is_tensor(area) else float(np.asarray(area, np.float64).sum())
+    fixed = float(np.asarray(f.fixed_map, np.float64).sum())
+    return (total / f.bin_area + fixed) / (f.nbx * f.nby)
 
 
 def _tensor(a, dt):
@@ -166,6 +184,7 @@ class Placer(object):
         for k in ("size", "ratio", "pins", "area", "lo", "hi"):
             setattr(pl, k, self._p(getattr(self, k)))
         pl.bx, pl.by, pl.target = f.bx, f.by, prob.target
+        pl.field_shift = mean_density(prob)
         self.fixed = self._hold(up("fixed", f.fixed_map, torch.float32))
         pl.fixed = self._p(self.fixed)
         pl.ovf_scale = f.bin_area / f.mov_area
@@ -290,15 +309,17 @@ class Placer(object):
                 self._passes(phase, k)
             per = native.launch_count() - before
             self._captured += per
+            _GRAPH_LAUNCHES["captured"] += per
             self._graphs[phase] = (g, per)
         g, per = self._graphs[phase]
         with torch.cuda.stream(self.stream):
             g.replay()
         self._replayed += per
+        _GRAPH_LAUNCHES["replayed"] += per
 
     def launches(self):
         """Kernels of libgp103 executed so far by this process (graph replays counted launch by launch)."""
-        return native.launch_count() - self._captured + self._replayed
+        return launches()
 
     def overflow_scale(self):
         return self.plan.jovf_scale if self.plan.jnbx > 0 else self.plan.ovf_scale

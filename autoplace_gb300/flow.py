@@ -27,63 +27,95 @@ def _gamma(base_gamma, overflow):
     return base_gamma * 10 ** ((overflow - 0.1) * 20 / 9 - 1)
 
 
+class Flow(object):
+    """A design's global placement, reusable: the cells' Placer is set up once and every run() places from a start
+    (the clusters, their problem and their Placer are made per run, as the reference makes them per placement).
+
+    field: the cells' field mode; coarse_field: the clusters' (default: the same; a grid the tensor cores cannot tile
+    runs in fp32). start: None = the reference's start (the clusters from the start positions with the wirelength-
+    only start); or a callable start(coarse, cplacer, cpos0, prob) -> (cluster positions [num + F, 2] on the device,
+    resume dict or None) that proposes the clusters' positions (and the density weight and smoothing to resume the
+    clusters' level with, ParamScheduler.resume) in place of the wirelength-only start."""
+
+    def __init__(self, prob, field="f16x3", coarse_field=None, device="cuda", check_every=16, use_graphs=True,
+                 stream=None, host=None):
+        self.prob = prob
+        self.dev = torch.device(device)
+        self.stream = stream or torch.cuda.Stream(self.dev)
+        self.kw = dict(device=self.dev, check_every=check_every, use_graphs=use_graphs, stream=self.stream)
+        self.field, self.coarse_field = field, coarse_field or field
+        self.fine = Placer(prob, field=field, host=host, **self.kw)
+        self.last_coarse = None
+
+    def run(self, pos0, log=None, start=None):
+        """Place from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
+        (stop_reason, iters, start_iters, gp_time_s, per_iter_s, grad_calls; with two levels also clusters,
+        cluster_time_s, coarse_num_bin, coarse_iters) plus pos (final positions on the device), hpwl and overflow of
+        the kept placement as the control measured them, and placer (the cells' Placer: placer.evaluate(pos) gives
+        the exact HPWL and overflow)."""
+        prob, fine, stream, dev = self.prob, self.fine, self.stream, self.dev
+        o, n = prob.opts, prob.num_mov
+        torch.cuda.synchronize(dev)
+        t0 = time.time()
+        stats, evals, resume, start_iters = {}, 0, None, 0
+        if o.cluster_ratio > 1:
+            coarse = cluster.coarse_problem(prob, device=dev, stream=stream)
+            cp = coarse.problem
+            stream.synchronize()
+            stats = dict(clusters=coarse.num, cluster_time_s=time.time() - t0, coarse_num_bin=cp.force.nbx)
+            if log:
+                log("two levels: %d clusters of %d cells (%.2fs), %d x %d bins"
+                    % (coarse.num, n, stats["cluster_time_s"], cp.force.nbx, cp.force.nby))
+            start_gamma = 10 * prob.base_gamma                      # the smoothing the cells start with
+            cplacer = Placer(cp, field=self.coarse_field, handover_gamma=start_gamma, **self.kw)
+            with torch.cuda.stream(stream):
+                p0 = torch.as_tensor(pos0, dtype=torch.float32).to(dev)
+                cpos0 = torch.cat([p0[:coarse.num], p0[n:]])
+            cresume = None
+            if start is not None:
+                t1 = time.time()
+                cpos0, cresume = start(coarse, cplacer, cpos0, prob)
+                stream.synchronize()
+                stats["start_time_s"] = time.time() - t1
+            level = cplacer.run(cpos0, log=log, resume=cresume)
+            cpos = level["pos"]
+            pos = cluster.expand(cpos, coarse, prob, o.seed, device=dev, stream=stream)
+            with torch.cuda.stream(stream):
+                torch.max(torch.min(pos, fine.hi), fine.lo, out=pos)
+            # the same share of the wire tension on both levels
+            tu_fine, ovf_fine = fine.tension_unit(pos)
+            tu_coarse = cplacer.tension_unit(cpos)[0]
+            weight = level["lam"] * tu_fine / tu_coarse
+            if o.wa_rule == "accuracy":                             # the same smoothing in units of the bin
+                gam = level["gam"] / cp.base_gamma * prob.base_gamma
+            else:
+                gam = _gamma(prob.base_gamma, ovf_fine)
+            resume = dict(lam=weight, gam=gam, iter=level["iter"], hpwl=fine.hpwl(pos), first_iter=level["iters"])
+            if log:
+                log("clusters placed after %d iterations (stop: %s, hpwl %.4E, overflow %.4f): the cells take over, "
+                    "density weight %.4E" % (level["iters"], level["reason"], level["hpwl"], level["overflow"],
+                                             weight))
+            evals, start_iters = level["evals"], level["start_iters"]
+            stats["coarse_iters"] = level["iters"]
+            stats["coarse_reason"] = level["reason"]
+            pos0 = pos
+            self.last_coarse = coarse
+            del cplacer, cp, cpos                                   # the clusters' buffers are not needed any more
+        level = fine.run(pos0, log=log, resume=resume)
+        torch.cuda.synchronize(dev)
+        gp_time, iters = time.time() - t0, level["iters"]
+        if log:
+            log("GP stop (%s): #iters %d hpwl: %.6E overflow: %.4f GP time: %.4fs per iter: %.6fs (%d gradient calls)"
+                % (level["reason"], iters, level["hpwl"], level["overflow"], gp_time, gp_time / max(iters, 1),
+                   evals + level["evals"]))
+        stats.update(stop_reason=level["reason"], iters=iters, start_iters=start_iters or level["start_iters"],
+                     gp_time_s=gp_time, per_iter_s=gp_time / max(iters, 1), grad_calls=evals + level["evals"],
+                     pos=level["pos"], hpwl=level["hpwl"], overflow=level["overflow"], placer=fine)
+        return stats
+
+
 def global_placement(prob, pos0, field="f16x3", device="cuda", log=None, check_every=16, use_graphs=True,
-                     stream=None):
-    """Place prob from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
-    (stop_reason, iters, start_iters, gp_time_s, per_iter_s, grad_calls; with two levels also clusters,
-    cluster_time_s, coarse_num_bin, coarse_iters) plus pos (final positions on the device), hpwl and overflow
-    of the kept placement as the control measured them, and placer (the cells' Placer: placer.evaluate(pos) gives
-    the exact HPWL and overflow)."""
-    o, n = prob.opts, prob.num_mov
-    dev = torch.device(device)
-    stream = stream or torch.cuda.Stream(dev)
-    torch.cuda.synchronize(dev)
-    start = time.time()
-    kw = dict(field=field, device=dev, check_every=check_every, use_graphs=use_graphs, stream=stream)
-    fine = Placer(prob, **kw)
-    stats, evals, resume, start_iters = {}, 0, None, 0
-    if o.cluster_ratio > 1:
-        coarse = cluster.coarse_problem(prob, device=dev, stream=stream)
-        cp = coarse.problem
-        stream.synchronize()
-        stats = dict(clusters=coarse.num, cluster_time_s=time.time() - start, coarse_num_bin=cp.force.nbx)
-        if log:
-            log("two levels: %d clusters of %d cells (%.2fs), %d x %d bins"
-                % (coarse.num, n, stats["cluster_time_s"], cp.force.nbx, cp.force.nby))
-        start_gamma = 10 * prob.base_gamma                      # the smoothing the cells start with
-        cplacer = Placer(cp, handover_gamma=start_gamma, **kw)
-        with torch.cuda.stream(stream):
-            p0 = torch.as_tensor(pos0, dtype=torch.float32).to(dev)
-            cpos0 = torch.cat([p0[:coarse.num], p0[n:]])
-        level = cplacer.run(cpos0, log=log)
-        cpos = level["pos"]
-        pos = cluster.expand(cpos, coarse, prob, o.seed, device=dev, stream=stream)
-        with torch.cuda.stream(stream):
-            torch.max(torch.min(pos, fine.hi), fine.lo, out=pos)
-        # the same share of the wire tension on both levels
-        tu_fine, ovf_fine = fine.tension_unit(pos)
-        tu_coarse = cplacer.tension_unit(cpos)[0]
-        weight = level["lam"] * tu_fine / tu_coarse
-        if o.wa_rule == "accuracy":                             # the same smoothing in units of the bin
-            gam = level["gam"] / cp.base_gamma * prob.base_gamma
-        else:
-            gam = _gamma(prob.base_gamma, ovf_fine)
-        resume = dict(lam=weight, gam=gam, iter=level["iter"], hpwl=fine.hpwl(pos), first_iter=level["iters"])
-        if log:
-            log("clusters placed after %d iterations (stop: %s, hpwl %.4E, overflow %.4f): the cells take over, "
-                "density weight %.4E" % (level["iters"], level["reason"], level["hpwl"], level["overflow"], weight))
-        evals, start_iters = level["evals"], level["start_iters"]
-        stats["coarse_iters"] = level["iters"]
-        pos0 = pos
-        del cplacer, coarse, cp, cpos                            # the clusters' buffers are not needed any more
-    level = fine.run(pos0, log=log, resume=resume)
-    torch.cuda.synchronize(dev)
-    gp_time, iters = time.time() - start, level["iters"]
-    if log:
-        log("GP stop (%s): #iters %d hpwl: %.6E overflow: %.4f GP time: %.4fs per iter: %.6fs (%d gradient calls)"
-            % (level["reason"], iters, level["hpwl"], level["overflow"], gp_time, gp_time / max(iters, 1),
-               evals + level["evals"]))
-    stats.update(stop_reason=level["reason"], iters=iters, start_iters=start_iters or level["start_iters"],
-                 gp_time_s=gp_time, per_iter_s=gp_time / max(iters, 1), grad_calls=evals + level["evals"],
-                 pos=level["pos"], hpwl=level["hpwl"], overflow=level["overflow"], placer=fine)
-    return stats
+                     stream=None, start=None):
+    """Place prob from pos0 ([num_nodes, 2], movable cells then fillers): Flow(prob, ...).run(pos0) (see Flow)."""
+    return Flow(prob, field=field, device=device, check_every=check_every, use_graphs=use_graphs,
+                stream=stream).run(pos0, log=log, start=start)

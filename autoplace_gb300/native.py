@@ -20,7 +20,7 @@ T = dict(alpha=0, a=1, iter=2, loop_it=3, done=4, stop=5, accept=6, hpwl=7, wa=8
          inner=12, ring=16)
 T_SIZE = 32
 
-_vp, _i, _f, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
+_vp, _i, _f, _d, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_size_t
 
 
 class Plan(ctypes.Structure):
@@ -41,6 +41,7 @@ class Plan(ctypes.Structure):
         ("pin_slot", _vp), ("net_split", _i),
         ("order", _vp), ("order_counts", _vp), ("order_cursor", _vp),
         ("net_mid", _i), ("net_two", _i), ("net_three", _i),
+        ("field_shift", _f),
     ]
 
 
@@ -89,6 +90,18 @@ _SIGS = {
     "gp103_smooth_nodes": ([_vp, _i, _i, _d, _d, _f, _f] + [_vp] * 7 + [_vp], _i),
     "gp103_net_order": ([_vp] * 4 + [_i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 5 + [_vp], _i),
     "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
+    # the learned start
+    "gp103_learn_graph_scratch": ([_i, _i], _sz),
+    "gp103_learn_graph": ([_vp] * 4 + [_i, _i, _i, _vp, _sz] + [_vp] * 6 + [_vp], _i),
+    "gp103_seg_gather": ([_vp, _i, _vp, _vp, _vp, _i, _i, _vp, _vp], _i),
+    "gp103_dense_fwd": ([_vp, _i, _i, _vp, _i, _vp, _vp, _vp, _i, _i, _vp, _vp], _i),
+    "gp103_dense_bwd_scratch": ([_i, _i, _i], _sz),
+    "gp103_dense_bwd": ([_vp, _i, _i, _vp, _i, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp,
+                         _vp], _i),
+    "gp103_mse": ([_vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
+    "gp103_adam": ([_vp, _vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _i, _f, _vp], _i),
+    "gp103_learn_features_scratch": ([_i, _i], _sz),
+    "gp103_learn_features": ([_vp] * 4 + [_i, _i, _i] + [_vp] * 6 + [_d, _f, _f, _i, _vp, _sz, _vp, _vp], _i),
 }
 EVAL_SCRATCH_BYTES = 16640
 

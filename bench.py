@@ -1,23 +1,26 @@
-"""Benchmark: time to overflow 0.07 of one global-placement level of the 1.2M-cell synthetic netlist on a GB300.
+"""Benchmark: time to overflow 0.07 of a global placement of the 1.2M-cell synthetic netlist on a GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config c2] [--field f16x3]
+                    [--start auto|learned|plain]
 
 Workload (config "c2"): 1,200,000 cells, 1,250,000 nets (5.2M pins, degree mix 2/3/4-10/11-100), 40 macros over 20 %
-of the region, target density 0.8, force grid 1024 x 1024, overflow grid 512 x 512; seeded synthetic data (the
-ISPD suites are not available). One step = one whole level from the seeded start to the stop (wirelength-only start,
-first density weight, density phase until overflow < 0.07 + the settle iterations), inputs resident in HBM. The
-working set (pins, nodes, maps, field planes) is larger than the 129 MB L2, so no flush is needed between steps.
+of the region, target density 0.8, force grid 1024 x 1024, overflow grid 512 x 512, two levels (cluster ratio 5, the
+reference's default: the clusters first, then the cells); seeded synthetic data (the ISPD suites are not available).
+One step = one whole placement from the seeded start to the stop (clustering, the clusters' level, expansion, the
+cells' level until overflow < 0.07 + the settle iterations), inputs resident in HBM. The working set (pins, nodes,
+maps, field planes) is larger than the 129 MB L2, so no flush is needed between steps.
 
-Reported on one JSON line (rank 0): value = seconds per placement (lower is better), e2e = the same through the
-public API from the netlist's host arrays (upload, the problem's arrays built on the device, run, download of the
-placement), the roofline of the dominant kernel (CUDA
-events on its stream), a CPU baseline (the oracle's restatement of the reference's CPU iteration timed on a bounded
-sample of iterations of the same netlist, scaled by the iterations the GPU run needed), SM clocks during the timed
+Reported on one JSON line (rank 0): value = seconds per placement with the product's configuration (lower is better:
+the tensor-core field, and the learned start when a trained model is present), the plain method on the same GPU
+beside it (the reference's start and a float32 field), e2e = the same placement through the public API from the
+netlist's host arrays (upload, the problem's arrays built on the device, run, download of the placement), the
+roofline of the dominant kernel (CUDA events on its stream), a CPU baseline (the oracle's restatement of the
+reference's CPU iteration on the host cores, timed on a bounded sample of iterations), SM clocks during the timed
 region, and the number of libgp103 kernels launched.
 
---impl reference: the reference's CPU path restated by the oracle (the reference's own code is Python + torch and
-cannot run on the GPU machine), on the host cores, same metric and config; the iterations to the stop come from the
-GB300 run recorded in profiles/bench_iterations.json.
+--impl reference: the reference's CPU path (its --gpu -1 PyTorch operators) restated by the oracle on every host core
+(float32 operators, FFT field), one whole placement of the same netlist and flow to its own stop, timed in full: its
+own iterations, exact HPWL and overflow; the K steps of the line are K consecutive shares of that one placement.
 """
 import argparse
 import json
@@ -33,7 +36,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time-to-overflow 0.07 (s) at 1.2M cells, learned+TC vs plain, HPWL within 1%"
-ITER_FILE = os.path.join(ROOT, "profiles", "bench_iterations.json")
 
 
 def parse():
@@ -44,7 +46,13 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2")
     p.add_argument("--field", default="f16x3", choices=["f16x3", "bf16x6", "bf16x3", "fp32"])
-    p.add_argument("--cpu-iters", type=int, default=4, help="density-phase iterations of the CPU sample")
+    p.add_argument("--start", default="auto", choices=["auto", "learned", "plain"],
+                   help="the clusters' start: the learned proposal (auto: when a trained model is present) or the "
+                        "reference's wirelength-only start")
+    p.add_argument("--plain-field", default="fp32", help="field mode of the plain method beside the measurement")
+    p.add_argument("--plain-steps", type=int, default=2, help="timed placements of the plain method")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--cpu-iters", type=int, default=12, help="density-phase iterations of the CPU sample")
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-pdl", action="store_true", help="plain stream order instead of programmatic dependent launch")
@@ -153,29 +161,28 @@ def workload(cfg, seed):
     return prob, pos0
 
 
-def config_dict(prob, args, world):
+def config_dict(prob, args, world, start="plain"):
     nl = prob.nl
-    return {"workload": "synthetic %s: %d cells, %d nets, %d pins, %d macros, %d fillers; force grid %d, overflow grid %d"
-                        % (args.config, nl.num_mov, nl.num_nets, nl.num_pins, len(nl.macros),
-                           prob.num_nodes - prob.num_mov, prob.force_bin, prob.num_bin),
+    levels = 2 if prob.opts.cluster_ratio > 1 else 1
+    return {"workload": "synthetic %s: %d cells, %d nets, %d pins, %d macros, %d fillers; force grid %d, overflow grid "
+                        "%d; %d level(s)" % (args.config, nl.num_mov, nl.num_nets, nl.num_pins, len(nl.macros),
+                                             prob.num_nodes - prob.num_mov, prob.force_bin, prob.num_bin, levels),
             "cells": nl.num_mov, "nets": nl.num_nets, "pins": nl.num_pins, "nodes": prob.num_nodes,
             "force_grid": prob.force_bin, "overflow_grid": prob.num_bin, "target_density": prob.target,
-            "field": args.field, "levels": 1, "start": "plain (wirelength-only)",
-            "streams": 2 if args.split else 1,
+            "cluster_ratio": prob.opts.cluster_ratio, "levels": levels, "field": args.field,
+            "start": start, "streams": 2 if args.split else 1,
             "l2": "working set > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world}
 
 
 # ------------------------------------------------------------------------------------------------ CPU baseline
-def cpu_sample(prob, pos0, iters, gpu_iters):
-    """Time `iters` density-phase iterations of the oracle's CPU iteration (gradient at the density phase: WA,
-    density map, overflow grid, field by FFT of the mirrored map, gather; Nesterov step; control), after one
-    untimed warm-up iteration. -> (seconds per iteration, threads)."""
+def cpu_sample(prob, pos0, iters):
+    """Time `iters` density-phase iterations of the oracle's CPU iteration on every host core (float32 WA, density map,
+    overflow grid, field by FFT of the mirrored map, gather; Nesterov step; control), after two untimed warm-up
+    iterations. -> (seconds per iteration, threads)."""
     import numpy as np
-    import torch
     from oracle import gp_oracle as O
     threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    lvl = O.CpuLevel(prob, dtype=np.float32, field="fft")
+    lvl = O.CpuLevel(prob, dtype=np.float32, field="fft", threads=threads)
     gr = prob.force
     v = np.clip(np.asarray(pos0, np.float64), gr.pos_lo, gr.pos_hi)
     gam, lam = 10 * prob.base_gamma, 1e-4
@@ -187,22 +194,22 @@ def cpu_sample(prob, pos0, iters, gpu_iters):
     kp = np.array([gam, lam, lam, 1.0, 0.0], np.float32)
     c = prob.constants()
     t0 = None
-    for k in range(iters + 1):
-        if k == 1:
+    for k in range(iters + 2):
+        if k == 2:
             t0 = time.time()
         un, vn = O.nesterov_step(u, v, g, gr.pos_lo, gr.pos_hi, kp[3], kp[4])
         gn, wa, hpwl, ovf = lvl.grad(vn, float(kp[1]), float(kp[0]))
         O.control(S, kp, c, np.linalg.norm(vn - v), np.linalg.norm(gn - g), hpwl, ovf, wa)
         u, v, g = un, vn, gn
-    per = (time.time() - t0) / iters
-    return per, threads
+    return (time.time() - t0) / iters, threads
 
 
-def cpu_baseline_dict(per, threads, iters, gpu_iters, source):
-    return {"value": per * gpu_iters, "unit": "s", "cores": threads, "kind": "port",
-            "sample": "%d density-phase iterations of the oracle CPU iteration (restating the reference's --gpu -1 "
-                      "path, FFT field) on the full netlist: %.3f s/iter x %d iterations to the stop (%s)"
-                      % (iters, per, gpu_iters, source)}
+def cpu_baseline_dict(per, threads, iters, gpu_iters):
+    return {"value": round(per * gpu_iters, 3), "unit": "s", "cores": threads, "kind": "port",
+            "sample": "%d density-phase iterations of the oracle's CPU iteration (the reference's --gpu -1 path "
+                      "restated: float32 operators, FFT field) on the cells of the full netlist, on %d host threads: "
+                      "%.4f s/iter x the %d iterations of this GB300 placement (a bounded sample; bench.py --impl "
+                      "reference runs the CPU placement to its own stop)" % (iters, threads, per, gpu_iters)}
 
 
 # ------------------------------------------------------------------------------------------------ roofline
@@ -301,48 +308,86 @@ def load_peaks():
 
 
 # ------------------------------------------------------------------------------------------------ arms
+def _start_hook(args):
+    """The clusters' start of the product's configuration -> (hook for Flow.run or None, name)."""
+    want = args.start
+    if want == "plain":
+        return None, "plain (wirelength-only)"
+    try:
+        from autoplace_gb300 import learn
+    except ImportError:
+        learn = None
+    if want == "auto" and (learn is None or not learn.model_available()):
+        return None, "plain (wirelength-only)"
+    return learn.Proposal(learn.load_model()).hook, "learned (message-passing proposal of the cluster positions)"
+
+
+def _timed_runs(flow, pos, steps, start=None):
+    """`steps` placements, CUDA events on the flow's stream around them -> (seconds per placement, last stats, wall)."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(flow.stream)
+    t0 = time.time()
+    st = None
+    for _ in range(steps):
+        st = flow.run(pos, start=start)
+    ev1.record(flow.stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1000.0 / max(steps, 1), st, time.time() - t0
+
+
 def run_gb300(args):
     import numpy as np
     import torch
-    from autoplace_gb300.engine import Placer
+    from autoplace_gb300 import engine
+    from autoplace_gb300.flow import Flow
     rank, world, local = dist_setup()
     if args.no_pdl:
         from autoplace_gb300 import native
         native.call("gp103_set_option", 0, 0)
     prob, pos0 = workload(args.config, seed=rank)
-    placer = Placer(prob, field=args.field, split=args.split)
+    start, start_name = _start_hook(args)
+    flow = Flow(prob, field=args.field)
     dpos = torch.tensor(pos0, device="cuda")
-    r = None
     for _ in range(max(args.warmup, 0)):
-        r = placer.run(dpos)
+        flow.run(dpos, start=start)
     torch.cuda.synchronize()
     barrier(world)
     clocks = Clocks(local)
     clocks.start()
-    l0 = placer.launches()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(placer.stream)
-    t0 = time.time()
-    runs = []
-    for _ in range(args.steps):
-        runs.append(placer.run(dpos))
-    ev1.record(placer.stream)
-    torch.cuda.synchronize()
-    wall = time.time() - t0
+    l0 = engine.launches()
+    step_s, last, wall = _timed_runs(flow, dpos, args.steps, start)
+    launches = engine.launches() - l0
     barrier(world)
     clk = clocks.stop()
-    launches = placer.launches() - l0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    step_s = reduce_max(ms / 1000.0, world)
-    last = runs[-1]
+    step_s = reduce_max(step_s, world)
     iters = last["iters"]
-    hpwl_exact, overflow_exact = placer.evaluate(last["pos"])
+    hpwl_exact, overflow_exact = flow.fine.evaluate(last["pos"])
+    result = {"stop": last["stop_reason"], "iterations": iters, "start_iterations": last["start_iters"],
+              "clusters": last.get("clusters"), "cluster_iterations": last.get("coarse_iters"),
+              "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "overflow_exact": overflow_exact,
+              "ms_per_iteration": round(step_s * 1000 / max(iters, 1), 4),
+              "wall_s_per_step": round(wall / max(args.steps, 1), 4)}
+
+    # the plain method on the same GPU: the reference's start (wirelength-only) and a float32 field
+    plain = None
+    if not args.no_plain:
+        pflow = Flow(prob, field=args.plain_field)
+        pflow.run(dpos)                                                     # warm-up (graphs, set-up)
+        p_s, pst, _ = _timed_runs(pflow, dpos, args.plain_steps)
+        ph, po = pflow.fine.evaluate(pst["pos"])
+        plain = {"value": round(p_s, 4), "unit": "s", "field": args.plain_field, "start": "plain (wirelength-only)",
+                 "stop": pst["stop_reason"], "iterations": pst["iters"], "hpwl_exact": ph, "overflow": pst["overflow"],
+                 "overflow_exact": po, "steps": args.plain_steps}
+        result["speedup_vs_plain"] = round(p_s / step_s, 3)
+        result["hpwl_vs_plain"] = round(hpwl_exact / ph, 5)
+        del pflow
 
     # e2e: from the netlist's pinned host arrays through the public API: upload, the problem's arrays built on the
-    # device (net CSR, cell order, smoothed nodes), the device set-up of the Placer, the run, the download of the
-    # placement. The host part of the problem (grids, fixed fractions, fillers: the reader's and initializer's
-    # work) is made once, before.
+    # device (net CSR, cell order, smoothed nodes), the cells' Placer and the flow, the run (the clusters' pins are
+    # uploaded again by the clustering), the download of the placement. The host part of the problem (grids, fixed
+    # fractions, fillers: the reader's and initializer's work) is made once, before.
     from autoplace_gb300.problem import Problem, netlist_arrays
     base = Problem(prob.nl, prob.opts, arrays=False)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
@@ -354,6 +399,8 @@ def run_gb300(args):
     out = torch.empty(host_pos.shape, dtype=torch.float32).pin_memory()
     h2d = sum(x.numel() * x.element_size() for x in list(host.values()) + list(maps.values())) + \
         host_pos.numel() * 4 + len(prob.constants()) * 8
+    if prob.opts.cluster_ratio > 1:
+        h2d += 16 * prob.nl.num_pins                     # the clustering's pin upload (cell, net, offset)
     d2h = out.numel() * 4
     # one untimed step first: it loads the device-build kernels, which only this path uses (a one-time cost per
     # process, like the warm-up placements of the device-timed loop)
@@ -361,41 +408,29 @@ def run_gb300(args):
     for i in range(1 + args.e2e_steps):
         torch.cuda.synchronize()
         t = time.time()
-        dprob = base.on_device(stream=placer.stream, host=host)
-        pl2 = Placer(dprob, field=args.field, stream=placer.stream, host=maps, split=args.split)
-        rr = pl2.run(host_pos)
+        dprob = base.on_device(stream=flow.stream, host=host)
+        f2 = Flow(dprob, field=args.field, stream=flow.stream, host=maps)
+        rr = f2.run(host_pos, start=start)
         out.copy_(rr["pos"])
         torch.cuda.synchronize()
         if i > 0:
             e2e_s.append(time.time() - t)
-        del pl2, dprob
+        del f2, dprob, rr
     e2e = reduce_max(statistics.median(e2e_s), world)
 
-    prof, _ = profile_pass(placer)
+    prof, _ = profile_pass(flow.fine)
     peaks = load_peaks()
     roof, table = roofline(prob, args.field, prof, peaks, args.config)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        per, threads = cpu_sample(prob, pos0, args.cpu_iters, iters)
-        cpu = cpu_baseline_dict(per, threads, args.cpu_iters, iters, "iterations of this GB300 run")
-    if rank == 0:
-        os.makedirs(os.path.dirname(ITER_FILE), exist_ok=True)
-        try:
-            with open(ITER_FILE, "w") as f:
-                json.dump({"config": args.config, "iterations": iters, "start_iters": last["start_iters"],
-                           "reason": last["reason"], "field": args.field}, f)
-        except OSError:
-            pass
+        per, threads = cpu_sample(prob, pos0, args.cpu_iters)
+        cpu = cpu_baseline_dict(per, threads, args.cpu_iters, iters)
     line = {"metric": METRIC, "value": round(step_s, 4), "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(step_s * 1000, 2), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (field: %s tensor cores; f64 reductions)" % args.field,
             "data": "synthetic (seeded generator standing in for ISPD 2015/2019)",
-            "config": config_dict(prob, args, world),
-            "result": {"stop": last["reason"], "iterations": iters, "start_iterations": last["start_iters"],
-                       "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "overflow_exact": overflow_exact,
-                       "ms_per_iteration":
-                       round(step_s * 1000 / max(iters, 1), 4), "wall_s_per_step": round(wall / args.steps, 4)},
+            "config": config_dict(prob, args, world, start_name), "result": result, "plain": plain,
             "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roof, "kernels": table, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": int(launches)}
@@ -403,35 +438,60 @@ def run_gb300(args):
         print(json.dumps(line))
 
 
+def _cpu_judges(prob, pos):
+    """Exact HPWL over every net and the movable cells' overflow with their real sizes (float64, the oracle)."""
+    import numpy as np
+    from oracle import gp_oracle as O
+    gr, C = prob.real_judge, prob.num_mov
+    pos = np.asarray(pos, np.float32)
+    hpwl = O.hpwl_all(pos, prob.all_cell, prob.all_off, prob.all_net_start, C)
+    size = np.ascontiguousarray(prob.nl.size, dtype=np.float32)
+    m = O.density_map_mt(pos[:C], size, np.ones(C, np.float32), C, gr.bx, gr.by, gr.nbx, gr.nby)
+    _, _, total = O.density_post(m, gr.fixed_map, gr.target, gr.nbx, gr.nby, mirrored=False)
+    return float(hpwl), float(total * gr.bin_area / gr.mov_area)
+
+
 def run_reference(args):
+    """The reference's CPU path (restated by the oracle: float32 operators, FFT of the mirrored map) on every host
+    core: W untimed gradient evaluations, then one whole placement of the same netlist and flow (two levels at the
+    reference's default cluster ratio) to its own stop, timed in full."""
     rank, world, _ = dist_setup()
     if rank != 0:
         return
+    import numpy as np
+    from oracle import gp_oracle as O
     prob, pos0 = workload(args.config, seed=0)
-    iters, source = None, None
-    try:
-        with open(ITER_FILE) as f:
-            rec = json.load(f)
-        if rec.get("config") == args.config:
-            iters, source = int(rec["iterations"]), "iterations of the GB300 run in profiles/bench_iterations.json"
-    except (OSError, ValueError, KeyError):
-        pass
-    if iters is None:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded iteration count for %s" % args.config}))
-        return
-    samples = []
-    for _ in range(max(args.steps, 1)):
-        per, threads = cpu_sample(prob, pos0, args.cpu_iters, iters)
-        samples.append(per)
-    per = statistics.median(samples)
-    value = per * iters
-    cpu = cpu_baseline_dict(per, threads, args.cpu_iters, iters, source)
-    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1000, 1),
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (CPU)",
-            "data": "synthetic (seeded generator standing in for ISPD 2015/2019)", "config": config_dict(prob, args, world),
-            "cpu_baseline": cpu, "e2e": {"value": round(value, 3), "unit": "s", "h2d_bytes_per_step": 0,
-                                         "d2h_bytes_per_step": 0}}
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    lvl = O.CpuLevel(prob, dtype=np.float32, field="fft", threads=threads)
+    gr = prob.force
+    v = np.clip(np.asarray(pos0, np.float64), gr.pos_lo, gr.pos_hi)
+    for _ in range(max(args.warmup, 0)):
+        lvl.grad(v, 1e-4, 10 * prob.base_gamma)
+    t0 = time.time()
+    if prob.opts.cluster_ratio > 1:
+        r = O.two_level(prob, pos0, dtype=np.float32, field="fft", threads=threads)
+        extra = {"clusters": r["clusters"], "cluster_iterations": r["coarse_iters"]}
+    else:
+        r = O.CpuLevel(prob, dtype=np.float32, field="fft", threads=threads).run(pos0)
+        extra = {}
+    total = time.time() - t0
+    hpwl, ovf = _cpu_judges(prob, r["pos"])
+    steps = max(args.steps, 1)
+    cpu = {"value": round(total, 3), "unit": "s", "cores": threads, "kind": "port",
+           "sample": "one whole placement to its own stop (%s, %d iterations), timed in full on %d host threads; "
+                     "the %d steps are consecutive shares of it" % (r["reason"], r["iters"], threads, steps)}
+    line = {"impl": "reference", "metric": METRIC, "value": round(total, 3), "unit": "s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": round(total * 1000 / steps, 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 operators, f64 control (CPU)",
+            "data": "synthetic (seeded generator standing in for ISPD 2015/2019)",
+            "config": config_dict(prob, args, world, "plain (wirelength-only)"),
+            "result": dict(stop=r["reason"], iterations=r["iters"], hpwl_exact=hpwl, overflow=r["overflow"],
+                           overflow_exact=ovf, **extra),
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(total, 3), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["config"]["field"] = "fft (float32, mirrored map)"
     print(json.dumps(line))
 
 

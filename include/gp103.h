@@ -192,6 +192,12 @@ typedef struct {
      * order gp103_net_order makes): their first pins follow from the net index, net_start is not read for them.
      * net_three = 0: not known, net_start is read for every net. */
     int net_two; int net_three;
+    /* subtracted from the density before the field's transforms (0: nothing). The field is the same either way: a
+     * constant changes only the zero-frequency coefficient, which the field drops. Set it to the grid's mean density
+     * (node area / bin area + the fixed map, over the bins: the charge is conserved while the nodes stay inside the
+     * region), so that the transforms' rounding follows the density's variation, not its mean -- on a spread
+     * placement, where the density is near its mean everywhere, the error against float64 falls by that ratio. */
+    float field_shift;
 } gp103_plan;
 
 typedef struct {
@@ -353,6 +359,63 @@ int gp103_hpwl(const float* pos, const int* pin_cell, const float* pin_off, cons
 int gp103_exact_overflow(const float* pos, const float* size, int num_mov, float bx, float by, int nbx, int nby,
                          const float* fixed, float target, double area_scale, unsigned long long* map,
                          void* scratch, double* out, cudaStream_t stream);
+
+/* ------------------------------------------------------------------------------------------------ part 3
+ * The learned start (no counterpart in the reference, whose clusters start at the seeded start positions,
+ * src/run_placement.py:98, and run the wirelength-only start, src/run_placement.py:48-65): a message-passing network
+ * over the cluster graph proposes the clusters' start positions. The graph is a netlist in the fused path's form:
+ * pins grouped by net (net_start [num_nets + 1], pin_cell [num_pins], a cell >= num_cells being a fixed pin at its
+ * pin_off) and by cell (cell_start [num_cells + 1], cell_pin [num_pins]). Deterministic: gathers in fixed order, no
+ * atomics. Dense layers take bf16 weights (row-major [in][out]) and accumulate in fp32; widths <= 64. */
+
+/* The weights of the graph's four gathers, each [num_pins]: net order (P2N and its transpose): net_pin_cell (the
+ * pin's cell, -1 for a fixed pin), w_p2n = 1 / the net's movable pins, w_n2ct = 1 / the pins of the pin's cell; cell
+ * order (N2C and its transpose): cell_pin_net (the pin's net), w_n2c = 1 / the cell's pins, w_p2nt = 1 / the movable
+ * pins of the pin's net. scratch: gp103_learn_graph_scratch(num_nets, num_pins) bytes. */
+size_t gp103_learn_graph_scratch(int num_nets, int num_pins);
+int gp103_learn_graph(const int* net_start, const int* pin_cell, const int* cell_start, const int* cell_pin,
+                      int num_nets, int num_cells, int num_pins, void* scratch, size_t scratch_bytes,
+                      int* net_pin_cell, float* w_p2n, float* w_n2ct, int* cell_pin_net, float* w_n2c, float* w_p2nt,
+                      cudaStream_t stream);
+
+/* out[s][0:width] (+)= sum over k in [seg_start[s], seg_start[s + 1]) of w[k] * src[idx[k]][0:width], in k order
+ * (idx[k] < 0: skipped; accumulate != 0: added to out). width 1 .. 64. */
+int gp103_seg_gather(const int* seg_start, int num_seg, const int* idx, const float* w, const float* src, int width,
+                     int accumulate, float* out, cudaStream_t stream);
+
+/* out[i][c] = act(bias[c] + sum_j x[i][j] wx[j][c] + sum_j a[i][j] wa[j][c]) for n rows, c < out_dim; act 0 = none,
+ * 1 = relu, 2 = sigmoid; in_a = 0: no second input. Weights bf16 (uint16 bit patterns), bias fp32. */
+int gp103_dense_fwd(const float* x, int n, int in_x, const float* a, int in_a, const uint16_t* wx, const uint16_t* wa,
+                    const float* bias, int out_dim, int act, float* out, cudaStream_t stream);
+
+/* The backward of gp103_dense_fwd given its output `out` and the gradient dout: dz = dout * act'(out) [n][out_dim];
+ * dx = dz wx^T, da = dz wa^T (either may be NULL); weight gradients gwx [in_x][out_dim], gwa, gbias (fp32, the rows'
+ * sum in a fixed order: per-block partials in `scratch`, gp103_dense_bwd_scratch bytes, added in block order). */
+size_t gp103_dense_bwd_scratch(int in_x, int in_a, int out_dim);
+int gp103_dense_bwd(const float* x, int n, int in_x, const float* a, int in_a, const uint16_t* wx, const uint16_t* wa,
+                    int out_dim, int act, const float* out, const float* dout, float* dz, float* dx, float* da,
+                    void* scratch, size_t scratch_bytes, float* gwx, float* gwa, float* gbias, cudaStream_t stream);
+
+/* Mean squared error: loss[0] = mean over the n rows of sum_d (y - t)^2 (float64, device), dy = 2 (y - t) / n.
+ * scratch: GP103_EVAL_SCRATCH_BYTES. */
+int gp103_mse(const float* y, const float* t, int n, int dim, float* dy, double* loss, void* scratch,
+              cudaStream_t stream);
+
+/* One Adam step (bias-corrected, decoupled weight decay) on fp32 parameters, also writing their bf16 copy. */
+int gp103_adam(float* param, const float* grad, float* m, float* v, uint16_t* param_bf16, int n, float lr, float beta1,
+               float beta2, float eps, int step, float weight_decay, cudaStream_t stream);
+
+/* The 8 input features of every cell of the graph [num_cells][8]: log(area / mean_area), log(1 + nets) / 4,
+ * log(1 + pin_count) / 4 (pin_count NULL: the cell's pins), the anchor (x / width, y / height: at hop 0 the mean of
+ * the fixed pins on the cell's nets, then, hop by hop up to max_hop, the mean over each net's anchored cells averaged
+ * over the cell's nets; the centre when none), hop / max_hop (1 when none), 1 if anchored, the anchor's distance from
+ * the centre. The gather weights come from gp103_learn_graph. scratch: gp103_learn_features_scratch bytes. */
+size_t gp103_learn_features_scratch(int num_nets, int num_cells);
+int gp103_learn_features(const int* net_start, const int* pin_cell, const float* pin_off, const int* cell_start,
+                         int num_nets, int num_cells, int num_pins, const int* net_pin_cell, const float* w_p2n,
+                         const int* cell_pin_net, const float* w_n2c, const float* area, const float* pin_count,
+                         double mean_area, float width, float height, int max_hop, void* scratch, size_t scratch_bytes,
+                         float* feat, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,8 @@ Each function names the reference lines it restates (paths inside the AutoPlace 
   control         gp_cuda_kernel.cu:183-240 with src/param_scheduler.py:63-116, src/resolution.py:33-56 (float64)
   select          gp_cuda_kernel.cu:243-249
   place_level     src/run_placement.py:41-76 + src/gpu_loop.py:35-81 (host loop; the CPU baseline)
+  *_mt            multi-threaded forms (oracle/level_ref.c, OpenMP) of WA (float32), the map and the gather, for
+                  CpuLevel(threads=...): a whole level of a large netlist on the host cores in minutes
   cluster_*       src/cluster.py:38-85 (star matching: pair edges, rounds), integer sums: exact
   coarse_pins     src/cluster.py:101-115 (the pins of the cluster problem)
   expand          src/cluster.py:133-144
@@ -45,8 +47,8 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(_HERE, "_build", "liboracle.so")
-        src = os.path.join(_HERE, "density_ref.c")
-        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        srcs = [os.path.join(_HERE, f) for f in ("density_ref.c", "level_ref.c", "Makefile")]
+        if not os.path.exists(path) or os.path.getmtime(path) < max(os.path.getmtime(f) for f in srcs):
             subprocess.check_call(["make", "-s", "-C", _HERE])
         L = ctypes.CDLL(path)
         i, f, d = ctypes.c_int, ctypes.c_float, ctypes.c_double
@@ -57,6 +59,15 @@ def lib():
         L.oracle_density_grad.argtypes = [_f32p, _f32p, _f32p, _f64p, _f64p, i, ctypes.c_void_p, i, _f32p, _f32p, i,
                                           d, d, f, f, i, i, _f64p]
         L.oracle_density_grad.restype = None
+        L.oracle_threads.argtypes = [i]
+        L.oracle_threads.restype = i
+        _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        L.oracle_wa_mt.argtypes = [_f32p, _i32p, _f32p, _i32p, i, i, f, _i32p, _i32p, _f32p, _f32p, _f32p, _f64p]
+        L.oracle_wa_mt.restype = None
+        L.oracle_density_map_mt.argtypes = L.oracle_density_map.argtypes
+        L.oracle_density_map_mt.restype = None
+        L.oracle_density_grad_mt.argtypes = L.oracle_density_grad.argtypes
+        L.oracle_density_grad_mt.restype = None
         _LIB = L
     return _LIB
 
@@ -93,6 +104,45 @@ def wa_forward(pos, cell32, off, net_start, num_mov, gamma, dtype=np.float64):
     grad = np.stack([np.bincount(cell32, weights=gp[:, a], minlength=num_mov + 1)[:num_mov] for a in range(2)], 1)
     out = np.stack([(xp - xn).sum(1), (hi - lo).sum(1)], 1)
     return float(out[:, 0].sum()), grad.astype(dtype), float(out[:, 1].sum()), out, gp
+
+
+def set_threads(n):
+    """Threads of the multi-threaded oracle operators (0: leave as is) -> the count in force."""
+    return int(lib().oracle_threads(int(n)))
+
+
+def wa_forward_mt(pos, cell32, off, net_start, cell_start, cell_pin, num_mov, gamma):
+    """wa_forward(dtype=float32) on the host threads (oracle/level_ref.c): the same arithmetic, each cell's pins summed
+    in pin order. -> (WA total, grad [num_mov, 2] float32, HPWL total, out [nets, 2] float32, pin gradient [P, 2])."""
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    num_nets, P = len(net_start) - 1, len(cell32)
+    pin_grad = np.empty((max(P, 1), 2), np.float32)
+    grad = np.empty((max(num_mov, 1), 2), np.float32)
+    out = np.empty((max(num_nets, 1), 2), np.float32)
+    tot = np.zeros(2)
+    lib().oracle_wa_mt(_c32(pos), i32(cell32), _c32(off), i32(net_start), num_nets, num_mov, float(gamma),
+                       i32(cell_start), i32(cell_pin), pin_grad, grad, out, tot)
+    return float(tot[0]), grad[:num_mov], float(tot[1]), out[:num_nets], pin_grad[:P]
+
+
+def density_map_mt(pos, size, ratio, num_mov, bx, by, nbx, nby):
+    """density_map on the host threads: the same integer map."""
+    m = np.zeros((2, nbx, nby), dtype=np.uint64)
+    lib().oracle_density_map_mt(_c32(pos), _c32(size), _c32(ratio), len(pos), num_mov, bx, by, nbx, nby, m)
+    return m
+
+
+def density_grad_mt(pos, size, ratio, fx, fy, wl_grad, pins, area, weight, precond, bx, by, nbx, nby):
+    """density_grad on the host threads: the same values."""
+    fx = np.ascontiguousarray(fx, np.float64)
+    fy = np.ascontiguousarray(fy, np.float64)
+    n = len(pos)
+    wl = _c32(wl_grad) if wl_grad is not None and len(wl_grad) else None
+    g = np.empty((n, 2), np.float64)
+    lib().oracle_density_grad_mt(_c32(pos), _c32(size), _c32(ratio), fx, fy, fx.shape[1],
+                                 wl.ctypes.data if wl is not None else None, 0 if wl is None else len(wl),
+                                 _c32(pins), _c32(area), n, float(weight), float(precond), bx, by, nbx, nby, g)
+    return g
 
 
 def hpwl_all(pos, pin_cell, pin_off, net_start, num_mov):
@@ -143,12 +193,24 @@ def spectral_operator(nbx, nby, bin_np, dtype=np.float64):
     return np.stack([-1j * kx * inv, -1j * ky * inv])
 
 
-def field_fft(rho_mirrored, nbx, nby, bin_np, dtype=np.float64):
+_OPS = {}
+
+
+def field_fft(rho_mirrored, nbx, nby, bin_np, dtype=np.float64, workers=None):
     """Field of the mirrored map -> [2, 2 nbx, 2 nby] (x plane, y plane); float64, or float32 / complex64 as the
-    reference's CPU path computes it."""
-    op = spectral_operator(nbx, nby, bin_np)
-    if dtype == np.float32:
-        op = op.astype(np.complex64)
+    reference's CPU path computes it. workers: transforms on that many host threads (scipy.fft), else numpy's."""
+    key = (nbx, nby, float(bin_np[0]), float(bin_np[1]), np.dtype(dtype).name)
+    op = _OPS.get(key)
+    if op is None:
+        op = spectral_operator(nbx, nby, bin_np)
+        if dtype == np.float32:
+            op = op.astype(np.complex64)
+        _OPS.clear()
+        _OPS[key] = op
+    if workers:
+        import scipy.fft as sf
+        spec = sf.rfft2(np.asarray(rho_mirrored, dtype), workers=workers)
+        return sf.irfft2(spec[None] * op, s=(2 * nbx, 2 * nby), workers=workers)
     spec = np.fft.rfft2(np.asarray(rho_mirrored, dtype))
     return np.fft.irfft2(spec[None] * op, s=(2 * nbx, 2 * nby))
 
@@ -444,32 +506,42 @@ class CpuLevel(object):
     the control rules above. `dtype` is the float type of the wirelength and field arithmetic; `field` = "dct"
     (cosine / sine transforms of the plain map) or "fft" (FFT of the mirrored map, as the reference)."""
 
-    def __init__(self, prob, dtype=np.float64, field="dct"):
+    def __init__(self, prob, dtype=np.float64, field="dct", threads=None):
+        """threads: run on that many host threads (the *_mt operators: WA in float32, the same map, the same gather;
+        transforms by scipy.fft), as the reference's CPU path runs on every core."""
         self.p, self.dtype, self.field = prob, dtype, field
+        self.threads = int(threads) if threads else 0
+        if self.threads:
+            set_threads(self.threads)
         self.evals = 0
 
     def wirelength(self, pos, gamma):
         cs = self.p.csr
+        if self.threads:
+            wa, grad, hpwl, _, _ = wa_forward_mt(pos, cs.cell32, cs.off, cs.net_start, cs.cell_start, cs.cell_pin,
+                                                 self.p.num_mov, gamma)
+            return wa, grad.astype(np.float64), hpwl
         wa, grad, hpwl, _, _ = wa_forward(pos, cs.cell32, cs.off, cs.net_start, self.p.num_mov, gamma, self.dtype)
         return wa, grad, hpwl
 
     def density(self, pos, wl_grad, weight, precond):
         """-> (gradient [n, 2], overflow on the overflow grid)."""
         p, gr = self.p, self.p.force
-        m = density_map(pos, gr.size, gr.ratio, p.num_mov, gr.bx, gr.by, gr.nbx, gr.nby)
+        dmap, dgrad = (density_map_mt, density_grad_mt) if self.threads else (density_map, density_grad)
+        m = dmap(pos, gr.size, gr.ratio, p.num_mov, gr.bx, gr.by, gr.nbx, gr.nby)
         rho, _, ovsum = density_post(m, gr.fixed_map, gr.target, gr.nbx, gr.nby, mirrored=self.field == "fft")
         overflow = ovsum * gr.bin_area / gr.mov_area
         if p.judge is not None:
             j = p.judge
-            mj = density_map(pos[:p.num_mov], j.size, j.ratio, p.num_mov, j.bx, j.by, j.nbx, j.nby)
+            mj = dmap(pos[:p.num_mov], j.size, j.ratio, p.num_mov, j.bx, j.by, j.nbx, j.nby)
             _, _, js = density_post(mj, j.fixed_map, j.target, j.nbx, j.nby, mirrored=False)
             overflow = js * j.bin_area / j.mov_area
         if self.field == "fft":
-            ex, ey = field_fft(rho, gr.nbx, gr.nby, gr.bin_np, self.dtype)
+            ex, ey = field_fft(rho, gr.nbx, gr.nby, gr.bin_np, self.dtype, workers=self.threads or None)
         else:
             ex, ey = field_dct(plain_density(m, gr.fixed_map), gr.bin_np)
-        g = density_grad(pos, gr.size, gr.ratio, ex, ey, wl_grad, p.pins, p.area, weight, precond, gr.bx, gr.by,
-                         gr.nbx, gr.nby)
+        g = dgrad(pos, gr.size, gr.ratio, ex, ey, wl_grad, p.pins, p.area, weight, precond, gr.bx, gr.by,
+                  gr.nbx, gr.nby)
         return g, overflow
 
     def grad(self, pos, lam, gam):
@@ -579,7 +651,7 @@ class CpuLevel(object):
                     lam=float(S[K["lam"]]) if S is not None else 0.0, gam=float(S[K["gam"]]) if S is not None else gam)
 
 
-def two_level(prob, pos0, dtype=np.float64, field="dct"):
+def two_level(prob, pos0, dtype=np.float64, field="dct", threads=None):
     """global_placement_main's two-level branch (src/run_placement.py:87-110) on the CPU: the clusters (cluster_cells
     with the reference's seeded torch draws), their problem (coarse_pins; sizes as squares of the summed area, a
     one-cell cluster keeping its shape; the grid between the overflow grid and the cells' force grid), one level of
@@ -609,13 +681,13 @@ def two_level(prob, pos0, dtype=np.float64, field="dct"):
     copts.settle_iter, copts.min_iter = 0, 0
     cprob = P.Problem.clusters(prob, csize, c_cell, c_off, c_net, nb, ff, copts)
     pos0 = np.asarray(pos0, np.float32)
-    coarse = CpuLevel(cprob, dtype, field)
+    coarse = CpuLevel(cprob, dtype, field, threads)
     level = coarse.run(np.concatenate([pos0[:num], pos0[n:]]), handover_gamma=10 * prob.base_gamma)
     cpos = np.asarray(level["pos"], np.float32)
     gen = torch.Generator().manual_seed(int(o.seed))
     pos = expand(cpos, cid, csize, size, torch.rand(n, 2, generator=gen).numpy(), num)
     pos = np.clip(pos, prob.force.pos_lo, prob.force.pos_hi)
-    fine = CpuLevel(prob, dtype, field)
+    fine = CpuLevel(prob, dtype, field, threads)
     weight = level["lam"] * fine.tension_unit(pos.astype(np.float64)) / coarse.tension_unit(cpos.astype(np.float64))
     if o.wa_rule == "accuracy":
         gam = level["gam"] / cprob.base_gamma * prob.base_gamma

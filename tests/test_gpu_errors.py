@@ -69,7 +69,9 @@ def test_field_timeout_is_reported_and_cleared(nb):
     s = torch.cuda.current_stream().cuda_stream
     pl, keep = _plan(nb, native.FIELD_F16X3)
     rng = np.random.default_rng(3)
-    a = (rng.random((nb, nb)) * 0.5 + 0.5).astype(np.float32)
+    a = rng.random((nb, nb)) * 0.3 + 0.6
+    a[nb // 3: nb // 3 + 5, nb // 2: nb // 2 + 7] += 40.0                   # a clump
+    a = a.astype(np.float32)
     d = torch.as_tensor(a).to(DEV)
     ex, ey = torch.full((nb, nb), 7.0, device=DEV), torch.full((nb, nb), 7.0, device=DEV)
     assert native.device_error(ctypes.byref(pl), s) == 0

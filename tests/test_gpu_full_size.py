@@ -169,8 +169,10 @@ def c2_states(c2):
 def test_full_size_field_error_on_real_states(c2, c2_states, state, mode, tol):
     """The tensor-core field of the 1024 x 1024 force grid against float64 (the cosine-transform statement of the
     reference's mirrored FFT) on the densities of a real run: max |E - E64| / max |E64| <= 1e-6. The density plane
-    is the run's own (the float32 total density of the fixed-point map)."""
+    is the run's own (the float32 total density of the fixed-point map), with the Placer's shift (the grid's mean
+    density, taken off before the transforms: the same field, rounding relative to the density's variation)."""
     import ctypes
+    from autoplace_gb300.engine import mean_density
     from tests.test_gpu_ops import _field_plan
     nl, prob, _ = c2
     gr = prob.force
@@ -178,6 +180,7 @@ def test_full_size_field_error_on_real_states(c2, c2_states, state, mode, tol):
     _, rho, _ = _native_map(pos, gr.size, gr.ratio, prob.num_mov, gr)
     a = np.ascontiguousarray(rho[:gr.nbx, :gr.nby])
     pl, keep = _field_plan(gr.nbx, mode, bx=gr.bx, by=gr.by)
+    pl.field_shift = mean_density(prob)            # as the Placer sets it: the grid's mean density
     ex, ey = torch.zeros((gr.nbx, gr.nby), device=DEV), torch.zeros((gr.nbx, gr.nby), device=DEV)
     d = cu(a)
     native.call("gp103_field", ctypes.byref(pl), d.data_ptr(), ex.data_ptr(), ey.data_ptr(),
