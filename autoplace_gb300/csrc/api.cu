@@ -113,7 +113,7 @@ extern "C" int gp103_wa(const float* pos, const int* pin_cell, const float* pin_
         j.num_nets = num_nets;
         j.num_mov = num_mov;
         j.split = num_nets;
-        j.mid = num_nets;
+        j.mid = j.g8 = j.g16 = num_nets;
         j.gamma = gamma;
         j.pin_grad = (float2*)pin_grad;
         j.out = (float2*)out;
@@ -198,7 +198,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
         OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
         OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid), OFF(net_two), OFF(net_three),
-        OFF(field_shift)};
+        OFF(field_shift), OFF(net_g8), OFF(net_g16)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -226,6 +226,8 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
     REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
     REQUIRE(p->net_mid == 0 || (p->net_mid >= p->net_split && p->net_mid <= p->num_nets));
+    REQUIRE(p->net_g16 == 0 || (p->net_mid > 0 && p->net_g8 >= p->net_mid && p->net_g16 >= p->net_g8 &&
+                                p->net_g16 <= p->num_nets));
     REQUIRE(p->net_three == 0 || (p->net_two >= 0 && p->net_two <= p->net_three && p->net_three <= p->net_split &&
                                   2LL * p->net_two + 3LL * (p->net_three - p->net_two) <= (long long)p->num_pins));
     REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
@@ -395,6 +397,8 @@ static WaJob wa_job(const gp103_plan* p) {
     w.num_mov = p->num_mov;
     w.split = p->net_split;
     w.mid = p->net_mid > 0 ? p->net_mid : p->net_split;
+    w.g8 = p->net_g16 > 0 ? p->net_g8 : w.mid;
+    w.g16 = p->net_g16 > 0 ? p->net_g16 : w.mid;
     w.two = p->net_three > 0 ? p->net_two : 0;
     w.three = p->net_three;
     w.slot = p->pin_slot;

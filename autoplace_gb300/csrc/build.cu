@@ -13,12 +13,15 @@
 namespace gp103 {
 
 constexpr int NO_SHORT = 8;               // nets of up to 8 pins are short (one thread each in the WA kernels)
-constexpr int NO_MID = 16;                // nets of 9 .. 16 pins: 4 lanes each; longer: a warp each
-constexpr int NO_CLASSES = 5;
+constexpr int NO_MID = 16;                // nets of 9 .. 16 pins: 4 lanes each
+constexpr int NO_G8 = 32;                 // 17 .. 32 pins: 8 lanes each
+constexpr int NO_G16 = 64;                // 33 .. 64 pins: 16 lanes each; longer: a warp each
+constexpr int NO_CLASSES = 7;
 // SCAN_TILE, SCAN_MAX_TILES: kernels.cuh
 
 __device__ __forceinline__ int net_class(int deg) {
-    return deg == 2 ? 0 : deg == 3 ? 1 : deg <= NO_SHORT ? 2 : deg <= NO_MID ? 3 : 4;
+    return deg == 2 ? 0 : deg == 3 ? 1 : deg <= NO_SHORT ? 2 : deg <= NO_MID ? 3 : deg <= NO_G8 ? 4 :
+           deg <= NO_G16 ? 5 : 6;
 }
 
 // key of a net = class * (num_mov + 1) + lowest cell (a cell index in [0, num_mov]); count per key
@@ -192,11 +195,12 @@ __global__ void __launch_bounds__(256) pin_slot_kernel(const int* cell_pin, cons
 }
 
 // split[0] = nets of up to 8 pins = start of the keys of class 3, split[1] = nets of up to 16 pins (class 4),
-// split[2] = nets of 2 pins (class 0), split[3] = nets of up to 3 pins (class 1)
+// split[2] = nets of 2 pins (class 0), split[3] = nets of up to 3 pins (class 1), split[4] = nets of up to 32 pins
+// (class 5), split[5] = nets of up to 64 pins (class 6)
 __global__ void net_split_kernel(const int* start, int stride, int num_nets, int keys, int* split) {
     pdl_wait();
-    const int cls[4] = {3, 4, 1, 2};
-    for (int c = 0; c < 4; c++) {
+    const int cls[6] = {3, 4, 1, 2, 5, 6};
+    for (int c = 0; c < 6; c++) {
         const int k = cls[c] * stride;
         split[c] = k < keys ? start[k] : num_nets;
     }

@@ -42,6 +42,8 @@ struct WaJob {
     int num_nets, num_mov;
     int split;              // nets [split, num_nets): one warp each; below: 32 per warp (num_nets: any order)
     int mid;                // nets [split, mid): 9 .. 16 pins, 4 lanes each (mid = split: none)
+    int g8, g16;            // nets [mid, g8): 17 .. 32 pins, 8 lanes each; [g8, g16): 33 .. 64 pins, 16 lanes each
+                            // (g8 = g16 = mid: none; the rest a warp each)
     int two, three;         // nets [0, two): 2 pins, [two, three): 3 pins, pins from 0 in net order (three = 0: none)
     const int* slot;        // pin p's gradient goes to pin_grad[slot[p]] (null: pin_grad[p])
     const float* gamma;

@@ -293,37 +293,52 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
     }
 }
 
-// Long nets [split, num_nets): nets [split, mid) (9 .. 16 pins) by groups of 4 lanes, eight per warp item; nets
-// [mid, num_nets) one per warp.
-constexpr int WA_GROUP = 4;
+// Long nets [split, num_nets), by degree class: [split, mid) (9 .. 16 pins) by groups of 4 lanes, eight nets per
+// warp item; [mid, g8) (17 .. 32) by 8 lanes, four per item; [g8, g16) (33 .. 64) by 16 lanes, two per item; the
+// rest one per warp. Every lane of a group holds at most WA_WREG pins.
+template <int L>
+__device__ __forceinline__ void group_item(const WaJob& j, const float2* pos, float ig, int first, int end, int item,
+                                           int lane, float& wa_sum, float& hp_sum) {
+    const int gl = lane & (L - 1), i = first + item * (32 / L) + lane / L;
+    const bool valid = i < end;
+    int s = 0, d = 0;
+    if (valid) {
+        s = j.net_start[i];
+        d = j.net_start[i + 1] - s;
+    }
+    float wa, hp;
+    net_group<L>(j, pos, ig, s, d, gl, wa, hp);
+    if (valid && gl == 0) {
+        if (j.out) j.out[i] = make_float2(wa, hp);
+        wa_sum += wa;
+        hp_sum += hp;
+    }
+}
+
+__host__ __device__ inline int group_items(int first, int end, int lanes) {
+    return (end - first + 32 / lanes - 1) / (32 / lanes);
+}
 
 __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
     pdl_wait();
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
-    const int lane = threadIdx.x & 31, gl = lane & (WA_GROUP - 1), gi = lane / WA_GROUP;
+    const int lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * (blockDim.x >> 5);
-    const int groups = (j.mid - j.split + 32 / WA_GROUP - 1) / (32 / WA_GROUP);
-    const int items = groups + (j.num_nets - j.mid);
+    const int n4 = group_items(j.split, j.mid, 4), n8 = group_items(j.mid, j.g8, 8);
+    const int n16 = group_items(j.g8, j.g16, 16);
+    const int groups = n4 + n8 + n16;
+    const int items = groups + (j.num_nets - j.g16);
     float wa_sum = 0.f, hp_sum = 0.f;
     for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
-        if (it < groups) {                                   // uniform over the warp
-            const int i = j.split + it * (32 / WA_GROUP) + gi;
-            const bool valid = i < j.mid;
-            int s = 0, d = 0;
-            if (valid) {
-                s = j.net_start[i];
-                d = j.net_start[i + 1] - s;
-            }
-            float wa, hp;
-            net_group<WA_GROUP>(j, pos, ig, s, d, gl, wa, hp);
-            if (valid && gl == 0) {
-                if (j.out) j.out[i] = make_float2(wa, hp);
-                wa_sum += wa;
-                hp_sum += hp;
-            }
+        if (it < n4) {                                       // (every branch is uniform over the warp)
+            group_item<4>(j, pos, ig, j.split, j.mid, it, lane, wa_sum, hp_sum);
+        } else if (it < n4 + n8) {
+            group_item<8>(j, pos, ig, j.mid, j.g8, it - n4, lane, wa_sum, hp_sum);
+        } else if (it < groups) {
+            group_item<16>(j, pos, ig, j.g8, j.g16, it - n4 - n8, lane, wa_sum, hp_sum);
         } else {
-            const int i = j.mid + (it - groups);
+            const int i = j.g16 + (it - groups);
             const int s = j.net_start[i], d = j.net_start[i + 1] - s;
             float wa, hp;
             net_warp(j, pos, ig, s, d, lane, wa, hp);
@@ -342,7 +357,8 @@ __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ Wa
 
 int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const long long chunks = (j.split + 31) / 32;
-    const long long longs = (j.mid - j.split + 32 / WA_GROUP - 1) / (32 / WA_GROUP) + (j.num_nets - j.mid);   // warp items
+    const long long longs = (long long)group_items(j.split, j.mid, 4) + group_items(j.mid, j.g8, 8) +
+                            group_items(j.g8, j.g16, 16) + (j.num_nets - j.g16);          // warp items
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
     static const int res_short = resident_blocks(wa_short_kernel<false>, 256);
     static const int res_long = resident_blocks(wa_long_kernel, 256);

@@ -32,22 +32,26 @@ START_EVERY = 4        # passes per poll of the wirelength-only start
 _GRAPH_LAUNCHES = {"captured": 0, "replayed": 0}        # libgp103 launches inside CUDA graphs, all Placers
 SHORT_NET = 8          # nets of up to this many pins are done one per thread (WA_REG of the kernel)
 MID_NET = 16           # nets of up to this many pins (and more than SHORT_NET) are done by 4 lanes each
+G8_NET = 32            # ... by 8 lanes each (nets of MID_NET + 1 .. G8_NET pins)
+G16_NET = 64           # ... by 16 lanes each (G8_NET + 1 .. G16_NET pins); longer nets by a warp each
 
 
 def net_order(net_start, cell32, cell_pin):
     """The device order of the optimised nets: short nets (<= SHORT_NET pins) first, in classes of 2, 3 and 4..8
     pins so that a warp's lanes do equal work, each class ordered by the net's lowest cell (nearby nets gather
-    nearby cells); the long nets after them (one warp each). Pins move with their nets.
+    nearby cells); the long nets after them in classes of 9..16, 17..32, 33..64 pins (groups of 4, 8, 16 lanes) and
+    longer (a warp each). Pins move with their nets.
     -> (pin permutation: new position -> old pin, new net_start, slot: new pin position -> its position in cell
-    order (cell_pin order, which every cell sums in), index of the first net of more than SHORT_NET pins, index of
-    the first net of more than MID_NET pins, number of 2-pin nets, number of nets of up to 3 pins)."""
+    order (cell_pin order, which every cell sums in), then the class boundaries as gp103_net_order's split: the
+    numbers of nets of up to SHORT_NET, MID_NET, 2, 3, G8_NET and G16_NET pins)."""
     ns = np.asarray(net_start, np.int64)
     deg = np.diff(ns)
     n = len(deg)
     if n == 0:
-        return np.zeros(0, np.int64), np.zeros(1, np.int32), np.zeros(0, np.int32), 0, 0, 0, 0
+        return np.zeros(0, np.int64), np.zeros(1, np.int32), np.zeros(0, np.int32), 0, 0, 0, 0, 0, 0
     first = np.minimum.reduceat(np.asarray(cell32, np.int64), ns[:-1]) if len(cell32) else np.zeros(n, np.int64)
-    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, np.where(deg <= MID_NET, 3, 4))))
+    cls = np.select([deg == 2, deg == 3, deg <= SHORT_NET, deg <= MID_NET, deg <= G8_NET, deg <= G16_NET],
+                    [0, 1, 2, 3, 4, 5], 6)
     order = np.lexsort((first, cls))
     lens = deg[order]
     new_start = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
@@ -57,7 +61,7 @@ def net_order(net_start, cell32, cell_pin):
     slot = np.empty(len(perm), np.int64)
     slot[newpos[np.asarray(cell_pin, np.int64)]] = np.arange(len(perm))
     return (perm, new_start.astype(np.int32), slot.astype(np.int32), int((cls < 3).sum()), int((cls < 4).sum()),
-            int((cls < 1).sum()), int((cls < 2).sum()))
+            int((cls < 1).sum()), int((cls < 2).sum()), int((cls < 5).sum()), int((cls < 6).sum()))
 
 
 def launches():
@@ -164,7 +168,7 @@ class Placer(object):
         self.cell_start = self._hold(up("cell_start", cs.cell_start, torch.int32))
         self.pin_cell, self.pin_off = z((max(P, 1),), torch.int32), z((max(P, 1), 2), torch.float32)
         self.net_start, self.pin_slot = z((N + 1,), torch.int32), z((max(P, 1),), torch.int32)
-        split = torch.zeros(4, dtype=torch.int32, device=dev)
+        split = torch.zeros(6, dtype=torch.int32, device=dev)
         scratch = torch.empty(int(native.lib().gp103_net_order_scratch(N, P, prob.num_mov)), dtype=torch.uint8,
                               device=dev)
         native.call("gp103_net_order", self._p(ns_in), self._p(cell_in), self._p(off_in), self._p(cp_in), N, P,
@@ -232,7 +236,8 @@ class Placer(object):
             setattr(pl, k, self._p(getattr(self, k)))
         native.call("gp103_field_constants", ctypes.byref(pl), self.stream.cuda_stream)
         # the one host synchronisation of the set-up: the net classes of the WA order (launch sizes of the passes)
-        pl.net_split, pl.net_mid, pl.net_two, pl.net_three = (int(x) for x in split.cpu().tolist())
+        (pl.net_split, pl.net_mid, pl.net_two, pl.net_three, pl.net_g8,
+         pl.net_g16) = (int(x) for x in split.cpu().tolist())
         self.plan = pl
         self._ref = ctypes.byref(pl)
 

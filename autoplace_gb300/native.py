@@ -42,6 +42,7 @@ class Plan(ctypes.Structure):
         ("order", _vp), ("order_counts", _vp), ("order_cursor", _vp),
         ("net_mid", _i), ("net_two", _i), ("net_three", _i),
         ("field_shift", _f),
+        ("net_g8", _i), ("net_g16", _i),
     ]
 
 

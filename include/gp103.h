@@ -198,6 +198,9 @@ typedef struct {
      * region), so that the transforms' rounding follows the density's variation, not its mean -- on a spread
      * placement, where the density is near its mean everywhere, the error against float64 falls by that ratio. */
     float field_shift;
+    /* nets [net_mid, net_g8) have 17 to 32 pins (eight lanes each, four nets per warp), [net_g8, net_g16) 33 to 64
+     * (sixteen lanes each, two per warp), the rest a warp each (net_g16 = 0: every net from net_mid on a warp) */
+    int net_g8; int net_g16;
 } gp103_plan;
 
 typedef struct {
@@ -261,12 +264,13 @@ int gp103_device_error(const gp103_plan* plan, int clear, int* code, cudaStream_
 /* Set-up of the fused path on the device: the nets of the optimised pin set (Wirelength._pin_set,
  * src/core/wa_wirelength_hpwl.py:38-46; net_start [num_nets + 1], pin_cell [num_pins] with num_mov for a fixed pin,
  * pin_off [num_pins, 2], cell_pin [num_pins] = the pins in cell order) reordered for the WA kernels: a stable sort
- * of the nets by (class, lowest cell), classes 2 pins / 3 pins / 4-8 pins / 9-16 pins / longer, pins moving with
- * their nets.
+ * of the nets by (class, lowest cell), classes 2 pins / 3 pins / 4-8 / 9-16 / 17-32 / 33-64 pins / longer, pins
+ * moving with their nets.
  * Writes net_start_out, pin_cell_out, pin_off_out (the plan's net_start, pin_cell, pin_off), pin_slot (each new
- * pin's position in cell order: the plan's pin_slot) and split (device int [4]: the plan's net_split, net_mid,
- * net_two and net_three = numbers of nets of up to 8, up to 16, 2 and up to 3 pins). scratch: gp103_net_order_scratch(...) bytes. No counterpart in the reference, whose kernel
- * reads the nets in their original order. GP103_ERR_TOO_LARGE beyond 5 (num_mov + 1) > 16,777,216. */
+ * pin's position in cell order: the plan's pin_slot) and split (device int [6]: the plan's net_split, net_mid,
+ * net_two, net_three, net_g8 and net_g16 = numbers of nets of up to 8, up to 16, 2, up to 3, up to 32 and up to 64
+ * pins). scratch: gp103_net_order_scratch(...) bytes. No counterpart in the reference, whose kernel reads the nets
+ * in their original order. GP103_ERR_TOO_LARGE beyond 7 (num_mov + 1) > 16,777,216. */
 size_t gp103_net_order_scratch(int num_nets, int num_pins, int num_mov);
 int gp103_net_order(const int* net_start, const int* pin_cell, const float* pin_off, const int* cell_pin,
                     int num_nets, int num_pins, int num_mov, void* scratch, size_t scratch_bytes,

@@ -61,13 +61,13 @@ def test_full_size_device_build_and_net_order_match_host(c2):
     nl, prob, _ = c2
     _check_device_problem(nl, prob.opts)
     cs = prob.csr
-    perm, new_start, slot, split, mid, two, three = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    perm, new_start, slot, *bounds = net_order(cs.net_start, cs.cell32, cs.cell_pin)
     ns_d, cell_d, off_d, slot_d, split_d = device_order(cs, nl.num_mov)
     assert np.array_equal(ns_d, new_start)
     assert np.array_equal(cell_d, cs.cell32[perm])
     assert np.array_equal(off_d.view(np.uint32), cs.off[perm].view(np.uint32))
     assert np.array_equal(slot_d, slot)
-    assert split_d == [split, mid, two, three]
+    assert split_d == list(bounds)
 
 
 # ------------------------------------------------------------------------------------------------ float work

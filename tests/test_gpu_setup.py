@@ -22,7 +22,7 @@ def device_order(cs, num_mov):
     cell_out = torch.zeros(max(P, 1), dtype=torch.int32, device=DEV)
     off_out = torch.zeros((max(P, 1), 2), dtype=torch.float32, device=DEV)
     slot = torch.zeros(max(P, 1), dtype=torch.int32, device=DEV)
-    split = torch.zeros(4, dtype=torch.int32, device=DEV)
+    split = torch.zeros(6, dtype=torch.int32, device=DEV)
     nbytes = int(native.lib().gp103_net_order_scratch(N, P, num_mov))
     scratch = torch.empty(nbytes, dtype=torch.uint8, device=DEV)
     ins = [cu(cs.net_start), cu(cs.cell32), cu(cs.off), cu(cs.cell_pin)]
@@ -38,13 +38,14 @@ def device_order(cs, num_mov):
 def test_device_net_order_matches_host(cells, seed):
     nl = synth.make_netlist(cells, int(cells * 1.05), window=200, macros=2, cover=0.1, seed=seed)
     cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
-    perm, new_start, slot, split, mid, two, three = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    perm, new_start, slot, *bounds = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    split, mid, two, three, g8, g16 = bounds
     ns_d, cell_d, off_d, slot_d, split_d = device_order(cs, nl.num_mov)
     assert np.array_equal(ns_d, new_start)
     assert np.array_equal(cell_d, cs.cell32[perm])
     assert np.array_equal(off_d.view(np.uint32), cs.off[perm].view(np.uint32))
     assert np.array_equal(slot_d, slot)
-    assert split_d == [split, mid, two, three]
+    assert split_d == list(bounds)
     deg = np.diff(new_start)
     assert (deg[:two] == 2).all() and (deg[two:three] == 3).all() and (deg[three:] > 3).all()
 
@@ -52,7 +53,7 @@ def test_device_net_order_matches_host(cells, seed):
 def test_device_net_order_empty():
     cs = problem.build_csr(np.zeros(0, np.int64), np.zeros((0, 2), np.float32), np.zeros(0, np.int64), 0, 10, 100)
     ns_d, _, _, _, split_d = device_order(cs, 10)
-    assert ns_d.tolist() == [0] and split_d == [0, 0, 0, 0]
+    assert ns_d.tolist() == [0] and split_d == [0] * 6
 
 
 def _same(a, b):

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from autoplace_gb300 import native, problem, synth
-from autoplace_gb300.engine import MID_NET, SHORT_NET, net_order
+from autoplace_gb300.engine import G8_NET, G16_NET, MID_NET, SHORT_NET, net_order
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -64,13 +64,16 @@ def test_argument_errors_without_gpu():
 def test_net_order_keeps_nets_and_cell_sums():
     nl = synth.make_netlist(3000, 3100, window=60, macros=3, cover=0.1, fixed_pin_share=0.05, seed=4)
     cs = problem.build_csr(nl.pin_cell, nl.pin_off, nl.pin_net, nl.num_nets, nl.num_mov, 100)
-    perm, ns, slot, split, mid, two, three = net_order(cs.net_start, cs.cell32, cs.cell_pin)
+    perm, ns, slot, split, mid, two, three, g8, g16 = net_order(cs.net_start, cs.cell32, cs.cell_pin)
     deg = np.diff(ns)
     assert np.all(deg[:split] <= SHORT_NET) and np.all(deg[split:] > SHORT_NET)
     assert np.all(deg[split:mid] <= MID_NET) and np.all(deg[mid:] > MID_NET)
+    assert np.all(deg[mid:g8] <= G8_NET) and np.all(deg[g8:] > G8_NET)
+    assert np.all(deg[g8:g16] <= G16_NET) and np.all(deg[g16:] > G16_NET)
     assert np.all(deg[:two] == 2) and np.all(deg[two:three] == 3) and np.all(deg[three:] > 3)
-    assert two > 0 and three > two
-    cls = np.where(deg == 2, 0, np.where(deg == 3, 1, np.where(deg <= SHORT_NET, 2, np.where(deg <= MID_NET, 3, 4))))
+    assert two > 0 and three > two and g16 > g8 > mid
+    cls = np.select([deg == 2, deg == 3, deg <= SHORT_NET, deg <= MID_NET, deg <= G8_NET, deg <= G16_NET],
+                    [0, 1, 2, 3, 4, 5], 6)
     assert np.all(np.diff(cls) >= 0)                       # classes in order
     assert sorted(perm.tolist()) == list(range(len(perm)))  # a permutation of the pins
     assert sorted(slot.tolist()) == list(range(len(slot)))
@@ -87,7 +90,7 @@ def test_net_order_keeps_nets_and_cell_sums():
     assert np.array_equal(cell_order, cs.cell_pin)
     # short nets of one class are ordered by their lowest cell
     first = np.minimum.reduceat(cs.cell32[perm], ns[:-1])
-    for c in range(5):
+    for c in range(7):
         f = first[cls == c]
         assert np.all(np.diff(f) >= 0)
 
