@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libgp103.so")
-SOURCES = ["wa.cu", "density.cu", "step.cu", "field.cu", "field_tc.cu", "api.cu", "eval.cu", "build.cu", "cluster.cu", "setup.cu", "noalloc.cu", "learn.cu"]
+SOURCES = ["wa.cu", "density.cu", "step.cu", "field.cu", "field_tc.cu", "api.cu", "eval.cu", "build.cu", "cluster.cu", "setup.cu", "noalloc.cu", "learn.cu", "batch.cu"]
 # The density kernels flush float32 denormals as the reference's kernels do (they are built with --use_fast_math).
 PER_FILE = {"density.cu": ["-ftz=true"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -388,7 +388,27 @@ class Placer(object):
         resume: dict(lam, gam, iter, hpwl, first_iter) to go on where a run on the clusters stopped
         (ParamScheduler.resume, src/param_scheduler.py:53-60; _place_level from first_iter, src/run_placement.py:41):
         the density weight lam and smoothing gam carried over, the scheduler's iteration count and last HPWL, the
-        loop counted on from first_iter; no wirelength-only start while lam > 0."""
+        loop counted on from first_iter; no wirelength-only start while lam > 0.
+        The phases are also separate calls (begin, the start phase's passes, start_end, the density phase's passes,
+        end), which a batch of instances in one graph uses (batch.py)."""
+        ctx = self.begin(pos0, resume)
+        if ctx["start"]:
+            while True:
+                self._replay(native.PHASE_START)
+                self.sync()
+                Th = self.T.cpu().numpy()
+                if Th[TI["done"]] or Th[TI["stop"]]:
+                    break
+            out = self.start_end(ctx, log)
+            if out is not None:
+                return out
+        self._density_loop(ctx, log)
+        return self.end(ctx)
+
+    def begin(self, pos0, resume=None):
+        """The host part before the passes: positions clamped into the region, the two probe steps of the step length
+        (estimate_initial_learning_rate and NesterovOptimizer.__init__, four gradient evaluations), and the state of the
+        first phase (T of the wirelength-only start, or S when resumed with the density term on). -> context dict."""
         p, o = self.p, self.p.opts
         t0 = time.time()
         r = resume or {}
@@ -403,7 +423,6 @@ class Placer(object):
             self.kp.copy_(torch.tensor([gam, lam0, lam0, 0, 0], dtype=torch.float32))
             self.cur.zero_()
         g, probe, g2 = self.G[0], self.tmp[0], self.tmp[1]
-        evals = 0
         # estimate_initial_learning_rate (with the density term once its weight is on)
         self.eval(v, g, weight=w, precond=pc)
         d1 = self.probe(v, g, o.lr, probe)
@@ -416,10 +435,10 @@ class Placer(object):
         d1 = self.probe(v, g, lr, probe)
         d2 = self.eval(probe, g2, g_ref=g, weight=w, precond=pc)[0]
         alpha = math.sqrt(d1) / math.sqrt(d2)
-        evals += 4
+        ctx = dict(t0=t0, gam=gam, evals=4, start=lam0 <= 0)
         if lam0 > 0:
-            start_iters, cur = 0, 0
-            lam, a, it0, iter0, hpwl_prev = lam0, 1.0, first, int(r["iter"]), float(r["hpwl"])
+            self._density_state(ctx, lam=lam0, alpha=alpha, a=1.0, it0=first, iter0=int(r["iter"]),
+                                hpwl_prev=float(r["hpwl"]), cur=0, start_iters=0)
         else:
             # the wirelength-only start
             Th = np.zeros(T_SIZE)
@@ -429,29 +448,35 @@ class Placer(object):
             with torch.cuda.stream(self.stream):
                 self.T.copy_(torch.as_tensor(Th))
                 self.kp.copy_(torch.tensor([gam, 0, 0, alpha, 0.0], dtype=torch.float32))
-            while True:
-                self._replay(native.PHASE_START)
-                self.sync()
-                Th = self.T.cpu().numpy()
-                if Th[TI["done"]] or Th[TI["stop"]]:
-                    break
-            evals += int(Th[TI["evals"]])
-            start_iters = int(Th[TI["loop_it"]])
-            if Th[TI["stop"]] == STOP_DEVICE_ERROR:
-                self.check_device("wirelength-only start")
-            if Th[TI["stop"]]:
-                reason = REASON[int(Th[TI["stop"]])]
-                cur = int(self.cur.cpu())
-                return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
-                            overflow=float("nan"), evals=evals, seconds=time.time() - t0, pos=self.V[cur],
-                            iter=int(Th[TI["iter"]]), lam=0.0, gam=gam, density_iters=0)
+        return ctx
+
+    def start_end(self, ctx, log=None):
+        """After the wirelength-only start's passes: the first density weight (density_weight x tension unit) and
+        the density phase's state. -> None, or the result dict when the start phase itself stopped the run."""
+        o = self.p.opts
+        Th = self.T.cpu().numpy()
+        ctx["evals"] += int(Th[TI["evals"]])
+        start_iters = int(Th[TI["loop_it"]])
+        if Th[TI["stop"]] == STOP_DEVICE_ERROR:
+            self.check_device("wirelength-only start")
+        if Th[TI["stop"]]:
+            reason = REASON[int(Th[TI["stop"]])]
             cur = int(self.cur.cpu())
-            # first density weight: density_weight x tension unit (Objective.tension_unit)
-            lam = o.density_weight * self.tension_unit(self.V[cur])[0]
-            if log:
-                log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
-                    % (start_iters, Th[TI["hpwl"]], lam))
-            alpha, a, it0, iter0, hpwl_prev = Th[TI["alpha"]], Th[TI["a"]], start_iters, Th[TI["iter"]], Th[TI["hpwl"]]
+            return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
+                        overflow=float("nan"), evals=ctx["evals"], seconds=time.time() - ctx["t0"], pos=self.V[cur],
+                        iter=int(Th[TI["iter"]]), lam=0.0, gam=ctx["gam"], density_iters=0)
+        cur = int(self.cur.cpu())
+        # first density weight: density_weight x tension unit (Objective.tension_unit)
+        lam = o.density_weight * self.tension_unit(self.V[cur])[0]
+        if log:
+            log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
+                % (start_iters, Th[TI["hpwl"]], lam))
+        self._density_state(ctx, lam=lam, alpha=Th[TI["alpha"]], a=Th[TI["a"]], it0=start_iters,
+                            iter0=Th[TI["iter"]], hpwl_prev=Th[TI["hpwl"]], cur=cur, start_iters=start_iters)
+        return None
+
+    def _density_state(self, ctx, lam, alpha, a, it0, iter0, hpwl_prev, cur, start_iters):
+        gam = ctx["gam"]
         S = np.zeros(len(S_FIELDS))
         S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, gam, alpha, a
         S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = iter0, hpwl_prev, 1.0
@@ -462,7 +487,11 @@ class Placer(object):
             self.S.copy_(torch.as_tensor(S))
             self.kp.copy_(torch.tensor([gam, lam, lam, alpha, coef], dtype=torch.float32))
             self.best.copy_(self.V[cur])
-        logged = it0 // o.log_freq
+        ctx.update(it0=it0, start_iters=start_iters)
+
+    def _density_loop(self, ctx, log=None):
+        o = self.p.opts
+        logged = ctx["it0"] // o.log_freq
         # Batches of passes, each followed by an asynchronous copy of the state into pinned memory. While no stop can
         # come within two batches, the next batch is queued before the host waits for the state of the last one, so
         # the GPU does not idle through the poll; near a predictable stop the host runs exactly the passes left.
@@ -498,6 +527,9 @@ class Placer(object):
                     % (it, Sh[SK["res_hpwl"]], Sh[SK["res_ovf"]], Sh[SK["lam"]], Sh[SK["gam"]]))
             if Sh[SK["stop"]]:
                 break
+
+    def end(self, ctx):
+        """After the density phase's passes: the pending best placement, the result dict."""
         native.call("gp103_finish", self._ref, self.stream.cuda_stream)     # (after any batch still queued)
         self.sync()
         Sh = self.S.cpu().numpy()
@@ -505,8 +537,8 @@ class Placer(object):
             self.check_device("density phase")
         cur = int(self.cur.cpu())
         pos = self.best if Sh[SK["has_best"]] else self.V[cur]
-        return dict(reason=REASON[int(Sh[SK["stop"]])], iters=int(Sh[SK["loop_it"]]), start_iters=start_iters,
+        return dict(reason=REASON[int(Sh[SK["stop"]])], iters=int(Sh[SK["loop_it"]]), start_iters=ctx["start_iters"],
                     hpwl=float(Sh[SK["res_hpwl"]]), overflow=float(Sh[SK["res_ovf"]]),
-                    evals=evals + int(Sh[SK["evals"]]), seconds=time.time() - t0, pos=pos,
-                    density_iters=int(Sh[SK["loop_it"]]) - it0, lam=float(Sh[SK["lam"]]),
+                    evals=ctx["evals"] + int(Sh[SK["evals"]]), seconds=time.time() - ctx["t0"], pos=pos,
+                    density_iters=int(Sh[SK["loop_it"]]) - ctx["it0"], lam=float(Sh[SK["lam"]]),
                     gam=float(Sh[SK["gam"]]), iter=int(Sh[SK["iter"]]))

@@ -177,3 +177,20 @@ def init_positions(nl, num_nodes, seed=0):
     cells = rng.standard_normal((nl.num_mov, 2)).astype(np.float32) * region * np.float32(0.001) + region * np.float32(0.5)
     fill = rng.random((num_nodes - nl.num_mov, 2)).astype(np.float32) * region
     return np.concatenate([cells, fill]).astype(np.float32)
+
+
+def batch_instances(count=64, seed=0, lo=5_000, hi=150_000):
+    """The batched workload (config 3): `count` seeded netlists with cell counts log-uniform in [lo, hi], nets 1.05 x
+    cells, the config-0 degree mix and window, 0-10 macros (over 3-15 % of the region when there are any), one level
+    each (cluster ratio 1), each with its own force grid by the grid rule (about one cell per free bin: 64 .. 512).
+    -> list of (netlist, options dict)."""
+    rng = np.random.default_rng(7_777 + seed)
+    out = []
+    for k in range(count):
+        cells = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        macros = int(rng.integers(0, 11))
+        cover = float(rng.uniform(0.03, 0.15)) if macros else 0.0
+        nl = make_netlist(cells, int(round(cells * 1.05)), window=200, macros=macros, cover=cover,
+                          seed=100_000 * (seed + 1) + k, name="c3_%d_%d" % (seed, k))
+        out.append((nl, {"target_density": 1.0, "num_bin": 0, "force_num_bin": 0, "cluster_ratio": 1.0}))
+    return out

@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-pdl", action="store_true", help="plain stream order instead of programmatic dependent launch")
     p.add_argument("--split", action="store_true", help="the WA kernels on a second stream, beside the density map")
+    p.add_argument("--instances", type=int, default=64, help="--config c3: instances per batch")
     return p.parse_args()
 
 
@@ -438,6 +439,82 @@ def run_gb300(args):
         print(json.dumps(line))
 
 
+def run_batch(args):
+    """--config c3: 64 uneven instances (5k-150k cells, grids 64-512, 0-10 macros), tuned per size class, placed as
+    one batch (one CUDA graph per phase) and one by one; aggregate iterations/s and p50 / p99 time to the stop."""
+    import numpy as np
+    import torch
+    from autoplace_gb300 import engine, problem, synth, tune
+    from autoplace_gb300.batch import Batch
+    from autoplace_gb300.engine import Placer
+    rank, world, local = dist_setup()
+    t_setup = time.time()
+    probs, pos = [], []
+    for nl, o in synth.batch_instances(count=args.instances, seed=rank):
+        pr = problem.Problem(nl, problem.options(**o))
+        probs.append(pr)
+        pos.append(synth.init_positions(nl, pr.num_nodes, seed=1))
+    host_s = time.time() - t_setup
+    t_tune = time.time()
+    tuned = [tune.tune(p, p0) for p, p0 in zip(probs, pos)]
+    tune_s = time.time() - t_tune
+    b = Batch(probs, tuned=tuned)
+    for _ in range(max(args.warmup, 1)):
+        b.run(pos)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = engine.launches()
+    walls, pers, res = [], [], None
+    for _ in range(args.steps):
+        res, per, wall = b.run(pos)
+        walls.append(wall)
+        pers.append(per)
+    launches = engine.launches() - l0
+    clk = clocks.stop()
+    iters = sum(r["iters"] for r in res)
+    wall = reduce_max(statistics.median(walls), world)
+    per = np.median(np.stack(pers), 0)
+    # one by one, the same tuned settings, each Placer set up once (warm-up run first)
+    singles = []
+    for p, p0, t in zip(probs, pos, tuned):
+        pl = Placer(p, field=t["field"])
+        tune.apply_wa(pl, t["wa"])
+        pl.run(p0)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        pl.run(p0)
+        torch.cuda.synchronize()
+        singles.append(time.time() - t0)
+        del pl
+    single_total = float(np.sum(singles))
+    line = {"metric": "aggregate iterations/s, batch of %d uneven instances in one CUDA graph per phase"
+                      % len(probs),
+            "value": round(iters / wall, 1), "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(wall * 1000, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (field per instance: tuned; f64 reductions)",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "synthetic c3: %d instances, cells log-uniform 5k-150k (%d .. %d), nets 1.05x, "
+                                   "0-10 macros, grids %d .. %d, one level each"
+                                   % (len(probs), min(p.num_mov for p in probs), max(p.num_mov for p in probs),
+                                      min(p.force.nbx for p in probs), max(p.force.nbx for p in probs)),
+                       "instances": len(probs), "graphs_per_batch": 2},
+            "result": {"iterations": iters, "batch_s": round(wall, 4),
+                       "time_to_stop_p50_s": round(float(np.percentile(per, 50)), 4),
+                       "time_to_stop_p99_s": round(float(np.percentile(per, 99)), 4),
+                       "one_by_one_s": round(single_total, 4),
+                       "one_by_one_iter_per_s": round(iters / single_total, 1),
+                       "one_by_one_p50_s": round(float(np.percentile(singles, 50)), 4),
+                       "one_by_one_p99_s": round(float(np.percentile(singles, 99)), 4),
+                       "speedup_vs_one_by_one": round(single_total / wall, 3),
+                       "stops": sorted(set(r["reason"] for r in res)),
+                       "tuned": {k: sum(1 for t in tuned if "%s/%s" % (t["field"], t["wa"]) == k)
+                                 for k in set("%s/%s" % (t["field"], t["wa"]) for t in tuned)},
+                       "host_setup_s": round(host_s, 2), "tune_s": round(tune_s, 2)},
+            "clocks": clk, "gpu_launches": int(launches)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def _cpu_judges(prob, pos):
     """Exact HPWL over every net and the movable cells' overflow with their real sizes (float64, the oracle)."""
     import numpy as np
@@ -499,5 +576,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "c3":
+        run_batch(a)
     else:
         run_gb300(a)

@@ -421,6 +421,23 @@ int gp103_learn_features(const int* net_start, const int* pin_cell, const float*
                          double mean_area, float width, float height, int max_hop, void* scratch, size_t scratch_bytes,
                          float* feat, cudaStream_t stream);
 
+/* ------------------------------------------------------------------------------------------------ part 4
+ * Batches of independent placement instances in one CUDA graph (no counterpart in the reference, which runs one
+ * design per process and polls the host every 16 passes, src/gpu_loop.py:58-70). Each instance is a conditional WHILE
+ * node of the graph: its body is `passes` passes of the instance's plan (the first one refreshing the spatial order
+ * when sort_first, density phase) and a condition kernel that ends the loop once the instance's control stops it
+ * (S[14] != 0 in the density phase; T[GP103_T_DONE] or T[GP103_T_STOP] in the start phase) or after max_loops bodies.
+ * The instances are separate branches, so the GPU runs them side by side. *loops (device int, zero it before each
+ * launch) counts an instance's bodies; *stop_ns (device) receives the device time (ns) at which its loop ended.
+ * gp103_batch_add captures the passes on `capture` (a stream of the plan's device, not the legacy default stream);
+ * the plans and their buffers must outlive the batch. gp103_batch_launch instantiates the graph on its first call and
+ * launches it on `stream`, after writing the device time to *t0_ns (when not NULL). */
+int gp103_batch_create(void** batch);
+int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first, int max_loops,
+                    int* loops, unsigned long long* stop_ns, cudaStream_t capture);
+int gp103_batch_launch(void* batch, unsigned long long* t0_ns, cudaStream_t stream);
+int gp103_batch_destroy(void* batch);
+
 #ifdef __cplusplus
 }
 #endif
