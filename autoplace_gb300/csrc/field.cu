@@ -224,6 +224,13 @@ int launch_sgemm(const SGemm& g, cudaStream_t s) {
     return GP103_OK;
 }
 
+// A caller's density less the plan's shift, into the work buffer's density plane (the field of the same map).
+__global__ void shift_density_kernel(const float* d, size_t n, float shift, float* out) {
+    pdl_wait();
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = __fsub_rn(d[e], shift);
+}
+
 int field_fp32(const FieldLayout& L, const void* cbuf, void* wbuf, const float* density, float* ex, float* ey,
                cudaStream_t s) {
     const char* c = (const char*)cbuf;
@@ -231,6 +238,13 @@ int field_fp32(const FieldLayout& L, const void* cbuf, void* wbuf, const float* 
     const int X = L.nbx, Y = L.nby;
     auto F = [&](const char* base, size_t off) { return (const float*)(base + off); };
     auto W = [&](size_t off) { return (float*)(w + off); };
+    if (density && L.shift != 0.f) {            // (the fused path's post kernel writes the shifted plane itself)
+        if (launch_k(shift_density_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density,
+                     (size_t)X * Y, L.shift, W(L.w_a)) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+        density = nullptr;
+    }
     const float* a = density ? density : W(L.w_a);
     int st;
     SGemm g1 = {X, Y, Y, a, F(c, L.c_cy), EPI_TRANS, W(L.w_tt), nullptr, nullptr, nullptr};

@@ -58,16 +58,19 @@ class Flow(object):
         torch.cuda.synchronize(dev)
         t0 = time.time()
         stats, evals, resume, start_iters = {}, 0, None, 0
+        marks = [("begin", t0)]                     # wall times at phase ends (each after a host synchronisation)
         if o.cluster_ratio > 1:
             coarse = cluster.coarse_problem(prob, device=dev, stream=stream)
             cp = coarse.problem
             stream.synchronize()
             stats = dict(clusters=coarse.num, cluster_time_s=time.time() - t0, coarse_num_bin=cp.force.nbx)
+            marks.append(("clustering", time.time()))
             if log:
                 log("two levels: %d clusters of %d cells (%.2fs), %d x %d bins"
                     % (coarse.num, n, stats["cluster_time_s"], cp.force.nbx, cp.force.nby))
             start_gamma = 10 * prob.base_gamma                      # the smoothing the cells start with
             cplacer = Placer(cp, field=self.coarse_field, handover_gamma=start_gamma, **self.kw)
+            marks.append(("cluster_setup", time.time()))
             with torch.cuda.stream(stream):
                 p0 = torch.as_tensor(pos0, dtype=torch.float32).to(dev)
                 cpos0 = torch.cat([p0[:coarse.num], p0[n:]])
@@ -77,7 +80,10 @@ class Flow(object):
                 cpos0, cresume = start(coarse, cplacer, cpos0, prob)
                 stream.synchronize()
                 stats["start_time_s"] = time.time() - t1
+            if start is not None:
+                marks.append(("proposal", time.time()))
             level = cplacer.run(cpos0, log=log, resume=cresume)
+            marks.append(("cluster_level", time.time()))
             cpos = level["pos"]
             pos = cluster.expand(cpos, coarse, prob, o.seed, device=dev, stream=stream)
             with torch.cuda.stream(stream):
@@ -91,6 +97,7 @@ class Flow(object):
             else:
                 gam = _gamma(prob.base_gamma, ovf_fine)
             resume = dict(lam=weight, gam=gam, iter=level["iter"], hpwl=fine.hpwl(pos), first_iter=level["iters"])
+            marks.append(("handover", time.time()))
             if log:
                 log("clusters placed after %d iterations (stop: %s, hpwl %.4E, overflow %.4f): the cells take over, "
                     "density weight %.4E" % (level["iters"], level["reason"], level["hpwl"], level["overflow"],
@@ -103,6 +110,8 @@ class Flow(object):
             del cplacer, cp, cpos                                   # the clusters' buffers are not needed any more
         level = fine.run(pos0, log=log, resume=resume)
         torch.cuda.synchronize(dev)
+        marks.append(("cell_level", time.time()))
+        stats["phase_s"] = {name: round(t - marks[k][1], 5) for k, (name, t) in enumerate(marks[1:])}
         gp_time, iters = time.time() - t0, level["iters"]
         if log:
             log("GP stop (%s): #iters %d hpwl: %.6E overflow: %.4f GP time: %.4fs per iter: %.6fs (%d gradient calls)"

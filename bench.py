@@ -368,7 +368,7 @@ def run_gb300(args):
     result = {"stop": last["stop_reason"], "iterations": iters, "start_iterations": last["start_iters"],
               "clusters": last.get("clusters"), "cluster_iterations": last.get("coarse_iters"),
               "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "overflow_exact": overflow_exact,
-              "ms_per_iteration": round(step_s * 1000 / max(iters, 1), 4),
+              "ms_per_iteration": round(step_s * 1000 / max(iters, 1), 4), "phase_s": last.get("phase_s"),
               "wall_s_per_step": round(wall / max(args.steps, 1), 4)}
 
     # the plain method on the same GPU: the reference's start (wirelength-only) and a float32 field

@@ -26,9 +26,10 @@ def graph_ops(net_start, pin_cell, cell_start, cell_pin, K):
     cnt = np.bincount(pin_net[mov], minlength=N).astype(np.float64)
     inv = np.where(cnt > 0, 1.0 / np.maximum(cnt, 1), 0.0)
     p2n = (pin_net[mov], pin_cell[mov], inv[pin_net[mov]])
-    deg = np.diff(np.asarray(cell_start, np.int64)).astype(np.float64)
-    cells = np.repeat(np.arange(K), np.diff(np.asarray(cell_start, np.int64)))
-    pins = np.asarray(cell_pin, np.int64)
+    cs = np.asarray(cell_start, np.int64)
+    deg = np.diff(cs).astype(np.float64)
+    cells = np.repeat(np.arange(K), np.diff(cs))
+    pins = np.asarray(cell_pin, np.int64)[:cs[-1]]          # (the fixed pins come after the last cell's)
     n2c = (cells, pin_net[pins], 1.0 / np.maximum(deg[cells], 1))
     return p2n, n2c, N
 
