@@ -150,7 +150,7 @@ def coarse_problem(prob, device="cuda", stream=None, build="device"):
     elif nb == prob.num_bin and getattr(prob, "judge_fraction", None) is not None:
         fixed_fraction = prob.judge_fraction
     else:
-        fixed_fraction = nl.fixed_fraction(nb, nb)
+        fixed_fraction = device_fixed_fraction(nl, nb, nb, device=dev, stream=stream)
     copts = SimpleNamespace(**vars(o))
     copts.settle_iter, copts.min_iter = 0, 0
     if build == "host":
@@ -163,6 +163,20 @@ def coarse_problem(prob, device="cuda", stream=None, build="device"):
         pins["node_size"] = np.ascontiguousarray(cprob.node_size, np.float64)
         cprob = cprob.on_device(dev, stream, host=pins)
     return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob)
+
+
+def device_fixed_fraction(nl, nbx, nby, device="cuda", stream=None):
+    """nl.fixed_fraction(nbx, nby) computed on the device (gp103_macro_fraction: the same bits) -> float64 numpy
+    [nbx, nby]."""
+    dev = torch.device(device)
+    stream = stream or torch.cuda.current_stream(dev)
+    rects = np.ascontiguousarray(np.asarray(nl.macros, np.float64).reshape(-1, 4))
+    with torch.cuda.stream(stream):
+        r = torch.as_tensor(rects).to(dev) if len(rects) else None
+        out = torch.empty((nbx, nby), dtype=torch.float64, device=dev)
+    native.call("gp103_macro_fraction", None if r is None else ctypes.c_void_p(r.data_ptr()), len(rects),
+                float(nl.width), float(nl.height), nbx, nby, ctypes.c_void_p(out.data_ptr()), stream.cuda_stream)
+    return out.cpu().numpy()
 
 
 def expand(cpos, coarse, prob, seed, device="cuda", stream=None):

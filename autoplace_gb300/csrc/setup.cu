@@ -304,3 +304,42 @@ extern "C" int gp103_smooth_nodes(const double* size, int n, int num_mov, double
                  min_y, width, height, (float2*)size_s, ratio, (float2*)lo, (float2*)hi, area, cell_pins, pins);
     return GP103_OK;
 }
+
+// ----------------------------------------------------------------------------- fixed fraction of the bins
+// The share of each bin under a fixed object (PlaceData.fixed_fraction, src/database.py:103-134, in the form it takes
+// when the rows cover the whole region and the fixed rectangles do not overlap, as in the synthetic netlists): per
+// bin, the overlap area of every rectangle in rectangle order, over the bin area, clipped to [0, 1]. float64, the
+// host statement's operations in its order (no contraction into fused multiply-adds): the same bits.
+namespace gp103 {
+__global__ void macro_fraction_kernel(const double* rects, int count, double bx, double by, int nbx, int nby,
+                                      double* out) {
+    gp103::pdl_wait();
+    const double area = __dmul_rn(bx, by);
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < (long long)nbx * nby;
+         b += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(b / nby), j = (int)(b - (long long)i * nby);
+        const double x0 = __dmul_rn((double)i, bx), x1 = __dmul_rn((double)(i + 1), bx);
+        const double y0 = __dmul_rn((double)j, by), y1 = __dmul_rn((double)(j + 1), by);
+        double cover = 0.0;
+        for (int m = 0; m < count; m++) {
+            const double* r = rects + 4 * m;
+            const double ox = fmax(__dsub_rn(fmin(x1, r[2]), fmax(x0, r[0])), 0.0);
+            const double oy = fmax(__dsub_rn(fmin(y1, r[3]), fmax(y0, r[1])), 0.0);
+            cover = __dadd_rn(cover, __dmul_rn(ox, oy));
+        }
+        out[b] = fmin(fmax(__ddiv_rn(cover, area), 0.0), 1.0);
+    }
+}
+}  // namespace gp103
+
+extern "C" int gp103_macro_fraction(const double* rects, int count, double width, double height, int nbx, int nby,
+                                    double* fraction, cudaStream_t s) {
+    if (count < 0 || nbx <= 0 || nby <= 0 || !(width > 0.0) || !(height > 0.0) || !fraction || (count > 0 && !rects))
+        return GP103_ERR_ARG;
+    const double bx = width / nbx, by = height / nby;
+    if (gp103::launch_k(macro_fraction_kernel, dim3(gp103::grid_for((long long)nbx * nby, 256, 8)), dim3(256), 0, s,
+                        rects, count, bx, by, nbx, nby, fraction) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}

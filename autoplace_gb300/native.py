@@ -91,6 +91,7 @@ _SIGS = {
     "gp103_smooth_nodes": ([_vp, _i, _i, _d, _d, _f, _f] + [_vp] * 7 + [_vp], _i),
     "gp103_net_order": ([_vp] * 4 + [_i, _i, _i, _vp, ctypes.c_size_t] + [_vp] * 5 + [_vp], _i),
     "gp103_exact_overflow": ([_vp, _vp, _i, _f, _f, _i, _i, _vp, _f, _d, _vp, _vp, _vp, _vp], _i),
+    "gp103_macro_fraction": ([_vp, _i, _d, _d, _i, _i, _vp, _vp], _i),
     # batches of instances in one graph
     "gp103_batch_create": ([ctypes.POINTER(_vp)], _i),
     "gp103_batch_add": ([_vp, ctypes.POINTER(Plan), _i, _i, _i, _i, _vp, _vp, _vp], _i),

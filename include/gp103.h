@@ -345,6 +345,14 @@ int gp103_smooth_nodes(const double* size, int n, int num_mov, double min_x, dou
                        float* size_s, float* ratio, float* lo, float* hi, float* area, const int* cell_pins,
                        float* pins, cudaStream_t stream);
 
+/* The fixed share of every bin of an nbx x nby grid over a width x height region (PlaceData.fixed_fraction,
+ * src/database.py:103-134, in the form it takes when the rows cover the region and the fixed rectangles -- rects
+ * [count][4] = (x0, y0, x1, y1), float64 -- do not overlap): per bin the rectangles' overlap area, in rectangle order,
+ * over the bin area, clipped to [0, 1]; fraction [nbx][nby] float64. The same bits as the host statement (numpy:
+ * the per-rectangle outer products of the x and y overlaps, summed in order). */
+int gp103_macro_fraction(const double* rects, int count, double width, double height, int nbx, int nby,
+                         double* fraction, cudaStream_t stream);
+
 /* ------------------------------------------------------------------------------------------------ part 3
  * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
  * *out is written by the device (read it after synchronising the stream). */
@@ -364,7 +372,7 @@ int gp103_exact_overflow(const float* pos, const float* size, int num_mov, float
                          const float* fixed, float target, double area_scale, unsigned long long* map,
                          void* scratch, double* out, cudaStream_t stream);
 
-/* ------------------------------------------------------------------------------------------------ part 3
+/* ------------------------------------------------------------------------------------------------ part 4
  * The learned start (no counterpart in the reference, whose clusters start at the seeded start positions,
  * src/run_placement.py:98, and run the wirelength-only start, src/run_placement.py:48-65): a message-passing network
  * over the cluster graph proposes the clusters' start positions. The graph is a netlist in the fused path's form:
@@ -421,7 +429,7 @@ int gp103_learn_features(const int* net_start, const int* pin_cell, const float*
                          double mean_area, float width, float height, int max_hop, void* scratch, size_t scratch_bytes,
                          float* feat, cudaStream_t stream);
 
-/* ------------------------------------------------------------------------------------------------ part 4
+/* ------------------------------------------------------------------------------------------------ part 5
  * Batches of independent placement instances in one CUDA graph (no counterpart in the reference, which runs one
  * design per process and polls the host every 16 passes, src/gpu_loop.py:58-70). Each instance is a conditional WHILE
  * node of the graph: its body is `passes` passes of the instance's plan (the first one refreshing the spatial order

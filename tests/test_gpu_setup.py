@@ -138,3 +138,15 @@ def test_device_problem_build_filters(ignore):
                                                        ignore_net_degree=ignore))
     if ignore == 1:
         assert dp.csr.num_nets == 0 and len(dp.csr.cell32) == 0
+
+
+@pytest.mark.parametrize("nb", [(64, 64), (512, 256), (1024, 1024)])
+def test_device_fixed_fraction_is_bit_exact(nb):
+    """The fixed share of the bins on the device (gp103_macro_fraction) against the host statement, bit for bit; with
+    and without macros, on square and non-square grids."""
+    from autoplace_gb300.cluster import device_fixed_fraction
+    for macros, cover in ((40, 0.2), (0, 0.0), (3, 0.12)):
+        nl = synth.make_netlist(20000, 21000, window=200, macros=macros, cover=cover, seed=macros + 1)
+        host = nl.fixed_fraction(*nb)
+        dev = device_fixed_fraction(nl, *nb)
+        assert dev.shape == host.shape and np.array_equal(dev.view(np.uint64), host.view(np.uint64))
