@@ -36,11 +36,62 @@ def limits(area, ratio):
     return int(big), int(math.floor(float(cap)))
 
 
+class Stream(object):
+    """The seeded CPU generator's float32 draws as one stream (torch.rand of torch.Generator().manual_seed(seed)):
+    consecutive torch.rand calls on a generator give the consecutive pieces of one long draw, so the stream is drawn
+    ahead in blocks, and a reader's rounds take the next `num` values each -- the numbers the reference's calls give.
+    Every placement with this seed reads the same stream from its start (reader()); the drawn part is kept."""
+
+    def __init__(self, seed, block):
+        self.gen = torch.Generator().manual_seed(int(seed))
+        self.block = max(int(block), 1)
+        self.buf = np.zeros(0, np.float32)
+
+    def upto(self, count):
+        while len(self.buf) < count:
+            more = max(self.block, count - len(self.buf))
+            self.buf = np.concatenate([self.buf, torch.rand(more, generator=self.gen).numpy()])
+        return self.buf
+
+    def reader(self):
+        stream, at = self, [0]
+
+        class Reader(object):
+            def take(self, num):
+                buf = stream.upto(at[0] + num)
+                out = buf[at[0]:at[0] + num]
+                at[0] += num
+                return out
+        return Reader()
+
+
+def prepare(prob, device="cuda", stream=None, max_degree=8):
+    """What a placement's clustering needs of its design, made once per design (like the cells' own uploads): the
+    pins on the device (int32 cells and nets, float32 offsets), the cells' areas and the merge limits, the pair
+    bound, the heads' seeded stream drawn ahead (four draws per cell) and expand's seeded draws. -> SimpleNamespace."""
+    nl, o, n = prob.nl, prob.opts, prob.num_mov
+    dev = torch.device(device)
+    stream = stream or torch.cuda.current_stream(dev)
+    with torch.cuda.stream(stream):
+        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev, non_blocking=True)
+        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
+        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
+    size = np.asarray(prob.node_size[:n], np.float32)
+    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
+    heads = Stream(o.seed, 4 * n)
+    heads.upto(4 * n)
+    gen = torch.Generator().manual_seed(int(o.seed))
+    return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, limits=limits(area, o.cluster_ratio),
+                           pair_bound=max(pair_bound(nl.pin_net, max_degree), 1), num_nets=int(nl.num_nets),
+                           seed=int(o.seed), heads=heads, expand_draws=torch.rand(n, 2, generator=gen), size=size)
+
+
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
-                  draws=None, stream=None, dev_pins=None):
+                  draws=None, stream=None, dev_pins=None, prep=None):
     """pin_cell / pin_net [P] sorted by net (cell index len(area) = a fixed pin); area [n] int64. -> (cluster of
     every cell [n] int64, area of every cluster [K] int64), as numpy arrays. draws(round, num) -> float32 [num] can
-    stand in for the seeded generator (tests). dev_pins: (pin_cell, pin_net) already on the device as int32."""
+    stand in for the seeded generator (tests). dev_pins: (pin_cell, pin_net) already on the device as int32. prep:
+    prepare()'s result for this design (pins, limits, pair bound, the seeded stream), made once per design."""
     area = np.ascontiguousarray(area, np.int64)
     n = len(area)
     if n == 0:
@@ -49,16 +100,21 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     stream = stream or torch.cuda.current_stream(dev)
     s = stream.cuda_stream
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    big, cap = limits(area, ratio)
-    pin_net = np.asarray(pin_net, np.int64)
-    num_nets = int(pin_net.max()) + 1 if len(pin_net) else 0
-    E = max(pair_bound(pin_net, max_degree), 1)
+    if prep is not None:
+        (big, cap), num_nets, E, dev_pins = prep.limits, prep.num_nets, prep.pair_bound, prep.pins
+        npins = int(prep.pins[0].shape[0])
+    else:
+        big, cap = limits(area, ratio)
+        pin_net = np.asarray(pin_net, np.int64)
+        num_nets = int(pin_net.max()) + 1 if len(pin_net) else 0
+        E = max(pair_bound(pin_net, max_degree), 1)
+        npins = len(pin_net)
     with torch.cuda.stream(stream):
         if dev_pins is not None:
             pc, pn = dev_pins
         else:
             pc = torch.as_tensor(np.asarray(pin_cell, np.int32)).to(dev)
-            pn = torch.as_tensor(pin_net.astype(np.int32)).to(dev)
+            pn = torch.as_tensor(np.asarray(pin_net, np.int32)).to(dev)
         scratch = torch.empty(int(native.lib().gp103_cluster_scratch(n, num_nets, E)), dtype=torch.uint8, device=dev)
         rows = [torch.zeros(n + 1, dtype=torch.int32, device=dev) for _ in range(2)]
         col = [torch.zeros(E, dtype=torch.int32, device=dev) for _ in range(2)]
@@ -67,17 +123,17 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
         counts = torch.zeros(2, dtype=torch.int32, device=dev)
         new_index = torch.zeros(n, dtype=torch.int32, device=dev)
         cid = torch.arange(n, dtype=torch.int32, device=dev)
-    native.call("gp103_cluster_edges", p(pc), p(pn), len(pin_net), num_nets, n, max_degree, E, p(scratch),
+    native.call("gp103_cluster_edges", p(pc), p(pn), npins, num_nets, n, max_degree, E, p(scratch),
                 scratch.numel(), p(rows[0]), p(col[0]), p(wgt[0]), p(counts), s)
     stream.synchronize()
     if int(counts[1]) > E:
         raise RuntimeError("pair bound too small: %d > %d" % (int(counts[1]), E))
-    gen = torch.Generator().manual_seed(int(seed))
+    heads = (prep.heads if prep is not None else Stream(seed, n)).reader()
     num, a = n, 0
     for r in range(max_rounds):
         if num * ratio <= n:
             break
-        d = draws(r, num) if draws is not None else torch.rand(num, generator=gen)
+        d = draws(r, num) if draws is not None else heads.take(num)
         head = torch.as_tensor(np.asarray(d) < np.float32(0.5)).to(torch.uint8)
         with torch.cuda.stream(stream):
             head = head.to(dev)
@@ -95,7 +151,7 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     return cid.cpu().numpy().astype(np.int64), areas[a][:num].cpu().numpy()
 
 
-def coarse_problem(prob, device="cuda", stream=None, build="device"):
+def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
     """The problem of the clusters (coarse_problem, src/cluster.py:88-130), from a cell-level Problem:
       - the cells clustered (cluster_cells, areas in 1/1024 of a site area, rounded from the float32 area);
       - a merged cluster is a square of its summed area with its pins at the centre, one per net; a cluster of one
@@ -104,7 +160,8 @@ def coarse_problem(prob, device="cuda", stream=None, build="device"):
         the cells' grid follows the cells.
     build: "device" = the clusters' per-pin and per-node arrays built on the device from the selected pins
     (Problem.on_device: torch tensors), "host" = downloaded and built in numpy (the same arrays, bit for bit).
-    -> SimpleNamespace(cid [n], num, size [num, 2] float32, problem: the clusters' Problem)."""
+    prep: prepare(prob)'s result (the design's pins on the device, areas, limits, seeded draws), made once per design.
+    -> SimpleNamespace(cid [n], num, size [num, 2] float32, problem: the clusters' Problem, prep)."""
     from . import problem as P
     dev = torch.device(device)
     stream = stream or torch.cuda.current_stream(dev)
@@ -112,14 +169,11 @@ def coarse_problem(prob, device="cuda", stream=None, build="device"):
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     nl, o, n = prob.nl, prob.opts, prob.num_mov
     P_ = len(nl.pin_cell)
-    with torch.cuda.stream(stream):
-        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev, non_blocking=True)
-        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
-        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
-    size = np.asarray(prob.node_size[:n], np.float32)
-    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
+    if prep is None:
+        prep = prepare(prob, device=dev, stream=stream)
+    (pc, pn), po, size, area = prep.pins, prep.pin_off, prep.size, prep.area
     cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
-                               dev_pins=(pc, pn))
+                               prep=prep)
     num = len(carea)
     csize = np.repeat(np.sqrt(carea.astype(np.float64) / 1024).astype(np.float32)[:, None], 2, 1)
     count = np.bincount(cid, minlength=num)
@@ -162,7 +216,7 @@ def coarse_problem(prob, device="cuda", stream=None, build="device"):
                                    fixed_fraction, copts, arrays=False)
         pins["node_size"] = np.ascontiguousarray(cprob.node_size, np.float64)
         cprob = cprob.on_device(dev, stream, host=pins)
-    return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob)
+    return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob, prep=prep)
 
 
 def device_fixed_fraction(nl, nbx, nby, device="cuda", stream=None):
@@ -186,8 +240,12 @@ def expand(cpos, coarse, prob, seed, device="cuda", stream=None):
     dev = torch.device(device)
     stream = stream or torch.cuda.current_stream(dev)
     n, num = prob.num_mov, coarse.num
-    gen = torch.Generator().manual_seed(int(seed))
-    r = torch.rand(n, 2, generator=gen)
+    prep = getattr(coarse, "prep", None)
+    if prep is not None and prep.seed == int(seed):
+        r = prep.expand_draws                           # (the seeded draws, made once per design)
+    else:
+        gen = torch.Generator().manual_seed(int(seed))
+        r = torch.rand(n, 2, generator=gen)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     with torch.cuda.stream(stream):
         cpos = torch.as_tensor(cpos, dtype=torch.float32).to(dev).contiguous()

@@ -46,6 +46,8 @@ class Flow(object):
         self.field, self.coarse_field = field, coarse_field or field
         self.fine = Placer(prob, field=field, host=host, **self.kw)
         self.last_coarse = None
+        # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws)
+        self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
 
     def run(self, pos0, log=None, start=None):
         """Place from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
@@ -60,7 +62,7 @@ class Flow(object):
         stats, evals, resume, start_iters = {}, 0, None, 0
         marks = [("begin", t0)]                     # wall times at phase ends (each after a host synchronisation)
         if o.cluster_ratio > 1:
-            coarse = cluster.coarse_problem(prob, device=dev, stream=stream)
+            coarse = cluster.coarse_problem(prob, device=dev, stream=stream, prep=self.prep)
             cp = coarse.problem
             stream.synchronize()
             stats = dict(clusters=coarse.num, cluster_time_s=time.time() - t0, coarse_num_bin=cp.force.nbx)

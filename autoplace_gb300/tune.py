@@ -6,9 +6,9 @@ Here two choices depend on the instance and are measured, not guessed:
     CUDA-core GEMMs (any grid; on small grids the tensor-core form's fixed costs can dominate);
   - the WA kernels' lane groups, i.e. the degree thresholds between one thread per net, groups of 4 / 8 / 16 lanes and
     a warp per net. The nets are ordered by degree class at set-up, so every partition of the class boundaries below
-    is a valid launch: "default" (<= 8 pins a thread, 9-16 four lanes, 17-32 eight, 33-64 sixteen, longer a warp),
-    "warp" (every net of more than 8 pins a warp), "wide" (9-32 pins eight lanes, 33-64 sixteen), "half" (9-16 four
-    lanes, 17-64 sixteen).
+    is a valid launch: "default" (<= 8 pins a thread, 9-16 four lanes, longer a warp), "groups" (as default, and 17-32
+    pins eight lanes, 33-64 sixteen), "warp" (every net of more than 8 pins a warp), "wide" (9-32 pins eight lanes,
+    33-64 sixteen).
 Each candidate runs `passes` density passes (after `warm` untimed ones) from a mid-run state of the instance; the
 fastest per-pass time wins. Results are cached by the instance's size class (cells rounded to a power of 2, grid).
 """
@@ -19,7 +19,7 @@ import torch
 from . import native
 from .engine import Placer
 
-WA_CHOICES = ("default", "warp", "wide", "half")
+WA_CHOICES = ("default", "groups", "warp", "wide")
 _CACHE = {}
 
 
@@ -27,16 +27,16 @@ def apply_wa(placer, choice):
     """Set the WA class boundaries of a Placer's plan (from the ones its net order found)."""
     pl = placer.plan
     if not hasattr(placer, "_wa_bounds"):
-        placer._wa_bounds = (pl.net_split, pl.net_mid, pl.net_g8, pl.net_g16)
+        placer._wa_bounds = (pl.net_split, pl.net_mid, placer.net_g8, placer.net_g16)
     split, mid, g8, g16 = placer._wa_bounds
     if choice == "default":
+        pl.net_mid, pl.net_g8, pl.net_g16 = mid, 0, 0
+    elif choice == "groups":
         pl.net_mid, pl.net_g8, pl.net_g16 = mid, g8, g16
     elif choice == "warp":
         pl.net_mid, pl.net_g8, pl.net_g16 = split, split, 0
     elif choice == "wide":
         pl.net_mid, pl.net_g8, pl.net_g16 = split, g8, g16
-    elif choice == "half":
-        pl.net_mid, pl.net_g8, pl.net_g16 = mid, mid, g16
     else:
         raise ValueError(choice)
     if pl.net_g16 == 0:
