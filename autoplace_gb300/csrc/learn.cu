@@ -321,22 +321,69 @@ __global__ void anchor_step_kernel(const float* z, int num_cells, int hop, float
     }
 }
 
+// One Jacobi sweep of the harmonic coordinates: each net's mean position over all its pins (a movable pin at its
+// cluster's current estimate h, a fixed pin where it is), r[net] = (x, y, 1) (0 for a net without pins).
+__global__ void net_mean_kernel(const int* net_start, const int* pin_cell, const float2* pin_off, const float* h,
+                                int num_nets, int num_cells, float inv_w, float inv_h, float* r) {
+    pdl_wait();
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < num_nets; e += gridDim.x * blockDim.x) {
+        float sx = 0.f, sy = 0.f;
+        const int b = net_start[e], n = net_start[e + 1] - b;
+        for (int p = b; p < b + n; p++) {
+            const int c = pin_cell[p];
+            if ((unsigned)c < (unsigned)num_cells) {
+                sx += h[2 * c];
+                sy += h[2 * c + 1];
+            } else {
+                sx += pin_off[p].x * inv_w;
+                sy += pin_off[p].y * inv_h;
+            }
+        }
+        r[3 * e] = n ? sx / n : 0.f;
+        r[3 * e + 1] = n ? sy / n : 0.f;
+        r[3 * e + 2] = n ? 1.f : 0.f;
+    }
+}
+
+// The sweep's cluster side: h = z.xy / z.w (the mean over the cluster's nets; a cluster without nets keeps its h).
+__global__ void harmonic_step_kernel(const float* z, int num_cells, float* h) {
+    pdl_wait();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < num_cells; c += gridDim.x * blockDim.x) {
+        const float w = z[3 * c + 2];
+        if (w > 0.f) {
+            h[2 * c] = z[3 * c] / w;
+            h[2 * c + 1] = z[3 * c + 1] / w;
+        }
+    }
+}
+
+// The sweeps start from the anchors (the region's centre for a cluster without one).
+__global__ void harmonic_init_kernel(const float* anc, const float* hops, int num_cells, float* h) {
+    pdl_wait();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < num_cells; c += gridDim.x * blockDim.x) {
+        const bool has = hops[c] >= 0.f;
+        h[2 * c] = has ? anc[3 * c] : 0.5f;
+        h[2 * c + 1] = has ? anc[3 * c + 1] : 0.5f;
+    }
+}
+
 __global__ void fill_kernel(float* p, int n, float v) {
     pdl_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
 
-// Features of each cluster, F = 8: log(area / mean area), log(1 + nets) / 4, log(1 + member pins) / 4, anchor x,
+// Features of each cluster, F = 10: log(area / mean area), log(1 + nets) / 4, log(1 + member pins) / 4, anchor x,
 // anchor y (fractions of the region; the centre when none), hop / max_hop (1 when none), 1 if anchored, the anchor's
-// distance from the region's centre.
+// distance from the region's centre, the harmonic x and y.
 __global__ void features_kernel(const float* area, double mean_area, const int* cell_start, const float* pin_count,
-                                const float* anc, const float* hops, int num_cells, int max_hop, float* feat) {
+                                const float* anc, const float* hops, const float* harm, int num_cells, int max_hop,
+                                float* feat) {
     pdl_wait();
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < num_cells; c += gridDim.x * blockDim.x) {
         const int nets = cell_start[c + 1] - cell_start[c];      // (the cluster problem: one pin per net and cluster)
         const bool has = hops[c] >= 0.f;
         const float ax = has ? anc[3 * c] : 0.5f, ay = has ? anc[3 * c + 1] : 0.5f;
-        float* f = feat + (size_t)c * 8;
+        float* f = feat + (size_t)c * 10;
         f[0] = logf(fmaxf(area[c], 1e-30f) / (float)mean_area);
         f[1] = log1pf((float)nets) * 0.25f;
         f[2] = log1pf(pin_count ? pin_count[c] : (float)nets) * 0.25f;
@@ -345,6 +392,8 @@ __global__ void features_kernel(const float* area, double mean_area, const int* 
         f[5] = has ? hops[c] / (float)max_hop : 1.f;
         f[6] = has ? 1.f : 0.f;
         f[7] = sqrtf((ax - 0.5f) * (ax - 0.5f) + (ay - 0.5f) * (ay - 0.5f));
+        f[8] = harm[2 * c];
+        f[9] = harm[2 * c + 1];
     }
 }
 
@@ -470,16 +519,18 @@ extern "C" int gp103_adam(float* param, const float* grad, float* m, float* v, u
 extern "C" size_t gp103_learn_features_scratch(int num_nets, int num_cells) {
     return ((size_t)3 * num_nets * sizeof(float) + 255 & ~(size_t)255) +
            2 * ((size_t)3 * num_cells * sizeof(float) + 255 & ~(size_t)255) +
-           ((size_t)num_cells * sizeof(float) + 255 & ~(size_t)255);
+           ((size_t)num_cells * sizeof(float) + 255 & ~(size_t)255) +
+           ((size_t)2 * num_cells * sizeof(float) + 255 & ~(size_t)255);
 }
 
 extern "C" int gp103_learn_features(const int* net_start, const int* pin_cell, const float* pin_off,
                                     const int* cell_start, int num_nets, int num_cells, int num_pins,
                                     const int* net_pin_cell, const float* w_p2n, const int* cell_pin_net,
                                     const float* w_n2c, const float* area, const float* pin_count, double mean_area,
-                                    float width, float height, int max_hop, void* scratch, size_t scratch_bytes,
-                                    float* feat, cudaStream_t s) {
-    REQUIRE(num_nets >= 0 && num_cells >= 0 && num_pins >= 0 && max_hop >= 1 && width > 0.f && height > 0.f);
+                                    float width, float height, int max_hop, int sweeps, void* scratch,
+                                    size_t scratch_bytes, float* feat, cudaStream_t s) {
+    REQUIRE(num_nets >= 0 && num_cells >= 0 && num_pins >= 0 && max_hop >= 1 && sweeps >= 0 && width > 0.f &&
+            height > 0.f);
     REQUIRE(net_start && cell_start && feat && scratch && mean_area > 0.0);
     REQUIRE(scratch_bytes >= gp103_learn_features_scratch(num_nets, num_cells));
     REQUIRE(num_pins == 0 || (pin_cell && pin_off && net_pin_cell && w_p2n && cell_pin_net && w_n2c));
@@ -494,6 +545,8 @@ extern "C" int gp103_learn_features(const int* net_start, const int* pin_cell, c
     float* z = (float*)w;
     w += up((size_t)3 * num_cells * sizeof(float));
     float* hops = (float*)w;
+    w += up((size_t)num_cells * sizeof(float));
+    float* harm = (float*)w;
     if (cudaMemsetAsync(anc, 0, sizeof(float) * 3 * num_cells, s) != cudaSuccess) return GP103_ERR_CUDA;
     if (launch_k(fill_kernel, dim3(grid_for(num_cells, 256, 8)), dim3(256), 0, s, hops, num_cells, -1.f) !=
         cudaSuccess)                                                 // no anchor yet
@@ -520,8 +573,26 @@ extern "C" int gp103_learn_features(const int* net_start, const int* pin_cell, c
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }
-    if (launch_k(features_kernel, dim3(grid_for(num_cells, 256, 8)), dim3(256), 0, s, area, mean_area, cell_start,
-                 pin_count, (const float*)anc, (const float*)hops, num_cells, max_hop, feat) != cudaSuccess)
+    // the harmonic coordinates: from the anchors, `sweeps` Jacobi sweeps of the mean over each cluster's nets
+    const int gc = grid_for(num_cells, 256, 8), ge = grid_for(num_nets > 0 ? num_nets : 1, 256, 8);
+    if (launch_k(harmonic_init_kernel, dim3(gc), dim3(256), 0, s, (const float*)anc, (const float*)hops, num_cells,
+                 harm) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    for (int k = 0; k < sweeps && num_nets > 0; k++) {
+        if (launch_k(net_mean_kernel, dim3(ge), dim3(256), 0, s, net_start, pin_cell, (const float2*)pin_off,
+                     (const float*)harm, num_nets, num_cells, 1.f / width, 1.f / height, rnet) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+        int st;
+        if ((st = gp103_seg_gather(cell_start, num_cells, cell_pin_net, w_n2c, rnet, 3, 0, z, s))) return st;
+        if (launch_k(harmonic_step_kernel, dim3(gc), dim3(256), 0, s, (const float*)z, num_cells, harm) !=
+            cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
+    if (launch_k(features_kernel, dim3(gc), dim3(256), 0, s, area, mean_area, cell_start, pin_count,
+                 (const float*)anc, (const float*)hops, (const float*)harm, num_cells, max_hop, feat) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;

@@ -49,12 +49,22 @@ class Flow(object):
         # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws)
         self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
 
-    def run(self, pos0, log=None, start=None):
+    def run(self, pos0, log=None, start=None, fallback=True):
         """Place from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's
         (stop_reason, iters, start_iters, gp_time_s, per_iter_s, grad_calls; with two levels also clusters,
         cluster_time_s, coarse_num_bin, coarse_iters) plus pos (final positions on the device), hpwl and overflow of
         the kept placement as the control measured them, and placer (the cells' Placer: placer.evaluate(pos) gives
-        the exact HPWL and overflow)."""
+        the exact HPWL and overflow). fallback: a placement from a `start` proposal that does not converge is placed
+        again from the reference's start (stats["fallback"] = True)."""
+        st = self._run(pos0, log, start)
+        if start is not None and fallback and st["stop_reason"] != "converged":
+            if log:
+                log("the proposal's placement stopped (%s): placed again from the plain start" % st["stop_reason"])
+            st = self._run(pos0, log, None)
+            st["fallback"] = True
+        return st
+
+    def _run(self, pos0, log, start):
         prob, fine, stream, dev = self.prob, self.fine, self.stream, self.dev
         o, n = prob.opts, prob.num_mov
         torch.cuda.synchronize(dev)

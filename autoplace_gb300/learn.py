@@ -3,7 +3,7 @@ the reference's start (the clusters at the seeded start positions, src/run_place
 start, src/run_placement.py:48-65 with src/param_scheduler.py:42-48). The reference has no learned part.
 
 Network (3 message-passing layers, hidden width 64, bf16 weights with an fp32 master copy, fp32 accumulation):
-    h0      = relu(x W0 + b0)                              x: 8 features per cluster (gp103_learn_features)
+    h0      = relu(x W0 + b0)                              x: 10 features per cluster (gp103_learn_features)
     a_l     = N2C(P2N(h_l))                                mean over each net's clusters, then over a cluster's nets
     h_{l+1} = relu(h_l S_l + a_l N_l + b_l),  l = 0, 1, 2
     y       = sigmoid(h3 Wo + bo)                          (x, y) as fractions of the region
@@ -17,8 +17,10 @@ of its cells. Training and inference run on the GPU through the same kernels.
 Use: Proposal(load_model()).hook is the `start` of flow.Flow.run: it computes the features of the run's clusters,
 runs the network, and starts the clusters' level from the proposed positions with the density term on (no
 wirelength-only start), the density weight in tension units as the plain start's first weight times the model's
-`lam_scale`. The plain start is the fallback (fallback_run): the plain method's HPWL and exact overflow judge the
-learned run, and the plain run is kept when the learned one's HPWL is worse at a matched overflow.
+`lam_scale`. The plain start is the fallback, at two levels: a model is used only when its held-out validation
+placements (the plain method's exact HPWL and overflow judging them, both runs at the same stop overflow) kept the
+plain start's HPWL within 1 % (the model file's `use`, model_available); and a placement from the proposal that does
+not converge is placed again from the plain start (flow.Flow.run(fallback=True)).
 """
 import ctypes
 import math
@@ -32,7 +34,7 @@ from . import native
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODEL_FILE = os.path.join(HERE, "start_net.npz")
-F_IN, WIDTH, LAYERS, MAX_HOP = 8, 64, 3, 12
+F_IN, WIDTH, LAYERS, MAX_HOP, SWEEPS = 10, 64, 3, 12, 64
 ACT_NONE, ACT_RELU, ACT_SIGMOID = 0, 1, 2
 
 def lib():
@@ -91,9 +93,9 @@ class Graph(object):
         _call("gp103_seg_gather", _p(self.cell_start), self.K, _p(self.cell_pin_net), _p(self.w_p2nt), _p(out_net), w,
               int(accumulate), _p(out), s)
 
-    def features(self, area, width, height, pin_count=None, max_hop=MAX_HOP):
-        """[K, 8] features (gp103_learn_features): area, nets, member pins, the propagated fixed-pin anchor and its
-        hop distance. area, pin_count: [K] device tensors (float32)."""
+    def features(self, area, width, height, pin_count=None, max_hop=MAX_HOP, sweeps=SWEEPS):
+        """[K, 10] features (gp103_learn_features): area, nets, member pins, the propagated fixed-pin anchor and its
+        hop distance, the harmonic coordinates. area, pin_count: [K] device tensors (float32)."""
         dev = self.net_start.device
         with torch.cuda.stream(self.stream):
             area = area.to(dev, torch.float32).contiguous()
@@ -104,7 +106,8 @@ class Graph(object):
             pc = None if pin_count is None else pin_count.to(dev, torch.float32).contiguous()
         _call("gp103_learn_features", _p(self.net_start), _p(self.pin_cell), _p(self.pin_off), _p(self.cell_start),
               self.N, self.K, self.P, _p(self.net_pin_cell), _p(self.w_p2n), _p(self.cell_pin_net), _p(self.w_n2c),
-              _p(area), _p(pc), max(mean_area, 1e-30), float(width), float(height), int(max_hop), _p(scratch),
+              _p(area), _p(pc), max(mean_area, 1e-30), float(width), float(height), int(max_hop), int(sweeps),
+              _p(scratch),
               scratch.numel(), _p(feat), self.stream.cuda_stream)
         return feat[:self.K]
 
@@ -251,7 +254,10 @@ class Pass(object):
 
 # ------------------------------------------------------------------------------------------------ models on disk
 def model_available(path=MODEL_FILE):
-    return os.path.exists(path)
+    """A trained model whose validation kept the plain start's HPWL within 1 % is present."""
+    if not os.path.exists(path):
+        return False
+    return bool(load_model(path).get("use", False))
 
 
 def load_model(path=MODEL_FILE):
@@ -271,7 +277,7 @@ def save_model(path, params, **meta):
 
 # ------------------------------------------------------------------------------------------------ the proposal
 def cluster_inputs(coarse, prob, device="cuda", stream=None):
-    """The features of a run's clusters: (Graph, features [K, 8]) from cluster.coarse_problem's result."""
+    """The features of a run's clusters: (Graph, features [K, 10]) from cluster.coarse_problem's result."""
     cp = coarse.problem
     K = coarse.num
     stream = stream or torch.cuda.current_stream(torch.device(device))
@@ -469,7 +475,7 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--workers", type=int, default=max((os.cpu_count() or 2) - 2, 1))
-    ap.add_argument("--lam-scales", default="1,3,10")
+    ap.add_argument("--lam-scales", default="1,3,10,30")
     ap.add_argument("--out", default=MODEL_FILE)
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
@@ -484,17 +490,23 @@ def main(argv=None):
     scales = [float(x) for x in a.lam_scales.split(",")]
     model = {"params": params}
     rows = evaluate_start(range(100_000, 100_000 + a.val), model, scales, log=log)
-    # the density-weight scale: the fastest mean time whose HPWL stays within 1 % of the plain start's on average
-    best, best_t = 1.0, None
+    # the density-weight scale: the fastest mean time whose HPWL stays within 1 % of the plain start's on average (the
+    # fallback rule: no such scale, or none faster than the plain start -> the model is not used)
+    best, best_t, summary = 1.0, None, {}
     for ls in scales:
         k = "learned_%g" % ls
         t = float(np.mean([r[k]["seconds"] / r["plain"]["seconds"] for r in rows]))
         h = float(np.mean([r[k]["hpwl"] / r["plain"]["hpwl"] for r in rows]))
-        log("lam_scale %g: time / plain %.3f, hpwl / plain %.4f" % (ls, t, h))
+        it = float(np.mean([r[k]["iters"] / r["plain"]["iters"] for r in rows]))
+        summary[ls] = (t, h, it)
+        log("lam_scale %g: time / plain %.3f, iterations / plain %.3f, hpwl / plain %.4f" % (ls, t, it, h))
         if h <= 1.01 and (best_t is None or t < best_t):
             best, best_t = ls, t
-    save_model(a.out, params, lam_scale=best, train_samples=len(samples), epochs=a.epochs,
-               final_loss=hist[-1], gen_seconds=t_gen, train_seconds=t_train)
+    use = best_t is not None and best_t < 1.0
+    t, h, it = summary.get(best, (1.0, 1.0, 1.0))
+    save_model(a.out, params, lam_scale=best, use=use, val_time_ratio=t, val_hpwl_ratio=h, val_iter_ratio=it,
+               train_samples=len(samples), epochs=a.epochs, final_loss=hist[-1], gen_seconds=t_gen,
+               train_seconds=t_train)
     if a.report:
         with open(a.report, "w") as f:
             json.dump(dict(history=hist, rows=rows, lam_scale=best, gen_seconds=t_gen, train_seconds=t_train,

@@ -108,7 +108,7 @@ _SIGS = {
     "gp103_mse": ([_vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     "gp103_adam": ([_vp, _vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _i, _f, _vp], _i),
     "gp103_learn_features_scratch": ([_i, _i], _sz),
-    "gp103_learn_features": ([_vp] * 4 + [_i, _i, _i] + [_vp] * 6 + [_d, _f, _f, _i, _vp, _sz, _vp, _vp], _i),
+    "gp103_learn_features": ([_vp] * 4 + [_i, _i, _i] + [_vp] * 6 + [_d, _f, _f, _i, _i, _vp, _sz, _vp, _vp], _i),
 }
 EVAL_SCRATCH_BYTES = 16640
 

@@ -417,17 +417,19 @@ int gp103_mse(const float* y, const float* t, int n, int dim, float* dy, double*
 int gp103_adam(float* param, const float* grad, float* m, float* v, uint16_t* param_bf16, int n, float lr, float beta1,
                float beta2, float eps, int step, float weight_decay, cudaStream_t stream);
 
-/* The 8 input features of every cell of the graph [num_cells][8]: log(area / mean_area), log(1 + nets) / 4,
+/* The 10 input features of every cell of the graph [num_cells][10]: log(area / mean_area), log(1 + nets) / 4,
  * log(1 + pin_count) / 4 (pin_count NULL: the cell's pins), the anchor (x / width, y / height: at hop 0 the mean of
  * the fixed pins on the cell's nets, then, hop by hop up to max_hop, the mean over each net's anchored cells averaged
  * over the cell's nets; the centre when none), hop / max_hop (1 when none), 1 if anchored, the anchor's distance from
- * the centre. The gather weights come from gp103_learn_graph. scratch: gp103_learn_features_scratch bytes. */
+ * the centre, and the harmonic coordinates: from the anchors, `sweeps` Jacobi sweeps in which every cell takes the
+ * mean over its nets of each net's mean pin position (fixed pins held where they are). The gather weights come from
+ * gp103_learn_graph. scratch: gp103_learn_features_scratch bytes. */
 size_t gp103_learn_features_scratch(int num_nets, int num_cells);
 int gp103_learn_features(const int* net_start, const int* pin_cell, const float* pin_off, const int* cell_start,
                          int num_nets, int num_cells, int num_pins, const int* net_pin_cell, const float* w_p2n,
                          const int* cell_pin_net, const float* w_n2c, const float* area, const float* pin_count,
-                         double mean_area, float width, float height, int max_hop, void* scratch, size_t scratch_bytes,
-                         float* feat, cudaStream_t stream);
+                         double mean_area, float width, float height, int max_hop, int sweeps, void* scratch,
+                         size_t scratch_bytes, float* feat, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------------------------------ part 5
  * Batches of independent placement instances in one CUDA graph (no counterpart in the reference, which runs one

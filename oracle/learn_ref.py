@@ -67,11 +67,13 @@ def forward_backward(params, x, target, net_start, pin_cell, cell_start, cell_pi
     return y.detach().numpy(), float(loss.detach()), {k: v.grad.numpy() for k, v in leaves.items()}
 
 
-def features(net_start, pin_cell, pin_off, cell_start, cell_pin, K, area, pin_count, width, height, max_hop=12):
-    """The 8 features of each cluster (gp103_learn_features) in float64: log(area / mean), log(1 + nets) / 4,
+def features(net_start, pin_cell, pin_off, cell_start, cell_pin, K, area, pin_count, width, height, max_hop=12,
+             sweeps=64):
+    """The 10 features of each cluster (gp103_learn_features) in float64: log(area / mean), log(1 + nets) / 4,
     log(1 + member pins) / 4, the anchor (x, y as fractions of the region: at hop 0 the mean of the fixed pins of the
     cluster's nets, then the mean over the anchored clusters of each net, averaged over the cluster's nets), hop /
-    max_hop, anchored, the anchor's distance from the centre."""
+    max_hop, anchored, the anchor's distance from the centre, the harmonic x and y (from the anchors, `sweeps` Jacobi
+    sweeps: a net's mean over all its pins, a fixed pin where it is, then a cluster's mean over its nets)."""
     net_start = np.asarray(net_start, np.int64)
     pin_cell = np.asarray(pin_cell, np.int64)
     off = np.asarray(pin_off, np.float64)
@@ -113,6 +115,18 @@ def features(net_start, pin_cell, pin_off, cell_start, cell_pin, K, area, pin_co
     area = np.asarray(area, np.float64)
     ax = np.where(hops >= 0, anc[:, 0], 0.5)
     ay = np.where(hops >= 0, anc[:, 1], 0.5)
+    h = np.stack([ax, ay], 1)
+    deg = np.diff(net_start).astype(np.float64)
+    fixed_xy = np.stack([off[:, 0] / width, off[:, 1] / height], 1)
+    for _ in range(sweeps):
+        pin_xy = np.where(fixed[:, None], fixed_xy, h[np.minimum(pin_cell, K - 1)])
+        r = np.zeros((N, 3))
+        np.add.at(r[:, :2], pin_net, pin_xy)
+        r[:, :2] /= np.maximum(deg, 1)[:, None]
+        r[:, 2] = deg > 0
+        z = n2c_mean(r)
+        upd = z[:, 2] > 0
+        h[upd] = z[upd, :2] / z[upd, 2:3]
     return np.stack([np.log(area / area.mean()), np.log1p(nets) / 4, np.log1p(np.asarray(pin_count, np.float64)) / 4,
                      ax, ay, np.where(hops >= 0, hops / max_hop, 1.0), (hops >= 0).astype(np.float64),
-                     np.sqrt((ax - 0.5) ** 2 + (ay - 0.5) ** 2)], 1)
+                     np.sqrt((ax - 0.5) ** 2 + (ay - 0.5) ** 2), h[:, 0], h[:, 1]], 1)

@@ -38,8 +38,10 @@ def test_features_match_oracle(clusters):
     pins = np.bincount(coarse.cid, weights=np.asarray(prob.nl.cell_pins, np.float64), minlength=K)
     ref = R.features(a["net_start"], a["pin_cell"], a["pin_off"], a["cell_start"], a["cell_pin"], K, area, pins,
                      prob.nl.width, prob.nl.height)
-    assert x.shape == ref.shape == (K, 8)
-    assert np.abs(x - ref).max() <= 1e-5, np.abs(x - ref).max(0)
+    assert x.shape == ref.shape == (K, 10)
+    # (the 64 harmonic sweeps run in float32 on the device: 1e-4 there, 1e-5 on the rest)
+    assert np.abs(x[:, :8] - ref[:, :8]).max() <= 1e-5, np.abs(x - ref).max(0)
+    assert np.abs(x[:, 8:] - ref[:, 8:]).max() <= 1e-4, np.abs(x - ref).max(0)
     anchored = ref[:, 6] > 0
     assert 0.5 < anchored.mean() <= 1.0                      # most clusters reach a fixed pin within 12 hops
 

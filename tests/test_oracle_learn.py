@@ -22,11 +22,13 @@ def _tiny_graph():
 
 def test_features_anchor_propagation():
     ns, pc, po, cs, cp = _tiny_graph()
-    f = R.features(ns, pc, po, cs, cp, 4, np.ones(4), np.full(4, 2.0), 100.0, 100.0, max_hop=4)
+    f = R.features(ns, pc, po, cs, cp, 4, np.ones(4), np.full(4, 2.0), 100.0, 100.0, max_hop=4, sweeps=200)
     # clusters 0 and 1 sit on the fixed pin's net: anchored at hop 0 at (0.1, 0.2); 2 and 3 reach it at hop 1
     assert np.allclose(f[:, 3], 0.1) and np.allclose(f[:, 4], 0.2)
     assert np.allclose(f[:, 5], [0.0, 0.0, 0.25, 0.25]) and np.all(f[:, 6] == 1.0)
     assert np.allclose(f[:, 0], 0.0) and np.allclose(f[:, 1], np.log1p(2) / 4)
+    # the harmonic coordinates of a graph with one fixed pin converge to that pin's position
+    assert np.allclose(f[:, 8], 0.1, atol=1e-6) and np.allclose(f[:, 9], 0.2, atol=1e-6)
 
 
 def test_autograd_against_central_differences():
@@ -36,7 +38,7 @@ def test_autograd_against_central_differences():
     params = L.init_params(seed=1)
     for k in params:
         params[k] = (params[k] + rng.standard_normal(params[k].shape) * 0.05).astype(np.float32)
-    x = rng.random((4, 8)).astype(np.float32)
+    x = rng.random((4, 10)).astype(np.float32)
     t = rng.random((4, 2)).astype(np.float32)
     y, loss, grads = R.forward_backward(params, x, t, ns, pc, cs, cp, 4)
     # biases are not rounded to bf16: central differences on them in float64 arithmetic of the same forward
