@@ -19,6 +19,7 @@ int after_launch(cudaStream_t s, const char* name);
 bool pdl_enabled();
 long long tc_wait_ns();     // GP103_OPT_WAIT_MS, in ns: the limit of a tensor-core field wait
 bool tc_test_stall();       // GP103_OPT_TEST_STALL_FIELD
+int wa_long_share();        // GP103_OPT_WA_FUSED: percent of the fused WA launch's blocks on long nets (0: two launches)
 
 // Programmatic dependent launch: a kernel may be launched while the one before it on the stream is finishing; it
 // waits here (at its very start, before touching any data) until that one has completed and its writes are

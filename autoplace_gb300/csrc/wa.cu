@@ -237,15 +237,13 @@ __device__ __forceinline__ void net_two_pair(const WaJob& j, const float2* pos, 
 // (any order) are done by the whole warp in turn; without it every net below split is short (the ordered layout).
 // Blocks write float64 partials at bid0 + blockIdx.x of nblk.
 template <bool LONG>
-__global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
-    pdl_wait();
+__device__ __forceinline__ void wa_short_body(const WaJob& j, int blk, int nb, float& wa_sum, float& hp_sum) {
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
     const int lane = threadIdx.x & 31;
-    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long nwarps = (long long)nb * (blockDim.x >> 5);
     const long long chunks = (j.split + 31) / 32;
-    float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float32 warp trees, float64 across warps and blocks
-    for (long long it = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < chunks; it += nwarps) {
+    for (long long it = (long long)blk * (blockDim.x >> 5) + (threadIdx.x >> 5); it < chunks; it += nwarps) {
         const int i = (int)(it * 32) + lane;
         const bool valid = i < j.split;
         int s = 0, d = 0;
@@ -287,6 +285,13 @@ __global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ W
             }
         }
     }
+}
+
+template <bool LONG>
+__global__ void __launch_bounds__(256) wa_short_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
+    pdl_wait();
+    float wa_sum = 0.f, hp_sum = 0.f;          // per-thread partials (a few nets); float32 warp trees, float64 across warps and blocks
+    wa_short_body<LONG>(j, blockIdx.x, gridDim.x, wa_sum, hp_sum);
     if (j.red.partials) {
         float v[2] = {wa_sum, hp_sum};
         grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
@@ -319,18 +324,16 @@ __host__ __device__ inline int group_items(int first, int end, int lanes) {
     return (end - first + 32 / lanes - 1) / (32 / lanes);
 }
 
-__global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
-    pdl_wait();
+__device__ __forceinline__ void wa_long_body(const WaJob& j, int blk, int nb, float& wa_sum, float& hp_sum) {
     const float2* pos = pick(j.pos_a, j.pos_b, j.sel);
     const float ig = __frcp_rn(*j.gamma);
     const int lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const int nwarps = nb * (blockDim.x >> 5);
     const int n4 = group_items(j.split, j.mid, 4), n8 = group_items(j.mid, j.g8, 8);
     const int n16 = group_items(j.g8, j.g16, 16);
     const int groups = n4 + n8 + n16;
     const int items = groups + (j.num_nets - j.g16);
-    float wa_sum = 0.f, hp_sum = 0.f;
-    for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
+    for (int it = blk * (blockDim.x >> 5) + (threadIdx.x >> 5); it < items; it += nwarps) {
         if (it < n4) {                                       // (every branch is uniform over the warp)
             group_item<4>(j, pos, ig, j.split, j.mid, it, lane, wa_sum, hp_sum);
         } else if (it < n4 + n8) {
@@ -349,9 +352,29 @@ __global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ Wa
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(256) wa_long_kernel(const __grid_constant__ WaJob j, int bid0, int nblk) {
+    pdl_wait();
+    float wa_sum = 0.f, hp_sum = 0.f;
+    wa_long_body(j, blockIdx.x, gridDim.x, wa_sum, hp_sum);
     if (j.red.partials) {
         float v[2] = {wa_sum, hp_sum};
         grid_sum<2>(v, j.red, nblk, bid0 + (int)blockIdx.x);
+    }
+}
+
+// Both halves in one launch (the ordered layout): blocks [0, nlong) take the long nets, the rest the short ones, so
+// the two run side by side in one resident wave instead of one after the other (each with its own tail). Partials:
+// block b writes slot b of nblk = gridDim.x.
+__global__ void __launch_bounds__(256) wa_fused_kernel(const __grid_constant__ WaJob j, int nlong) {
+    pdl_wait();
+    float wa_sum = 0.f, hp_sum = 0.f;
+    if ((int)blockIdx.x < nlong) wa_long_body(j, blockIdx.x, nlong, wa_sum, hp_sum);
+    else wa_short_body<false>(j, blockIdx.x - nlong, gridDim.x - nlong, wa_sum, hp_sum);
+    if (j.red.partials) {
+        float v[2] = {wa_sum, hp_sum};
+        grid_sum<2>(v, j.red, gridDim.x, (int)blockIdx.x);
     }
 }
 
@@ -362,6 +385,15 @@ int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
     static const int res_short = resident_blocks(wa_short_kernel<false>, 256);
     static const int res_long = resident_blocks(wa_long_kernel, 256);
+    const int pct = wa_long_share();
+    if (pct > 0 && !inline_long && chunks > 0 && longs > 0) {
+        // one resident wave: pct % of its blocks on the long nets, the rest on the short ones
+        static const int res = resident_blocks(wa_fused_kernel, 256);
+        const int nlong = max(1, min((res * pct + 50) / 100, res - 1));
+        if (launch_k(wa_fused_kernel, dim3(res), dim3(256), 0, s, j, nlong) != cudaSuccess) return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+        return GP103_OK;
+    }
     const int g1 = chunks > 0 || longs == 0 ? min(grid_for(chunks * 32, 256, 8), res_short) : 0;
     const int g2 = longs > 0 ? min(grid_for(longs * 32, 256, 4), res_long) : 0;
     if (g1 > 0) {
