@@ -365,7 +365,8 @@ def run_gb300(args):
     step_s = reduce_max(step_s, world)
     iters = last["iters"]
     hpwl_exact, overflow_exact = flow.fine.evaluate(last["pos"])
-    result = {"stop": last["stop_reason"], "iterations": iters, "start_iterations": last["start_iters"],
+    result = {"stop": last["stop_reason"], "fallback": bool(last.get("fallback", False)),
+              "iterations": iters, "start_iterations": last["start_iters"],
               "clusters": last.get("clusters"), "cluster_iterations": last.get("coarse_iters"),
               "hpwl_exact": hpwl_exact, "overflow": last["overflow"], "overflow_exact": overflow_exact,
               "ms_per_iteration": round(step_s * 1000 / max(iters, 1), 4), "phase_s": last.get("phase_s"),
@@ -384,6 +385,14 @@ def run_gb300(args):
         result["speedup_vs_plain"] = round(p_s / step_s, 3)
         result["hpwl_vs_plain"] = round(hpwl_exact / ph, 5)
         del pflow
+        if start is not None:
+            # the learned start's own share: the same tensor-core field with the plain start
+            flow.run(dpos)
+            t_s, tst, _ = _timed_runs(flow, dpos, args.plain_steps)
+            th, to = flow.fine.evaluate(tst["pos"])
+            plain["tc_plain_start"] = {"value": round(t_s, 4), "iterations": tst["iters"], "hpwl_exact": th,
+                                       "overflow_exact": to}
+            result["speedup_vs_tc_plain_start"] = round(t_s / step_s, 3)
 
     # e2e: from the netlist's pinned host arrays through the public API: upload, the problem's arrays built on the
     # device (net CSR, cell order, smoothed nodes), the cells' Placer and the flow, the run (the clusters' pins are
