@@ -81,17 +81,23 @@ def prepare(prob, device="cuda", stream=None, max_degree=8):
     heads = Stream(o.seed, 4 * n)
     heads.upto(4 * n)
     gen = torch.Generator().manual_seed(int(o.seed))
-    return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, limits=limits(area, o.cluster_ratio),
-                           pair_bound=max(pair_bound(nl.pin_net, max_degree), 1), num_nets=int(nl.num_nets),
-                           seed=int(o.seed), heads=heads, expand_draws=torch.rand(n, 2, generator=gen), size=size)
+    with torch.cuda.stream(stream):
+        area_dev = torch.as_tensor(area).to(dev, non_blocking=True)
+        size_dev = torch.as_tensor(size).to(dev, non_blocking=True)
+        draws_dev = torch.rand(n, 2, generator=gen).to(dev, non_blocking=True)
+    return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, area_dev=area_dev, size_dev=size_dev,
+                           limits=limits(area, o.cluster_ratio), pair_bound=max(pair_bound(nl.pin_net, max_degree), 1),
+                           num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, expand_draws=draws_dev,
+                           size=size)
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
-                  draws=None, stream=None, dev_pins=None, prep=None):
+                  draws=None, stream=None, dev_pins=None, prep=None, on_device=False):
     """pin_cell / pin_net [P] sorted by net (cell index len(area) = a fixed pin); area [n] int64. -> (cluster of
     every cell [n] int64, area of every cluster [K] int64), as numpy arrays. draws(round, num) -> float32 [num] can
     stand in for the seeded generator (tests). dev_pins: (pin_cell, pin_net) already on the device as int32. prep:
-    prepare()'s result for this design (pins, limits, pair bound, the seeded stream), made once per design."""
+    prepare()'s result for this design (pins, limits, pair bound, the seeded stream), made once per design.
+    on_device: -> (cluster of every cell [n] int32, area of every cluster [K] int64) as device tensors instead."""
     area = np.ascontiguousarray(area, np.int64)
     n = len(area)
     if n == 0:
@@ -119,7 +125,8 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
         rows = [torch.zeros(n + 1, dtype=torch.int32, device=dev) for _ in range(2)]
         col = [torch.zeros(E, dtype=torch.int32, device=dev) for _ in range(2)]
         wgt = [torch.zeros(E, dtype=torch.int32, device=dev) for _ in range(2)]
-        areas = [torch.as_tensor(area).to(dev), torch.zeros(n, dtype=torch.int64, device=dev)]
+        areas = [prep.area_dev.clone() if prep is not None else torch.as_tensor(area).to(dev),
+                 torch.zeros(n, dtype=torch.int64, device=dev)]
         counts = torch.zeros(2, dtype=torch.int32, device=dev)
         new_index = torch.zeros(n, dtype=torch.int32, device=dev)
         cid = torch.arange(n, dtype=torch.int32, device=dev)
@@ -147,8 +154,25 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
             break
         native.call("gp103_cluster_relabel", p(cid), n, p(new_index), s)
         num, a = kept, b
+    if on_device:
+        return cid, areas[a][:num]
     stream.synchronize()
     return cid.cpu().numpy().astype(np.int64), areas[a][:num].cpu().numpy()
+
+
+class Clusters(object):
+    """coarse_problem's result: cid_dev [n] (device int32), num, size [num, 2] float32 (host), single_dev [num]
+    (device uint8), problem, prep; cid [n] (host int64) downloaded on first use."""
+
+    def __init__(self, cid_dev, num, size, single_dev, problem, prep):
+        self.cid_dev, self.num, self.size, self.single_dev = cid_dev, num, size, single_dev
+        self.problem, self.prep, self._cid = problem, prep, None
+
+    @property
+    def cid(self):
+        if self._cid is None:
+            self._cid = self.cid_dev.cpu().numpy().astype(np.int64)
+        return self._cid
 
 
 def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
@@ -172,19 +196,18 @@ def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
     if prep is None:
         prep = prepare(prob, device=dev, stream=stream)
     (pc, pn), po, size, area = prep.pins, prep.pin_off, prep.size, prep.area
-    cid, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
-                               prep=prep)
-    num = len(carea)
-    csize = np.repeat(np.sqrt(carea.astype(np.float64) / 1024).astype(np.float32)[:, None], 2, 1)
-    count = np.bincount(cid, minlength=num)
-    single = count == 1
-    member = np.zeros(num, np.int64)
-    member[cid] = np.arange(n)                         # a one-cell cluster's cell
-    csize[single] = size[member[single]]
+    cd, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
+                              prep=prep, on_device=True)
+    num = int(carea.shape[0])
+    # sizes: a merged cluster the square of its summed area, a one-cell cluster its cell's (gp103_cluster_members)
+    with torch.cuda.stream(stream):
+        cnt_c = torch.empty(max(num, 1), dtype=torch.int32, device=dev)
+        sg = torch.empty(max(num, 1), dtype=torch.uint8, device=dev)
+        csize_dev = torch.empty((max(num, 1), 2), dtype=torch.float32, device=dev)
+    native.call("gp103_cluster_members", p(cd), n, num, p(carea), p(prep.size_dev), p(cnt_c), p(sg), p(csize_dev), s)
+    csize = csize_dev[:num].cpu().numpy()
     # pins: on the device
     with torch.cuda.stream(stream):
-        cd = torch.as_tensor(cid.astype(np.int32)).to(dev)
-        sg = torch.as_tensor(single.astype(np.uint8)).to(dev)
         scratch = torch.empty(int(native.lib().gp103_coarse_pins_scratch(P_)), dtype=torch.uint8, device=dev)
         oc = torch.empty(max(P_, 1), dtype=torch.int32, device=dev)
         oo = torch.empty((max(P_, 1), 2), dtype=torch.float32, device=dev)
@@ -216,7 +239,7 @@ def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
                                    fixed_fraction, copts, arrays=False)
         pins["node_size"] = np.ascontiguousarray(cprob.node_size, np.float64)
         cprob = cprob.on_device(dev, stream, host=pins)
-    return SimpleNamespace(cid=cid, num=num, size=csize, problem=cprob, prep=prep)
+    return Clusters(cd, num, csize, sg[:num], cprob, prep)
 
 
 def device_fixed_fraction(nl, nbx, nby, device="cuda", stream=None):
@@ -251,7 +274,7 @@ def expand(cpos, coarse, prob, seed, device="cuda", stream=None):
         cpos = torch.as_tensor(cpos, dtype=torch.float32).to(dev).contiguous()
         out = torch.empty((n + cpos.shape[0] - num, 2), dtype=torch.float32, device=dev)
         out[n:] = cpos[num:]
-        cid = torch.as_tensor(coarse.cid.astype(np.int32)).to(dev)
+        cid = coarse.cid_dev if hasattr(coarse, "cid_dev") else torch.as_tensor(coarse.cid.astype(np.int32)).to(dev)
         cs = torch.as_tensor(coarse.size).to(dev)
         sz = torch.as_tensor(np.asarray(prob.node_size[:n], np.float32)).to(dev)
         rd = r.to(dev)

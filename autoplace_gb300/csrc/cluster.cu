@@ -364,10 +364,65 @@ CsrTemp csr_temp(char* base, const ClusterScratch& L) {
     return t;
 }
 
+// The clusters' members: counts per cluster (integer atomics: the same counts in any order).
+__global__ void member_count_kernel(const int* cid, int n, int* count) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&count[cid[i]], 1);
+}
+
+// Per cluster: single = one member; the size of a merged cluster is the square of its summed area (areas in 1/1024 of
+// a site area): float32(sqrt(area / 1024)) from float64, each side.
+__global__ void cluster_square_kernel(const int* count, const long long* carea, int num, unsigned char* single,
+                                      float2* csize) {
+    pdl_wait();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < num; c += gridDim.x * blockDim.x) {
+        const bool one = count[c] == 1;
+        single[c] = one ? 1 : 0;
+        if (!one) {
+            const float side = (float)__dsqrt_rn(__ddiv_rn((double)carea[c], 1024.0));
+            csize[c] = make_float2(side, side);
+        }
+    }
+}
+
+// A one-cell cluster keeps its cell's size (its only member writes it).
+__global__ void single_size_kernel(const int* cid, int n, const unsigned char* single, const float2* size,
+                                   float2* csize) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int c = cid[i];
+        if (single[c]) csize[c] = size[i];
+    }
+}
+
 }  // namespace
 }  // namespace gp103
 
 using namespace gp103;
+
+extern "C" int gp103_cluster_members(const int* cid, int n, int num, const long long* carea, const float* size,
+                                     int* count, unsigned char* single, float* csize, cudaStream_t s) {
+    if (n < 0 || num < 0 || (n > 0 && (!cid || !size)) || (num > 0 && (!carea || !count || !single || !csize)))
+        return GP103_ERR_ARG;
+    if (num == 0) return GP103_OK;
+    if (cudaMemsetAsync(count, 0, sizeof(int) * (size_t)num, s) != cudaSuccess) return GP103_ERR_CUDA;
+    if (n > 0) {
+        if (launch_k(member_count_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, cid, n, count) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
+    if (launch_k(cluster_square_kernel, dim3(grid_for(num, 256, 8)), dim3(256), 0, s, (const int*)count, carea, num,
+                 single, (float2*)csize) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (n > 0) {
+        if (launch_k(single_size_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, cid, n,
+                     (const unsigned char*)single, (const float2*)size, (float2*)csize) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    }
+    return GP103_OK;
+}
 
 extern "C" size_t gp103_cluster_scratch(int n, int num_nets, int max_edges) {
     if (n < 0 || num_nets < 0 || max_edges < 0) return 0;

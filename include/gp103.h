@@ -306,6 +306,13 @@ int gp103_cluster_round(const int* row_start, const int* col, const int* w, int 
                         int* col_out, int* w_out, int* counts, cudaStream_t stream);
 int gp103_cluster_relabel(int* cid, int n, const int* new_index, cudaStream_t stream);
 
+/* The clusters of cluster_cells' result (cid [n] in 0..num-1, carea [num] int64 in 1/1024 of a site area): count
+ * [num] (scratch, zeroed here) the members of each, single [num] = 1 for a cluster of one cell, csize [num, 2] float32
+ * = the cell's own size for a one-cell cluster, else float32(sqrt(carea / 1024)) on both sides (coarse_problem,
+ * src/cluster.py:102-107: a merged cluster is the square of its summed area). size [n, 2]: the cells' sizes. */
+int gp103_cluster_members(const int* cid, int n, int num, const long long* carea, const float* size, int* count,
+                          unsigned char* single, float* csize, cudaStream_t stream);
+
 /* The pins of the cluster problem (coarse_problem, src/cluster.py:88-130): every pin of every net (pin_cell with n
  * for a fixed pin, pin_off [num_pins, 2], pin_net sorted by net) mapped to its cluster (cid [n]; num for a fixed
  * pin); a pin on a one-cell cluster (single [num] = 1) or a fixed pin is kept with its offset, otherwise only the first
