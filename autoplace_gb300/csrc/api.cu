@@ -22,7 +22,7 @@ using namespace gp103;
 static int g_pdl = 1;
 static int g_wait_ms = 2000;
 static int g_stall = 0;
-static int g_wa_share = 0;
+static int g_wa_share = 55;
 bool gp103::pdl_enabled() { return g_pdl != 0; }
 long long gp103::tc_wait_ns() { return (long long)g_wait_ms * 1000000LL; }
 bool gp103::tc_test_stall() { return g_stall != 0; }

@@ -19,7 +19,8 @@ runs the network, and starts the clusters' level from the proposed positions wit
 wirelength-only start), the density weight in tension units as the plain start's first weight times the model's
 `lam_scale`. The plain start is the fallback, at two levels: a model is used only when its held-out validation
 placements (the plain method's exact HPWL and overflow judging them, both runs at the same stop overflow) kept the
-plain start's HPWL within 1 % (the model file's `use`, model_available); and a placement from the proposal that does
+plain start's HPWL within 1 % (the model file's `use`, model_available), and only for designs in the size range it was
+trained and validated on (`cells_min` .. `cells_max`, Proposal.applies); and a placement from the proposal that does
 not converge is placed again from the plain start (flow.Flow.run(fallback=True)).
 """
 import ctypes
@@ -35,6 +36,7 @@ from . import native
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODEL_FILE = os.path.join(HERE, "start_net.npz")
 F_IN, WIDTH, LAYERS, MAX_HOP, SWEEPS = 10, 64, 3, 12, 64
+CELLS_MIN, CELLS_MAX = 5000, 50000       # the training generator's design sizes (sample_netlist)
 ACT_NONE, ACT_RELU, ACT_SIGMOID = 0, 1, 2
 
 def lib():
@@ -261,10 +263,10 @@ def model_available(path=MODEL_FILE):
 
 
 def load_model(path=MODEL_FILE):
-    """-> dict(params={name: fp32 array}, lam_scale, meta...)."""
+    """-> dict(params={name: fp32 array}, lam_scale, cells_min, cells_max, meta...)."""
     z = np.load(path, allow_pickle=False)
     params = {k[2:]: z[k] for k in z.files if k.startswith("p_")}
-    out = {"params": params}
+    out = {"params": params, "cells_min": CELLS_MIN, "cells_max": CELLS_MAX}
     for k in z.files:
         if not k.startswith("p_"):
             out[k] = z[k].item() if z[k].shape == () else z[k]
@@ -296,6 +298,7 @@ class Proposal(object):
 
     def __init__(self, model, device="cuda"):
         self.model = model
+        self.cells = (int(model.get("cells_min", CELLS_MIN)), int(model.get("cells_max", CELLS_MAX)))
         self.dev = torch.device(device)
         self.net = Net(model["params"], device=self.dev)
         self.lam_scale = float(model.get("lam_scale", 1.0))
@@ -305,6 +308,10 @@ class Proposal(object):
         g, x = cluster_inputs(coarse, prob, self.dev, stream)
         y = Pass.for_graph(self.net, g).forward(g, x)
         return y, g
+
+    def applies(self, prob):
+        """The model is used for designs of the size range it was trained and validated on (the fallback rule)."""
+        return self.cells[0] <= prob.num_mov <= self.cells[1]
 
     def hook(self, coarse, cplacer, cpos0, prob):
         """-> (cluster + filler positions, resume dict): the clusters at the network's positions (clamped to their
@@ -505,6 +512,7 @@ def main(argv=None):
     use = best_t is not None and best_t < 1.0
     t, h, it = summary.get(best, (1.0, 1.0, 1.0))
     save_model(a.out, params, lam_scale=best, use=use, val_time_ratio=t, val_hpwl_ratio=h, val_iter_ratio=it,
+               cells_min=min(s["cells"] for s in samples), cells_max=max(s["cells"] for s in samples),
                train_samples=len(samples), epochs=a.epochs, final_loss=hist[-1], gen_seconds=t_gen,
                train_seconds=t_train)
     if a.report:

@@ -309,18 +309,21 @@ def load_peaks():
 
 
 # ------------------------------------------------------------------------------------------------ arms
-def _start_hook(args):
-    """The clusters' start of the product's configuration -> (hook for Flow.run or None, name)."""
-    want = args.start
-    if want == "plain":
-        return None, "plain (wirelength-only)"
-    try:
-        from autoplace_gb300 import learn
-    except ImportError:
-        learn = None
-    if want == "auto" and (learn is None or not learn.model_available()):
-        return None, "plain (wirelength-only)"
-    return learn.Proposal(learn.load_model()).hook, "learned (message-passing proposal of the cluster positions)"
+def _start_hook(args, prob):
+    """The clusters' start of the product's configuration -> (hook for Flow.run or None, name, the learned hook when
+    a model exists (measured beside the line even when the fallback rule keeps the plain start))."""
+    from autoplace_gb300 import learn
+    prop = learn.Proposal(learn.load_model()) if os.path.exists(learn.MODEL_FILE) else None
+    if args.start == "plain" or prop is None:
+        return None, "plain (wirelength-only)", prop
+    if args.start == "learned":
+        return prop.hook, "learned (message-passing proposal of the cluster positions)", prop
+    if not learn.model_available():
+        return None, "plain (wirelength-only; the model did not pass its validation)", prop
+    if not prop.applies(prob):
+        return None, ("plain (wirelength-only): fallback, %d cells is outside the %d-%d cells the learned start was "
+                      "trained and validated on" % (prob.num_mov, prop.cells[0], prop.cells[1])), prop
+    return prop.hook, "learned (message-passing proposal of the cluster positions)", prop
 
 
 def _timed_runs(flow, pos, steps, start=None):
@@ -348,7 +351,7 @@ def run_gb300(args):
         from autoplace_gb300 import native
         native.call("gp103_set_option", 0, 0)
     prob, pos0 = workload(args.config, seed=rank)
-    start, start_name = _start_hook(args)
+    start, start_name, prop = _start_hook(args, prob)
     flow = Flow(prob, field=args.field)
     dpos = torch.tensor(pos0, device="cuda")
     for _ in range(max(args.warmup, 0)):
@@ -385,6 +388,15 @@ def run_gb300(args):
         result["speedup_vs_plain"] = round(p_s / step_s, 3)
         result["hpwl_vs_plain"] = round(hpwl_exact / ph, 5)
         del pflow
+        if start is None and prop is not None:
+            # the learned start measured beside the line (the fallback rule kept the plain start)
+            flow.run(dpos, start=prop.hook)
+            l_s, lst, _ = _timed_runs(flow, dpos, args.plain_steps, prop.hook)
+            lh, lo = flow.fine.evaluate(lst["pos"])
+            result["learned_start"] = {"value": round(l_s, 4), "iterations": lst["iters"], "hpwl_exact": lh,
+                                       "overflow_exact": lo, "vs_this_line": round(l_s / step_s, 3),
+                                       "hpwl_vs_this_line": round(lh / hpwl_exact, 5),
+                                       "proposal_s": lst.get("phase_s", {}).get("proposal")}
         if start is not None:
             # the learned start's own share: the same tensor-core field with the plain start
             flow.run(dpos)
