@@ -169,7 +169,9 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
 }
 
 // ----------------------------------------------------------------------------- float32 CUDA-core GEMM
-// 64 x 64 output tile per block, 256 threads x (4 x 4) outputs, k-tiles of 16 staged in shared memory.
+// 64 x 64 output tile per block, 256 threads x (4 x 4) outputs, k-tiles of 16 staged in shared memory. Each k-tile's
+// 16 products are summed apart and then added to the output's running sum (two-level summation: the rounding error
+// grows with K / 16 + 16 terms instead of K).
 constexpr int SG_BM = 64, SG_BN = 64, SG_BK = 16;
 
 __global__ void __launch_bounds__(256) sgemm_kernel(SGemm g) {
@@ -187,6 +189,7 @@ __global__ void __launch_bounds__(256) sgemm_kernel(SGemm g) {
             Bs[kk][r] = (n < g.N && k < g.K) ? g.B[(size_t)n * g.K + k] : 0.f;
         }
         __syncthreads();
+        float part[4][4] = {};
 #pragma unroll
         for (int kk = 0; kk < SG_BK; kk++) {
             float a[4], b[4];
@@ -195,8 +198,12 @@ __global__ void __launch_bounds__(256) sgemm_kernel(SGemm g) {
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
-                for (int jj = 0; jj < 4; jj++) acc[i][jj] = fmaf(a[i], b[jj], acc[i][jj]);
+                for (int jj = 0; jj < 4; jj++) part[i][jj] = fmaf(a[i], b[jj], part[i][jj]);
         }
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) acc[i][jj] += part[i][jj];
         __syncthreads();
     }
 #pragma unroll

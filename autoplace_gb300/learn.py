@@ -31,7 +31,7 @@ import time
 import numpy as np
 import torch
 
-from . import native
+from . import native, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODEL_FILE = os.path.join(HERE, "start_net.npz")
@@ -285,7 +285,7 @@ def cluster_inputs(coarse, prob, device="cuda", stream=None):
     stream = stream or torch.cuda.current_stream(torch.device(device))
     g = Graph(cp.csr, K, device=device, stream=stream)
     with torch.cuda.stream(stream):
-        area = torch.as_tensor(np.asarray(cp.node_size[:K], np.float64).prod(1).astype(np.float32)).to(device)
+        area = torch.as_tensor(synth.areas(cp.node_size[:K]).astype(np.float32)).to(device)
         cell_pins = np.asarray(prob.nl.cell_pins, np.float64)
         pin_count = torch.as_tensor(np.bincount(coarse.cid, weights=cell_pins, minlength=K).astype(np.float32)).to(
             device)

@@ -22,6 +22,13 @@ import numpy as np
 ROW_HEIGHT = 10.0
 
 
+def areas(size):
+    """[n, 2] sizes -> [n] float64 areas, the same values as size.prod(1) (one product per row), without numpy's slow
+    reduction over a two-element axis."""
+    a = np.asarray(size, np.float64)
+    return a[:, 0] * a[:, 1]
+
+
 @dataclass
 class Netlist:
     name: str
@@ -46,7 +53,7 @@ class Netlist:
 
     @property
     def mov_area(self):
-        return float(self.size.prod(1).sum())
+        return float(areas(self.size).sum())
 
     @property
     def cell_pins(self):
@@ -117,7 +124,7 @@ def _place_macros(rng, count, cover, side, row_height):
     if count == 0 or cover <= 0:
         return np.zeros((0, 4))
     dims = rng.uniform(0.05, 0.15, (count, 2)) * side
-    dims *= math.sqrt(cover * side * side / float(dims.prod(1).sum()))
+    dims *= math.sqrt(cover * side * side / float(areas(dims).sum()))
     dims[:, 1] = np.maximum(np.round(dims[:, 1] / row_height), 1) * row_height
     dims[:, 0] = np.maximum(np.round(dims[:, 0]), 1)
     placed = []
@@ -138,7 +145,7 @@ def make_netlist(cells, nets, window=200, macros=0, cover=0.0, util=0.7, fixed_p
                  name=None, **_ignored):
     rng = np.random.default_rng(seed)
     size = np.stack([rng.integers(1, 9, cells).astype(np.float64), np.full(cells, ROW_HEIGHT)], 1)
-    mov_area = float(size.prod(1).sum())
+    mov_area = float(areas(size).sum())
     region = mov_area / util / (1.0 - cover)
     side = math.ceil(math.sqrt(region) / ROW_HEIGHT) * ROW_HEIGHT
     mac = _place_macros(rng, macros, cover, side, ROW_HEIGHT)
