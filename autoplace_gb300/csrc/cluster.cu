@@ -24,6 +24,8 @@ struct CsrTemp {
     int* tmp_w;    // [max entries]
     int* tile;     // [SCAN_MAX_TILES]
     int* total;    // [4]
+    int* long_rows;  // [rows]: the rows merged by a warp each
+    int* nlong;      // [1]: their number
 };
 
 // (entries beyond cap were never written, rows out of range never produced: both guarded all the same)
@@ -46,42 +48,140 @@ __global__ void __launch_bounds__(256) coo_place_kernel(const int* ci, const int
     }
 }
 
-// a row's entries sorted by column (insertion sort: rows hold a few dozen entries), equal columns merged to the front
-__global__ void __launch_bounds__(256) row_merge_kernel(const int* start, int rows, int* tj, int* tw, int* merged) {
+// A warp's appends to one list: lane l appends k_l entries; -> the position of the lane's first one (one atomic per
+// warp; every lane of the warp must call it). The order of the entries in the list is arbitrary either way: the
+// CSR build sorts each row and sums the weights of equal columns (integers).
+__device__ __forceinline__ int warp_append(int* m, int k) {
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(m, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - k;
+}
+
+// A row's entries sorted by column, equal columns merged (weights summed) to the front of the row. Rows of up to
+// ROW_SHORT entries: a thread per row (insertion sort); longer ones: a warp per row (bitonic sort of (column, weight)
+// keys in shared memory, then the runs of equal columns summed); beyond ROW_WARP_MAX entries (rare): lane 0 by
+// insertion sort. Integer sums in any order: every form gives the same row.
+__device__ int serial_merge_row(int b, int e, int* tj, int* tw) {
+    for (int k = b + 1; k < e; k++) {
+        const int j = tj[k], w = tw[k];
+        int q = k - 1;
+        while (q >= b && tj[q] > j) {
+            tj[q + 1] = tj[q];
+            tw[q + 1] = tw[q];
+            q--;
+        }
+        tj[q + 1] = j;
+        tw[q + 1] = w;
+    }
+    int out = b;
+    for (int k = b; k < e; k++) {
+        if (out > b && tj[out - 1] == tj[k]) {
+            tw[out - 1] += tw[k];
+        } else {
+            tj[out] = tj[k];
+            tw[out] = tw[k];
+            out++;
+        }
+    }
+    return out - b;
+}
+
+__device__ __forceinline__ int warp_id_global() { return (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); }
+__device__ __forceinline__ int warps_in_grid() { return (int)(((size_t)gridDim.x * blockDim.x) >> 5); }
+
+// Rows of up to ROW_SHORT entries: a thread per row; longer ones go to a list (warp-aggregated appends) for
+// row_merge_long_kernel.
+constexpr int ROW_SHORT = 32;
+
+__global__ void __launch_bounds__(256) row_merge_kernel(const int* start, int rows, int* tj, int* tw, int* merged,
+                                                        int* long_rows, int* nlong) {
     pdl_wait();
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-        const int b = start[r], e = start[r + 1];
-        for (int k = b + 1; k < e; k++) {
-            const int j = tj[k], w = tw[k];
-            int q = k - 1;
-            while (q >= b && tj[q] > j) {
-                tj[q + 1] = tj[q];
-                tw[q + 1] = tw[q];
-                q--;
-            }
-            tj[q + 1] = j;
-            tw[q + 1] = w;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < rows; base += stride) {          // warp-uniform trip count
+        const int r = base + threadIdx.x;
+        bool is_long = false;
+        if (r < rows) {
+            const int b = start[r], e = start[r + 1];
+            if (e - b <= ROW_SHORT) merged[r] = serial_merge_row(b, e, tj, tw);
+            else is_long = true;
         }
-        int out = b;
-        for (int k = b; k < e; k++) {
-            if (out > b && tj[out - 1] == tj[k]) {
-                tw[out - 1] += tw[k];
-            } else {
-                tj[out] = tj[k];
-                tw[out] = tw[k];
-                out++;
-            }
-        }
-        merged[r] = out - b;
+        const int at = warp_append(nlong, is_long ? 1 : 0);
+        if (is_long) long_rows[at] = r;
     }
 }
 
+// the listed long rows, a warp per row: keys (column << 32 | weight) sorted ascending, padded to a power of two
+constexpr int ROW_WARP_MAX = 512;
+
+__global__ void __launch_bounds__(256) row_merge_long_kernel(const int* start, const int* long_rows, const int* nlong,
+                                                             int* tj, int* tw, int* merged) {
+    pdl_wait();
+    __shared__ unsigned long long keys[8][ROW_WARP_MAX];
+    const int lane = threadIdx.x & 31, count = *nlong;
+    unsigned long long* sk = keys[threadIdx.x >> 5];
+    for (int q = warp_id_global(); q < count; q += warps_in_grid()) {
+        const int r = long_rows[q];
+        const int b = start[r], k = start[r + 1] - b;
+        int m = 0;
+        if (k > ROW_WARP_MAX) {
+            if (lane == 0) m = serial_merge_row(b, b + k, tj, tw);
+            m = __shfl_sync(0xffffffffu, m, 0);
+        } else {
+            int n = 64;
+            while (n < k) n <<= 1;
+            for (int i = lane; i < n; i += 32)
+                sk[i] = i < k ? ((unsigned long long)(unsigned)tj[b + i] << 32) | (unsigned)tw[b + i] : ~0ull;
+            __syncwarp();
+            for (int size = 2; size <= n; size <<= 1)
+                for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (int t = lane; t < n / 2; t += 32) {
+                        const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+                        const unsigned long long x = sk[i], y = sk[j];
+                        if ((x > y) == ((i & size) == 0)) {
+                            sk[i] = y;
+                            sk[j] = x;
+                        }
+                    }
+                    __syncwarp();
+                }
+            // runs of equal columns: each run's first entry writes the run's sum at its rank among the runs
+            for (int c = 0; c < k; c += 32) {
+                const int i = c + lane;
+                const unsigned col = i < k ? (unsigned)(sk[i] >> 32) : 0u;
+                const bool first = i < k && (i == 0 || (unsigned)(sk[i - 1] >> 32) != col);
+                const unsigned fb = __ballot_sync(0xffffffffu, first);
+                if (first) {
+                    int sum = 0;
+                    for (int j = i; j < k && (unsigned)(sk[j] >> 32) == col; j++) sum += (int)(unsigned)sk[j];
+                    const int at = m + __popc(fb & ((1u << lane) - 1u));
+                    tj[b + at] = (int)col;
+                    tw[b + at] = sum;
+                }
+                m += __popc(fb);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) merged[r] = m;
+    }
+}
+
+// the merged front of every row to its place in the CSR, one warp per row (coalesced copies)
 __global__ void __launch_bounds__(256) row_compact_kernel(const int* start, const int* row_start, int rows,
                                                           const int* tj, const int* tw, int* col, int* w) {
     pdl_wait();
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int r = warp_id_global(); r < rows; r += warps_in_grid()) {
         const int b = start[r], o = row_start[r], k = row_start[r + 1] - o;
-        for (int t = 0; t < k; t++) {
+        for (int t = lane; t < k; t += 32) {
             col[o + t] = tj[b + t];
             w[o + t] = tw[b + t];
         }
@@ -92,7 +192,7 @@ __global__ void __launch_bounds__(256) row_compact_kernel(const int* start, cons
 int coo_to_csr(const int* ci, const int* cj, const int* cw, const int* num, int cap, int rows, const CsrTemp& t,
                int* row_start, int* col, int* w, int* nnz, cudaStream_t s) {
     if (cudaMemsetAsync(t.count, 0, sizeof(int) * (size_t)(rows + 1), s) != cudaSuccess) return GP103_ERR_CUDA;
-    const int ge = grid_for(cap > 0 ? cap : 1, 256, 8), gr = grid_for(rows > 0 ? rows : 1, 256, 8);
+    const int ge = grid_for(cap > 0 ? cap : 1, 256, 8);
     if (launch_k(coo_count_kernel, dim3(ge), dim3(256), 0, s, ci, num, cap, rows, t.count) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
@@ -106,14 +206,20 @@ int coo_to_csr(const int* ci, const int* cj, const int* cw, const int* num, int 
                  t.tmp_w) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
-    // t.merged = row starts; merged counts go to t.count
-    if (launch_k(row_merge_kernel, dim3(gr), dim3(256), 0, s, (const int*)t.merged, rows, t.tmp_j, t.tmp_w, t.count) !=
-        cudaSuccess)
+    // t.merged = row starts; merged counts go to t.count (short rows by a thread each, long ones by a warp each)
+    const int gr = grid_for(rows > 0 ? rows : 1, 256, 8), gw = grid_for(rows > 0 ? 32LL * rows : 1, 256, 8);
+    if (cudaMemsetAsync(t.nlong, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
+    if (launch_k(row_merge_kernel, dim3(gr), dim3(256), 0, s, (const int*)t.merged, rows, t.tmp_j, t.tmp_w, t.count,
+                 t.long_rows, t.nlong) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    if (launch_k(row_merge_long_kernel, dim3(gw), dim3(256), 0, s, (const int*)t.merged, (const int*)t.long_rows,
+                 (const int*)t.nlong, t.tmp_j, t.tmp_w, t.count) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     if (cudaMemsetAsync(t.count + rows, 0, sizeof(int), s) != cudaSuccess) return GP103_ERR_CUDA;
     if ((st = exclusive_scan(t.count, rows + 1, row_start, t.tile, nnz, s))) return st;
-    if (launch_k(row_compact_kernel, dim3(gr), dim3(256), 0, s, (const int*)t.merged, (const int*)row_start, rows,
+    if (launch_k(row_compact_kernel, dim3(gw), dim3(256), 0, s, (const int*)t.merged, (const int*)row_start, rows,
                  (const int*)t.tmp_j, (const int*)t.tmp_w, col, w) != cudaSuccess)
         return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
@@ -130,33 +236,56 @@ __global__ void __launch_bounds__(256) net_degree_count_kernel(const int* pin_ne
     }
 }
 
-// pins k apart in the pin list (k < max_degree) of one net of at most max_degree pins: both ordered pairs
+// pins k apart in the pin list (k < max_degree) of one net of at most max_degree pins: both ordered pairs (a thread per
+// pin counts its pairs, then the warp appends them with one atomic)
+__device__ __forceinline__ bool pair_ok(const int* pin_cell, const int* pin_net, int num_pins, int n, int p, int k,
+                                        int net, int a, int& b) {
+    if (p + k >= num_pins || pin_net[p + k] != net) return false;
+    b = pin_cell[p + k];
+    return !(a < 0 || b < 0 || a >= n || b >= n || a == b);
+}
+
 __global__ void __launch_bounds__(256) pair_emit_kernel(const int* pin_cell, const int* pin_net, int num_pins,
                                                         int num_nets, int n, int max_degree, const int* deg, int cap,
                                                         int* num, int* ci, int* cj, int* cw) {
     pdl_wait();
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < num_pins; p += gridDim.x * blockDim.x) {
-        const int net = pin_net[p];
-        if ((unsigned)net >= (unsigned)num_nets) continue;
-        const int d = deg[net];
-        if (d > max_degree || d < 2) continue;
-        const int a = pin_cell[p];
-        for (int k = 1; k < max_degree && p + k < num_pins; k++) {
-            if (pin_net[p + k] != net) break;
-            const int b = pin_cell[p + k];
-            if (a < 0 || b < 0 || a >= n || b >= n || a == b) continue;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < num_pins; base += stride) {     // warp-uniform trip count
+        const int p = base + threadIdx.x;
+        int net = -1, d = 0, a = -1, cnt = 0;
+        if (p < num_pins) {
+            net = pin_net[p];
+            if ((unsigned)net < (unsigned)num_nets) {
+                d = deg[net];
+                a = pin_cell[p];
+            }
+        }
+        const bool live = d >= 2 && d <= max_degree;
+        if (live)
+            for (int k = 1; k < max_degree; k++) {
+                int b;
+                if (p + k >= num_pins || pin_net[p + k] != net) break;
+                if (pair_ok(pin_cell, pin_net, num_pins, n, p, k, net, a, b)) cnt++;
+            }
+        int at = warp_append(num, 2 * cnt);
+        if (live) {
             const int wgt = 420 / (d - 1);
-            const int at = atomicAdd(num, 2);
-            if (at + 1 < cap) {
-                ci[at] = a; cj[at] = b; cw[at] = wgt;
-                ci[at + 1] = b; cj[at + 1] = a; cw[at + 1] = wgt;
+            for (int k = 1; k < max_degree; k++) {
+                int b;
+                if (p + k >= num_pins || pin_net[p + k] != net) break;
+                if (!pair_ok(pin_cell, pin_net, num_pins, n, p, k, net, a, b)) continue;
+                if (at + 1 < cap) {
+                    ci[at] = a; cj[at] = b; cw[at] = wgt;
+                    ci[at + 1] = b; cj[at + 1] = a; cw[at + 1] = wgt;
+                }
+                at += 2;
             }
         }
     }
 }
 
 // ---------------------------------------------------------------------------------------------- a round
-// per non-head cluster: the head of the largest score, the first one (lowest column) on ties
+// per non-head cluster: the head of the largest score, the first one (first edge of the row) on ties
 __global__ void __launch_bounds__(256) best_head_kernel(const int* row_start, const int* col, const int* w, int num,
                                                         const long long* area, const unsigned char* head,
                                                         long long cap, long long big, int* best_to, double* best) {
@@ -242,22 +371,32 @@ __global__ void __launch_bounds__(256) renumber_kernel(const int* parent, const 
     }
 }
 
-// the edges between the new clusters (a cluster's own edges dropped), as entries for coo_to_csr
+// the edges between the new clusters (a cluster's own edges dropped), as entries for coo_to_csr (a thread per old
+// cluster counts its kept edges, then the warp appends them with one atomic)
 __global__ void __launch_bounds__(256) edge_relabel_kernel(const int* row_start, const int* col, const int* w, int num,
                                                            const int* new_index, int cap, int* m, int* ci, int* cj,
                                                            int* cw) {
     pdl_wait();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num; i += gridDim.x * blockDim.x) {
-        const int a = new_index[i];
-        for (int e = row_start[i]; e < row_start[i + 1]; e++) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x; base < num; base += stride) {           // warp-uniform trip count
+        const int i = base + threadIdx.x;
+        int a = -1, b0 = 0, b1 = 0, cnt = 0;
+        if (i < num) {
+            a = new_index[i];
+            b0 = row_start[i];
+            b1 = row_start[i + 1];
+            for (int e = b0; e < b1; e++) cnt += new_index[col[e]] != a;
+        }
+        int at = warp_append(m, cnt);
+        for (int e = b0; e < b1; e++) {
             const int b = new_index[col[e]];
             if (a == b) continue;
-            const int at = atomicAdd(m, 1);
             if (at < cap) {
                 ci[at] = a;
                 cj[at] = b;
                 cw[at] = w[e];
             }
+            at++;
         }
     }
 }
@@ -361,6 +500,9 @@ CsrTemp csr_temp(char* base, const ClusterScratch& L) {
     t.tmp_w = (int*)(base + L.tmp_w);
     t.tile = (int*)(base + L.tile);
     t.total = (int*)(base + L.total) + 4;
+    // (the candidate list of a round is consumed before the round's CSR build)
+    t.long_rows = (int*)(base + L.list);
+    t.nlong = (int*)(base + L.total) + 2;
     return t;
 }
 

@@ -187,6 +187,33 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Two 32-column loads in flight before one wait (columns taddr .. + 31 into v, taddr + 32 .. + 63 into u).
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[32], float (&u)[32]) {
+    uint32_t r[32], q[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]), "=r"(q[5]), "=r"(q[6]), "=r"(q[7]),
+          "=r"(q[8]), "=r"(q[9]), "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]), "=r"(q[15]),
+          "=r"(q[16]), "=r"(q[17]), "=r"(q[18]), "=r"(q[19]), "=r"(q[20]), "=r"(q[21]), "=r"(q[22]), "=r"(q[23]),
+          "=r"(q[24]), "=r"(q[25]), "=r"(q[26]), "=r"(q[27]), "=r"(q[28]), "=r"(q[29]), "=r"(q[30]), "=r"(q[31])
+        : "r"(taddr + 32u));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) {
+        v[i] = __uint_as_float(r[i]);
+        u[i] = __uint_as_float(q[i]);
+    }
+}
+
 // 1 / t for the field weights (t > 0 normal): the hardware approximation refined by one Newton-Raphson step,
 // r' = r + r (1 - t r), within an ulp of the rounded reciprocal (the weights need float32 accuracy, not rounding).
 __device__ __forceinline__ float recip(float t) {
@@ -229,9 +256,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     constexpr bool F16 = MODE == 2;
     constexpr int B_TILE = BN * TC_BK * 2;
     constexpr int NA = X6 ? 3 : 2, NB = NA, NPROD = X6 ? 6 : 3;
-    // BN = 64: the products are grouped by B term into NBLK column blocks of the accumulator (block j = the
-    // products with b_j), so that one MMA can cover several B terms at once (below); BN = 128: one block
-    constexpr bool CONCAT = BN == 64;
+    // bf16 modes, BN = 64: the products are grouped by B term into NBLK column blocks of the accumulator (block j =
+    // the products with b_j), so that one MMA can cover several B terms at once (below). f16x3 and BN = 128: one
+    // block, every product into it (the same tensor time: an MMA's time goes with its N; the readers load one block
+    // per k-block instead of NB)
+    constexpr bool CONCAT = BN == 64 && !F16;
     constexpr int NBLK = CONCAT ? NB : 1;
     constexpr uint32_t ACC_COLS = (uint32_t)(NBLK * BN);         // per accumulator buffer (two buffers)
     constexpr uint32_t TMEM_COLS = 2 * ACC_COLS <= 128 ? 128 : 2 * ACC_COLS <= 256 ? 256 : 512;
@@ -412,10 +441,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (!mbar_wait(accf_bar(b), (uint32_t)(it >> 1) & 1u, err, 4, limit)) { ok = false; break; }
             tc_fence_after();
             const uint32_t base = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)b * ACC_COLS;
+            // f16x3, 64 columns: both halves of the block in flight before one wait
+            constexpr bool PAIR = F16 && BN == 64 && NBLK == 1;
+            float v2[PAIR ? 32 : 1];
 #pragma unroll
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
-                tmem_ld32(base + (uint32_t)c0, v);
+                if constexpr (PAIR) {
+                    if (c0 == 0) tmem_ld64(base, v, v2);
+                    else {
+#pragma unroll
+                        for (int i = 0; i < 32; i++) v[i] = v2[i];
+                    }
+                } else {
+                    tmem_ld32(base + (uint32_t)c0, v);
+                }
                 if constexpr (NBLK > 1) {                        // blocks of the smaller products: add them first
                     float w[32];
                     tmem_ld32(base + (uint32_t)((NBLK - 1) * BN + c0), w);

@@ -175,7 +175,14 @@ class Placer(object):
                     prob.num_mov, self._p(scratch), scratch.numel(), self._p(self.net_start), self._p(self.pin_cell),
                     self._p(self.pin_off), self._p(self.pin_slot), self._p(split), self.stream.cuda_stream)
         pl.pin_cell, pl.pin_off, pl.net_start = self._p(self.pin_cell), self._p(self.pin_off), self._p(self.net_start)
-        pl.cell_start, pl.pin_slot = self._p(self.cell_start), self._p(self.pin_slot)
+        # the pin gradients stay in net order (the WA kernels' stores are contiguous); the gather reads each cell's
+        # pins, in cell_pin order, through cell_pin_net = the inverse of pin_slot (the same sums, bit for bit; on the
+        # 1.2M-cell pass 0.284 ms against 0.288 ms with the gradients stored in cell order)
+        with torch.cuda.stream(self.stream):
+            self.cell_pin_net = self._hold(torch.empty(max(P, 1), dtype=torch.int32, device=dev))
+            if P:
+                self.cell_pin_net[self.pin_slot[:P].long()] = torch.arange(P, dtype=torch.int32, device=dev)
+        pl.cell_start, pl.cell_pin, pl.pin_slot = self._p(self.cell_start), self._p(self.cell_pin_net), None
         # (the stream-ordered allocator may hand these blocks to the allocations below: their kernels run after
         # gp103_net_order on the same stream; the split counts are read back at the end, after the other set-up)
         del ns_in, cell_in, off_in, cp_in, scratch

@@ -3,7 +3,7 @@ the region, target density 0.9, force grid 512 x 512): one level of the cells in
 16th density pass against float64 (oracle/precision.py) beside the reference's float32 FFT formula on the same map,
 and the final HPWL / overflow of each mode. Bars (of the float64 field's largest value, at every checked pass):
 bf16x6 1e-6, f16x3 1.5e-6, bf16x3 3e-5, fp32 (CUDA cores, float32 sums of 16 products added to a running sum)
-3e-6 -- the reference's own float32 FFT formula measures up to 2e-6 on the same maps; every mode converges, its HPWL
+1e-6 -- the reference's own float32 FFT formula measures up to 2e-6 on the same maps; every mode converges, its HPWL
 within 0.5 % of bf16x6's."""
 import json
 
@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 # f16x3's two float16 terms are exact to 2^-22 of their 64-wide chunk's largest value, bf16x6's three bf16 terms to
 # 2^-24 of each value: bf16x6 holds the 1e-6 bar at every pass, f16x3 (the faster default) 1.5e-6
-MODES = [("f16x3", 1.5e-6), ("bf16x6", 1e-6), ("bf16x3", 3e-5), ("fp32", 3e-6)]
+MODES = [("f16x3", 1.5e-6), ("bf16x6", 1e-6), ("bf16x3", 3e-5), ("fp32", 1e-6)]
 
 
 @pytest.fixture(scope="module")
