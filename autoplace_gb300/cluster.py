@@ -4,7 +4,8 @@ Mirrors cluster_cells (src/cluster.py:38-85) call for call: the pair edges of th
 `max_rounds` rounds, each with half of the clusters drawn as heads from a seeded CPU generator (torch.rand of
 torch.Generator().manual_seed(seed), as the reference draws them), until the clusters are few enough or a round
 merges nothing. The edge building and every round run in libgp103 (gp103_cluster_edges / _round / _relabel); the
-host draws the heads and reads two counts per round. Integer weights and areas and fixed tie rules make the result
+generator's stream is drawn once per design and copied to the device, where each round compares its share with 0.5;
+the host reads two counts per round. Integer weights and areas and fixed tie rules make the result
 the reference's, bit for bit.
 """
 import ctypes
@@ -39,8 +40,8 @@ def limits(area, ratio):
 class Stream(object):
     """The seeded CPU generator's float32 draws as one stream (torch.rand of torch.Generator().manual_seed(seed)):
     consecutive torch.rand calls on a generator give the consecutive pieces of one long draw, so the stream is drawn
-    ahead in blocks, and a reader's rounds take the next `num` values each -- the numbers the reference's calls give.
-    Every placement with this seed reads the same stream from its start (reader()); the drawn part is kept."""
+    ahead in blocks, and a placement's rounds take the next `num` values each -- the numbers the reference's calls
+    give. Every placement with this seed reads the same stream from its start; the drawn part is kept."""
 
     def __init__(self, seed, block):
         self.gen = torch.Generator().manual_seed(int(seed))
@@ -53,42 +54,44 @@ class Stream(object):
             self.buf = np.concatenate([self.buf, torch.rand(more, generator=self.gen).numpy()])
         return self.buf
 
-    def reader(self):
-        stream, at = self, [0]
 
-        class Reader(object):
-            def take(self, num):
-                buf = stream.upto(at[0] + num)
-                out = buf[at[0]:at[0] + num]
-                at[0] += num
-                return out
-        return Reader()
+def device_pair_bound(pin_net, num_nets, max_degree=8):
+    """pair_bound of the pins' nets already on the device (int32 [P]), one host read."""
+    deg = torch.bincount(pin_net.long(), minlength=max(int(num_nets), 1))
+    d = deg[(deg >= 2) & (deg <= max_degree)]
+    return int((d * (d - 1)).sum())
 
 
 def prepare(prob, device="cuda", stream=None, max_degree=8):
     """What a placement's clustering needs of its design, made once per design (like the cells' own uploads): the
-    pins on the device (int32 cells and nets, float32 offsets), the cells' areas and the merge limits, the pair
-    bound, the heads' seeded stream drawn ahead (four draws per cell) and expand's seeded draws. -> SimpleNamespace."""
+    pins on the device (int32 cells and nets, float32 offsets: the device problem's own, else uploaded), the cells'
+    areas and the merge limits, the pair bound, the heads' seeded stream drawn ahead (four draws per cell) and
+    expand's seeded draws. -> SimpleNamespace."""
     nl, o, n = prob.nl, prob.opts, prob.num_mov
     dev = torch.device(device)
     stream = stream or torch.cuda.current_stream(dev)
     with torch.cuda.stream(stream):
-        pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev, non_blocking=True)
-        pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
-        po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
+        if torch.is_tensor(getattr(prob, "all_net", None)) and prob.all_net.is_cuda:
+            pc, pn, po = prob.all_cell, prob.all_net, prob.all_off
+        else:
+            pc = torch.as_tensor(np.asarray(nl.pin_cell, np.int32)).to(dev, non_blocking=True)
+            pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
+            po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
+        bound = device_pair_bound(pn, nl.num_nets, max_degree)
     size = np.asarray(prob.node_size[:n], np.float32)
     area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
-    heads = Stream(o.seed, 4 * n)
+    heads = Stream(o.seed, n)                  # (extended n draws at a time when the rounds need more)
     heads.upto(4 * n)
     gen = torch.Generator().manual_seed(int(o.seed))
     with torch.cuda.stream(stream):
         area_dev = torch.as_tensor(area).to(dev, non_blocking=True)
         size_dev = torch.as_tensor(size).to(dev, non_blocking=True)
         draws_dev = torch.rand(n, 2, generator=gen).to(dev, non_blocking=True)
+        heads_dev = torch.as_tensor(heads.buf[:4 * n]).to(dev, non_blocking=True)
     return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, area_dev=area_dev, size_dev=size_dev,
-                           limits=limits(area, o.cluster_ratio), pair_bound=max(pair_bound(nl.pin_net, max_degree), 1),
-                           num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, expand_draws=draws_dev,
-                           size=size)
+                           limits=limits(area, o.cluster_ratio), pair_bound=max(bound, 1),
+                           num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, heads_dev=heads_dev,
+                           expand_draws=draws_dev, size=size)
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
@@ -135,15 +138,26 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     stream.synchronize()
     if int(counts[1]) > E:
         raise RuntimeError("pair bound too small: %d > %d" % (int(counts[1]), E))
-    heads = (prep.heads if prep is not None else Stream(seed, n)).reader()
-    num, a = n, 0
+    heads = prep.heads if prep is not None else Stream(seed, n)
+    drawn = prep.heads_dev if prep is not None and draws is None else None   # the stream's start, on the device
+    num, a, at = n, 0, 0
     for r in range(max_rounds):
         if num * ratio <= n:
             break
-        d = draws(r, num) if draws is not None else heads.take(num)
-        head = torch.as_tensor(np.asarray(d) < np.float32(0.5)).to(torch.uint8)
-        with torch.cuda.stream(stream):
-            head = head.to(dev)
+        if drawn is not None and at + num > drawn.numel():          # the stream's next part, on the device once
+            buf = heads.upto(at + num)
+            with torch.cuda.stream(stream):
+                drawn = torch.cat([drawn, torch.as_tensor(buf[drawn.numel():]).to(dev)])
+            prep.heads_dev = drawn
+        if drawn is not None:
+            with torch.cuda.stream(stream):
+                head = (drawn[at:at + num] < 0.5).to(torch.uint8)
+        else:
+            d = draws(r, num) if draws is not None else heads.upto(at + num)[at:at + num]
+            head = torch.as_tensor(np.asarray(d) < np.float32(0.5)).to(torch.uint8)
+            with torch.cuda.stream(stream):
+                head = head.to(dev)
+        at += num
         b = 1 - a
         native.call("gp103_cluster_round", p(rows[a]), p(col[a]), p(wgt[a]), num, E, p(areas[a]), p(head),
                     cap, big, per_head, p(scratch), scratch.numel(), p(new_index), p(areas[b]), p(rows[b]), p(col[b]),

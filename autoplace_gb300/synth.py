@@ -53,7 +53,11 @@ class Netlist:
 
     @property
     def mov_area(self):
-        return float(areas(self.size).sum())
+        key = (id(self.size), self.size.shape)          # (computed once per size array)
+        if self.__dict__.get("_mov_area_key") != key:
+            self.__dict__["_mov_area_key"] = key
+            self.__dict__["_mov_area"] = float(areas(self.size).sum())
+        return self.__dict__["_mov_area"]
 
     @property
     def cell_pins(self):

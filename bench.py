@@ -407,8 +407,8 @@ def run_gb300(args):
             result["speedup_vs_tc_plain_start"] = round(t_s / step_s, 3)
 
     # e2e: from the netlist's pinned host arrays through the public API: upload, the problem's arrays built on the
-    # device (net CSR, cell order, smoothed nodes), the cells' Placer and the flow, the run (the clusters' pins are
-    # uploaded again by the clustering), the download of the placement. The host part of the problem (grids, fixed
+    # device (net CSR, cell order, smoothed nodes), the cells' Placer and the flow (the clustering reads the problem's
+    # pins on the device), the run, the download of the placement. The host part of the problem (grids, fixed
     # fractions, fillers: the reader's and initializer's work) is made once, before.
     from autoplace_gb300.problem import Problem, netlist_arrays
     base = Problem(prob.nl, prob.opts, arrays=False)
@@ -421,8 +421,6 @@ def run_gb300(args):
     out = torch.empty(host_pos.shape, dtype=torch.float32).pin_memory()
     h2d = sum(x.numel() * x.element_size() for x in list(host.values()) + list(maps.values())) + \
         host_pos.numel() * 4 + len(prob.constants()) * 8
-    if prob.opts.cluster_ratio > 1:
-        h2d += 16 * prob.nl.num_pins                     # the clustering's pin upload (cell, net, offset)
     d2h = out.numel() * 4
     # one untimed step first: it loads the device-build kernels, which only this path uses (a one-time cost per
     # process, like the warm-up placements of the device-timed loop)

@@ -365,8 +365,8 @@ int gp103_macro_fraction(const double* rects, int count, double width, double he
                          double* fraction, cudaStream_t stream);
 
 /* ------------------------------------------------------------------------------------------------ part 3
- * Exact evaluators in float64 (the judges of a run). `scratch` is GP103_EVAL_SCRATCH_BYTES of device memory;
- * *out is written by the device (read it after synchronising the stream). */
+ * Exact evaluators in float64 (the exact HPWL and overflow of a placement). `scratch` is GP103_EVAL_SCRATCH_BYTES of
+ * device memory; *out is written by the device (read it after synchronising the stream). */
 #define GP103_EVAL_SCRATCH_BYTES 16640
 
 /* HPWL over every net (Wirelength.hpwl, src/core/wa_wirelength_hpwl.py:66-70): pin position pos[pin_cell] +
