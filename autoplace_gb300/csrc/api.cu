@@ -23,7 +23,9 @@ static int g_pdl = 1;
 static int g_wait_ms = 2000;
 static int g_stall = 0;
 static int g_wa_share = 55;
+static int g_field_early = 3;
 bool gp103::pdl_enabled() { return g_pdl != 0; }
+int gp103::field_early() { return g_field_early; }
 long long gp103::tc_wait_ns() { return (long long)g_wait_ms * 1000000LL; }
 bool gp103::tc_test_stall() { return g_stall != 0; }
 int gp103::wa_long_share() { return g_wa_share; }
@@ -39,6 +41,10 @@ extern "C" int gp103_set_option(int option, int value) {
         case GP103_OPT_WA_FUSED:
             REQUIRE(value >= 0 && value <= 99);
             g_wa_share = value;
+            return GP103_OK;
+        case GP103_OPT_FIELD_EARLY:
+            REQUIRE(value >= 0 && value <= 3);
+            g_field_early = value;
             return GP103_OK;
         default: return GP103_ERR_ARG;
     }

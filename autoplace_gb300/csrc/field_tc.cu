@@ -58,6 +58,8 @@ struct TcArgs {
     int* err;
     long long wait_ns;           // limit of one wait (GP103_OPT_WAIT_MS)
     int stall;                   // GP103_OPT_TEST_STALL_FIELD: the producer issues no load (every wait runs out)
+    int early;                   // bit 0: A of the first stages loaded before the dependency wait; bit 1: the next
+                                 // kernel may launch once this block's accumulation is done
 };
 
 // The products of a mode, smallest first: bf16x6 (X6 = 1) has 3 terms per operand and 6 products, bf16x3 2 and 3.
@@ -315,6 +317,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // The A operand of every GEMM of the field is one of its constant matrices, written by the field's set-up and
+    // followed there by kernels that each wait for their predecessor: no kernel still running when this one starts
+    // writes it. So the A tiles of the first stages are requested before the wait for the previous kernel (whose
+    // outputs B is), and their latency overlaps that kernel's tail.
+    const int pre = (args.early & 1) && !args.stall ? (total < stages ? total : stages) : 0;
+    if (warp == 0 && lane == 0) {
+        for (int it = 0; it < pre; it++) {                       // stage it, first use: no wait for a free stage
+            mbar_expect_tx(full_bar(it), stage_bytes);
+#pragma unroll
+            for (int t = 0; t < NA; t++)
+                tma_load_3d(smem_u32(smem + it * stage_bytes + t * TC_A_TILE), ma, full_bar(it), it * TC_BK, m0, t);
+        }
+    }
     pdl_wait();
 
     if (warp == 0) {
@@ -323,12 +338,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int it = 0; it < total && !args.stall; it++) {
                 const int s = it % stages;
                 const uint32_t ph = (uint32_t)(it / stages) & 1u;
-                if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1, limit)) break;
-                mbar_expect_tx(full_bar(s), stage_bytes);
                 uint8_t* st = smem + s * stage_bytes;
+                if (it >= pre) {                                 // (the first `pre` stages have their A already)
+                    if (!mbar_wait(empty_bar(s), ph ^ 1u, err, 1, limit)) break;
+                    mbar_expect_tx(full_bar(s), stage_bytes);
 #pragma unroll
-                for (int t = 0; t < NA; t++)
-                    tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
+                    for (int t = 0; t < NA; t++)
+                        tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
+                }
 #pragma unroll
                 for (int t = 0; t < NB; t++) {
                     const uint32_t dst = smem_u32(st + NA * TC_A_TILE + t * B_TILE);
@@ -486,6 +503,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(acce_bar(b));
         }
+        // the accumulation is done: a following GEMM may launch now (on the SMs this grid leaves free, and on each SM
+        // as its block exits), so that its set-up and its constant loads overlap this epilogue
+        if (args.early & 2) pdl_trigger();
         // Epilogue: the outputs go through shared memory (the stage buffers, idle now: every TMA load has been
         // consumed by a completed MMA) in the 128-byte-swizzled layout of 128-row x 128-byte boxes, and leave by
         // TMA stores, whole lines at a time (a thread holds one output row: direct stores would scatter 16-byte
@@ -793,7 +813,7 @@ struct TcOp {
 };
 
 template <int BN, int EPI, int MODE>
-static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
+static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s, int early) {
     constexpr bool F16 = MODE == 2;
     // the shared-memory attribute is a property of the function on each device: set once per device (a race of two
     // host threads sets it twice, which is harmless)
@@ -841,6 +861,7 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
     args.err = err;
     args.wait_ns = tc_wait_ns();
     args.stall = tc_test_stall() ? 1 : 0;
+    args.early = early;
     const TcProblem& p = ops[0].p;
     dim3 grid(p.N / BN, p.M / TC_BM, nops);
     if (launch_k(tc_gemm_kernel<BN, EPI, MODE>, dim3(grid), dim3(TC_THREADS), TC_SMEM, s, maps[0], maps[1], maps[2],
@@ -851,27 +872,29 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s) {
 }
 
 template <int BN, int EPI>
-static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s) {
-    if (mode == GP103_FIELD_BF16X3) return launch_tc_mode<BN, EPI, 0>(ops, nops, err, s);
-    if (mode == GP103_FIELD_F16X3) return launch_tc_mode<BN, EPI, 2>(ops, nops, err, s);
-    return launch_tc_mode<BN, EPI, 1>(ops, nops, err, s);
+static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int early) {
+    if (mode == GP103_FIELD_BF16X3) return launch_tc_mode<BN, EPI, 0>(ops, nops, err, s, early);
+    if (mode == GP103_FIELD_F16X3) return launch_tc_mode<BN, EPI, 2>(ops, nops, err, s, early);
+    return launch_tc_mode<BN, EPI, 1>(ops, nops, err, s, early);
 }
 
 // One GEMM per launch: 64-column tiles (twice the blocks); two per launch: 128-column tiles, or 64-column ones
 // (bn = 64: two half-height problems). The epilogue is a template argument (every problem of a launch has the same
-// one).
-static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int bn = 0) {
+// one). `last`: no GEMM of the field follows this launch (it then does not let the next kernel launch early).
+static int launch_tc(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int bn = 0, bool last = false) {
     const int epi = ops[0].p.epi;
-    if (epi == EPI_SPLIT && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s);
-    if (epi == EPI_WEIGHT2 && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s);
+    const int early = field_early() & (last ? 1 : 3);
+    if (epi == EPI_SPLIT && (nops == 1 || bn == 64)) return launch_tc_bn<64, EPI_SPLIT>(ops, nops, mode, err, s, early);
+    if (epi == EPI_WEIGHT2 && (nops == 1 || bn == 64))
+        return launch_tc_bn<64, EPI_WEIGHT2>(ops, nops, mode, err, s, early);
     if (epi == EPI_FOLD)                                         // 128 columns: 64 and their mirror (f16x3 only)
-        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<128, EPI_FOLD, 2>(ops, nops, err, s) : GP103_ERR_ARG;
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<128, EPI_FOLD, 2>(ops, nops, err, s, early) : GP103_ERR_ARG;
     if (epi == EPI_MSPLIT)                                       // half-height tiles, each with its mirror (f16x3)
-        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MSPLIT, 2>(ops, nops, err, s) : GP103_ERR_ARG;
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MSPLIT, 2>(ops, nops, err, s, early) : GP103_ERR_ARG;
     if (epi == EPI_MPLAIN)
-        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MPLAIN, 2>(ops, nops, err, s) : GP103_ERR_ARG;
-    if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s);
-    if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s);
+        return mode == GP103_FIELD_F16X3 ? launch_tc_mode<64, EPI_MPLAIN, 2>(ops, nops, err, s, early) : GP103_ERR_ARG;
+    if (nops == 2 && epi == EPI_SPLIT) return launch_tc_bn<128, EPI_SPLIT>(ops, nops, mode, err, s, early);
+    if (nops == 2 && epi == EPI_PLAIN) return launch_tc_bn<128, EPI_PLAIN>(ops, nops, mode, err, s, early);
     return GP103_ERR_ARG;                                        // no other combination is used
 }
 
@@ -1072,7 +1095,7 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     o4[1].p.out_f32 = ey;
     o4[0].p.b_exp = E(L.e_pt);
     o4[1].p.b_exp = E(L.e_qt);
-    return launch_tc(o4, 2, L.mode, err, s);
+    return launch_tc(o4, 2, L.mode, err, s, 0, true);
 }
 
 }  // namespace gp103

@@ -20,6 +20,7 @@ bool pdl_enabled();
 long long tc_wait_ns();     // GP103_OPT_WAIT_MS, in ns: the limit of a tensor-core field wait
 bool tc_test_stall();       // GP103_OPT_TEST_STALL_FIELD
 int wa_long_share();        // GP103_OPT_WA_FUSED: percent of the fused WA launch's blocks on long nets (0: two launches)
+int field_early();          // GP103_OPT_FIELD_EARLY: bit 0 constant operand before the wait, bit 1 early trigger
 
 // Programmatic dependent launch: a kernel may be launched while the one before it on the stream is finishing; it
 // waits here (at its very start, before touching any data) until that one has completed and its writes are

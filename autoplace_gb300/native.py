@@ -8,7 +8,7 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_ARG, ERR_CUDA, ERR_SHAPE = 0, 1, 2, 3
-OPT_PDL, OPT_WAIT_MS, OPT_TEST_STALL_FIELD, OPT_WA_FUSED = 0, 1, 2, 3
+OPT_PDL, OPT_WAIT_MS, OPT_TEST_STALL_FIELD, OPT_WA_FUSED, OPT_FIELD_EARLY = 0, 1, 2, 3, 4
 # the waits of the tensor-core field (gp103_device_error codes)
 DEVICE_ERRORS = {1: "a TMA stage's slot", 2: "an accumulator's buffer", 3: "a TMA stage's data",
                  4: "an accumulator's result"}

@@ -47,8 +47,14 @@ const char* gp103_status_string(int status);
  * GP103_OPT_WA_FUSED (default 55, 0 .. 99): 0 = the WA kernels of a pass as two launches (short nets, then long
  *   ones); p > 0 = one launch of one resident wave, p % of its blocks on the long nets and the rest on the short
  *   ones, so that the two halves run side by side (every net's arithmetic is unchanged; the WA and HPWL totals are
- *   summed from other block partials). Measured at 1.2M cells: 0.0854 ms per pass in two launches, 0.0778 at 55. */
-enum { GP103_OPT_PDL = 0, GP103_OPT_WAIT_MS = 1, GP103_OPT_TEST_STALL_FIELD = 2, GP103_OPT_WA_FUSED = 3 };
+ *   summed from other block partials). Measured at 1.2M cells: 0.0854 ms per pass in two launches, 0.0778 at 55.
+ * GP103_OPT_FIELD_EARLY (default 3, bits): how a tensor-core field GEMM overlaps the kernel before it (with
+ *   GP103_OPT_PDL). Bit 0: the constant operand (a cosine or sine matrix, written once by the field's set-up) of the
+ *   first pipeline stages is loaded before the wait for the previous kernel; bit 1: the GEMMs that another GEMM
+ *   follows let it launch as soon as their accumulation is done, so that its set-up and constant loads run beside
+ *   their epilogue. The results are the same bits either way. */
+enum { GP103_OPT_PDL = 0, GP103_OPT_WAIT_MS = 1, GP103_OPT_TEST_STALL_FIELD = 2, GP103_OPT_WA_FUSED = 3,
+       GP103_OPT_FIELD_EARLY = 4 };
 int gp103_set_option(int option, int value);
 
 /* Kernel launches issued through this library so far (a launch captured into a CUDA graph counts once). */
