@@ -221,7 +221,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
 extern "C" int gp103_plan_sizes(int nbx, int nby, int field_mode, gp103_sizes* out) {
     REQUIRE(out && nbx > 0 && nby > 0);
     REQUIRE(field_mode == GP103_FIELD_FP32 || field_mode == GP103_FIELD_BF16X3 || field_mode == GP103_FIELD_BF16X6 ||
-            field_mode == GP103_FIELD_F16X3);
+            field_mode == GP103_FIELD_F16X3 || field_mode == GP103_FIELD_TF32X3);
     if (field_mode != GP103_FIELD_FP32 && !field_tc_supported(nbx, nby)) return GP103_ERR_SHAPE;
     FieldLayout L = field_layout(nbx, nby, field_mode);
     out->field_const = L.const_bytes;
@@ -233,7 +233,7 @@ extern "C" int gp103_plan_sizes(int nbx, int nby, int field_mode, gp103_sizes* o
 static int check_plan(const gp103_plan* p) {
     REQUIRE(p && p->num_nodes >= 0 && p->num_mov >= 0 && p->num_mov <= p->num_nodes && p->num_nets >= 0);
     REQUIRE(p->nbx > 0 && p->nby > 0 && p->bx > 0.f && p->by > 0.f);
-    REQUIRE(p->field_mode >= GP103_FIELD_FP32 && p->field_mode <= GP103_FIELD_F16X3);
+    REQUIRE(p->field_mode >= GP103_FIELD_FP32 && p->field_mode <= GP103_FIELD_TF32X3);
     REQUIRE(p->field_const && p->field_work && p->ex && p->ey && p->red && p->counters && p->map && p->kp);
     REQUIRE(p->jnbx == 0 || (p->jnby > 0 && p->jmap && p->jsize && p->jratio && p->jfixed));
     REQUIRE(p->net_split >= 0 && p->net_split <= p->num_nets);
@@ -352,6 +352,9 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
     pj.shift = p->field_shift;
     if (p->field_mode == GP103_FIELD_FP32) {
         pj.dens = (float*)((char*)p->field_work + L.w_a);
+    } else if (p->field_mode == GP103_FIELD_TF32X3) {
+        pj.tf0 = (float*)((char*)p->field_work + L.w_a);
+        pj.tf1 = pj.tf0 + nb;
     } else {
         __nv_bfloat16* t = (__nv_bfloat16*)((char*)p->field_work + L.w_a);
         pj.t0 = t;

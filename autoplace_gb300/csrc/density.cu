@@ -440,6 +440,14 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
 #pragma unroll
             for (int k = 0; k < 4; k++) r[k] = __fsub_rn(r[k], j.shift);
             if (j.dens) *(float4*)(j.dens + b) = make_float4(r[0], r[1], r[2], r[3]);
+            if (j.tf0) {                                     // tf32 terms: the rounding and what it leaves
+                float4 a, c;
+                a.x = tf32_round(r[0]); a.y = tf32_round(r[1]); a.z = tf32_round(r[2]); a.w = tf32_round(r[3]);
+                c.x = tf32_round(__fsub_rn(r[0], a.x)); c.y = tf32_round(__fsub_rn(r[1], a.y));
+                c.z = tf32_round(__fsub_rn(r[2], a.z)); c.w = tf32_round(__fsub_rn(r[3], a.w));
+                *(float4*)(j.tf0 + b) = a;
+                *(float4*)(j.tf1 + b) = c;
+            }
             if (j.exps) {
                 // a 64-bin chunk of a row is 16 consecutive quads: half a warp (the loop keeps whole warps, since
                 // quads is a multiple of 32 on the tensor-core grids); its scale from its largest magnitude
@@ -485,6 +493,11 @@ __global__ void post_plain_kernel(const __grid_constant__ PostPair pair) {
             const float r = __fsub_rn(__fadd_rn(mov, unfixed32(j.map[nb + b])), j.shift);
             if (j.dens) j.dens[b] = r;
             if (j.t0) split_bf16(r, j.terms, j.t0, j.t1, j.t2, b);
+            if (j.tf0) {
+                const float a = tf32_round(r);
+                j.tf0[b] = a;
+                j.tf1[b] = tf32_round(__fsub_rn(r, a));
+            }
             j.map[nb + b] = 0ull;
         }
         j.map[b] = 0ull;

@@ -39,8 +39,9 @@ __device__ __forceinline__ double trig(int kind, int p, int u, int n) {
     return kind == 0 ? cospi(t) : sinpi(t);
 }
 
-// what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]; f16: two float16 terms of
-// the value times 2^F16_CONST instead of three bf16 terms
+// what: 0 = C[p][u], 1 = S[p][u], 2 = C^T[m][p] = C[p][m], 3 = S^T[m][p] = S[p][m]; f16 = 1: two float16 terms of
+// the value times 2^F16_CONST instead of three bf16 terms; f16 = 2: two tf32 terms as float32 planes (t0, t1 point
+// at float planes)
 // The frequency of position c in the folded order of the coefficients (f16x3): the even frequencies 0, 2, .. first,
 // then the odd ones 1, 3, ..
 __device__ __forceinline__ int folded_freq(int c, int n) { return c < n / 2 ? 2 * c : 2 * (c - n / 2) + 1; }
@@ -61,7 +62,11 @@ __global__ void trig_matrix_kernel(int what, int n, float* f32, __nv_bfloat16* t
         else if (what < 2) v = trig(kind, r, col, n);
         else v = trig(kind, pcols ? folded_freq(col, n) : col, r, n);
         if (f32) f32[e] = (float)v;
-        if (t0 && f16) {
+        if (t0 && f16 == 2) {
+            const float a = tf32_round((float)v);
+            ((float*)t0)[e] = a;
+            ((float*)t1)[e] = tf32_round((float)(v - (double)a));
+        } else if (t0 && f16) {
             const double w = ldexp(v, F16_CONST);
             const __half a = __double2half(w);
             const __half b = __double2half(w - (double)__half2float(a));
@@ -117,7 +122,8 @@ FieldLayout field_layout(int nbx, int nby, int mode) {
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 1023) & ~(size_t)1023; return at; };
     // constants: the 6 operand matrices (float32 or 3 bf16 terms) and the two weight planes (float32)
-    const size_t es = mode == GP103_FIELD_FP32 ? 4 : 3 * 2;     // bytes per element (all terms)
+    // bytes per element (all terms): float32; 3 x 16 bits (the 16-bit modes use 2 or 3 of them); tf32x3: 2 x 32 bits
+    const size_t es = mode == GP103_FIELD_FP32 ? 4 : mode == GP103_FIELD_TF32X3 ? 8 : 3 * 2;
     L.c_cx = take(xx * es); L.c_cy = take(yy * es); L.c_cyt = take(yy * es);
     L.c_sxt = take(xx * es); L.c_syt = take(yy * es); L.c_cxt = take(xx * es);
     L.c_wx = take(xy * 4); L.c_wy = take(xy * 4);
@@ -151,8 +157,11 @@ int field_constants(const FieldLayout& L, void* cbuf, cudaStream_t s) {
         const size_t plane = m.fold ? (size_t)(m.n / 2) * (m.n / 2) : (size_t)m.n * m.n;
         float* f = fp32 ? (float*)(c + m.off) : nullptr;
         __nv_bfloat16* t0 = fp32 ? nullptr : (__nv_bfloat16*)(c + m.off);
-        if (launch_k(trig_matrix_kernel, dim3(grid_for(plane, 256, 8)), dim3(256), 0, s, m.what, m.n, f, t0, t0 ? t0 + plane : nullptr,
-                     t0 ? t0 + 2 * plane : nullptr, plane, (int)(L.mode == GP103_FIELD_F16X3), m.fold, m.pcols) != cudaSuccess)
+        const bool tf = L.mode == GP103_FIELD_TF32X3;            // two float32 planes
+        __nv_bfloat16* t1 = !t0 ? nullptr : tf ? (__nv_bfloat16*)((float*)t0 + plane) : t0 + plane;
+        __nv_bfloat16* t2 = !t0 || tf ? nullptr : t0 + 2 * plane;
+        if (launch_k(trig_matrix_kernel, dim3(grid_for(plane, 256, 8)), dim3(256), 0, s, m.what, m.n, f, t0, t1, t2, plane,
+                     tf ? 2 : (int)(L.mode == GP103_FIELD_F16X3), m.fold, m.pcols) != cudaSuccess)
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     }

@@ -8,6 +8,8 @@
 //   bf16x3: (1,0) (0,1) (0,0)                          ~1e-5 of the max
 //   bf16x6: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)        ~2e-7 of the max (float32-level)
 // f16x3 instead keeps two float16 terms per operand, data chunks scaled by powers of two (below), 3 products.
+// tf32x3 keeps two tf32 terms per operand as float32 planes (kind::tf32 MMAs: a 128-byte row is 32 of K), 3 products
+// as bf16x3's.
 // Tiles are 128 rows x BN columns: BN = 64 when a launch has one GEMM (twice the blocks), 128 when it has two.
 // Folded transforms (f16x3, grids of multiples of 256; field.cuh): the forward ones as two half-size GEMMs per launch
 // (64-column tiles; the first with EPI_FOLD, 64-row B tiles and their mirrors), the inverse ones as half-height
@@ -23,8 +25,8 @@
 
 namespace gp103 {
 
-constexpr int TC_BM = 128, TC_BK = 64;
-constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                     // 16 KB per A term tile
+constexpr int TC_BM = 128, TC_BK = 64;                           // TC_BK: 16-bit elements of K per k-block
+constexpr int TC_A_TILE = TC_BM * TC_BK * 2;                     // 16 KB per A term tile (128-byte rows, any mode)
 constexpr int TC_STAGE_SPACE = 216 * 1024;                       // room for the stages
 constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_SMEM = TC_STAGE_SPACE + 1024 + 256;
@@ -155,18 +157,28 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor: D float32, A and B both bf16 (F16 = false) or both float16, both K-major, M = 128, N.
-template <int N, bool F16>
+// Operand kinds: A and B of one MMA always have the same type.
+enum { KIND_BF16 = 0, KIND_F16 = 1, KIND_TF32 = 2 };
+
+// Instruction descriptor: D float32; A and B both bf16 (format 1) or both float16 (format 0) for kind::f16, both tf32
+// (format 2) for kind::tf32; both K-major; M = 128, N.
+template <int N, int KIND>
 __device__ __forceinline__ constexpr uint32_t idesc() {
-    return (1u << 4) | (F16 ? 0u : (1u << 7) | (1u << 10)) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(TC_BM >> 4) << 24);
+    constexpr uint32_t fmt = KIND == KIND_BF16 ? 1u : KIND == KIND_F16 ? 0u : 2u;
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 }
 
-template <int N, bool F16>
+// One MMA: D (+)= A B^T over a K step of 32 bytes of the operand rows (16 elements of 16 bits, or 8 of tf32).
+template <int N, int KIND>
 __device__ __forceinline__ void mma_n(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N, F16>()), "r"(accumulate));
+    if constexpr (KIND == KIND_TF32)
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+            ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N, KIND>()), "r"(accumulate));
+    else
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+            ::"r"(tmem), "l"(a), "l"(b), "r"(idesc<N, KIND>()), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -254,8 +266,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                    const __grid_constant__ CUtensorMap o1a, const __grid_constant__ CUtensorMap o1b, TcArgs args) {
     // The set-up (barriers, tensor memory, tensor-map prefetch) reads nothing the previous kernel writes: it runs
     // before griddepcontrol.wait, overlapping the previous kernel's tail.
-    constexpr int X6 = MODE == 1 ? 1 : 0;                        // bf16x6 (MODE 0: bf16x3, MODE 2: f16x3)
+    constexpr int X6 = MODE == 1 ? 1 : 0;                        // bf16x6 (MODE 0: bf16x3, 2: f16x3, 3: tf32x3)
     constexpr bool F16 = MODE == 2;
+    constexpr bool TF32 = MODE == 3;
+    constexpr int KIND = TF32 ? KIND_TF32 : F16 ? KIND_F16 : KIND_BF16;
+    constexpr int BKE = TF32 ? 32 : TC_BK;                       // elements of K per k-block (a 128-byte row)
     constexpr int B_TILE = BN * TC_BK * 2;
     constexpr int NA = X6 ? 3 : 2, NB = NA, NPROD = X6 ? 6 : 3;
     // bf16 modes, BN = 64: the products are grouped by B term into NBLK column blocks of the accumulator (block j =
@@ -283,7 +298,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const CUtensorMap* ma = z ? &a1 : &a0;
     const CUtensorMap* mb = z ? &b1 : &b0;
     const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
-    const int total = P.K / TC_BK, stages = args.stages;
+    const int total = P.K / BKE, stages = args.stages;
     constexpr int stage_bytes = NA * TC_A_TILE + NB * B_TILE;
     int* err = args.err;
     const long long limit = args.wait_ns;
@@ -327,7 +342,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_expect_tx(full_bar(it), stage_bytes);
 #pragma unroll
             for (int t = 0; t < NA; t++)
-                tma_load_3d(smem_u32(smem + it * stage_bytes + t * TC_A_TILE), ma, full_bar(it), it * TC_BK, m0, t);
+                tma_load_3d(smem_u32(smem + it * stage_bytes + t * TC_A_TILE), ma, full_bar(it), it * BKE, m0, t);
         }
     }
     pdl_wait();
@@ -344,7 +359,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     mbar_expect_tx(full_bar(s), stage_bytes);
 #pragma unroll
                     for (int t = 0; t < NA; t++)
-                        tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * TC_BK, m0, t);
+                        tma_load_3d(smem_u32(st + t * TC_A_TILE), ma, full_bar(s), it * BKE, m0, t);
                 }
 #pragma unroll
                 for (int t = 0; t < NB; t++) {
@@ -353,7 +368,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         tma_load_3d(dst, mb, full_bar(s), it * TC_BK, 64 * (int)blockIdx.x, t);
                         tma_load_3d(dst + 64 * 128, mb, full_bar(s), it * TC_BK, P.N - 64 - 64 * (int)blockIdx.x, t);
                     } else {
-                        tma_load_3d(dst, mb, full_bar(s), it * TC_BK, n0, t);
+                        tma_load_3d(dst, mb, full_bar(s), it * BKE, n0, t);
                     }
                 }
                 issued = it + 1;
@@ -385,29 +400,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     // product first, and each block starts fresh (accumulate = 0) with its first product.
                     if constexpr (X6) {
 #pragma unroll
-                        for (int kk = 0; kk < 4; kk++) mma_n<64, F16>(acc, A(2, kk), Bd(0, kk), kk > 0);     // a2 b0
-                        mma_n<64, F16>(acc + 64, A(1, 0), Bd(1, 0), 0);                                      // a1 b1
-                        mma_n<64, F16>(acc, A(1, 0), Bd(0, 0), 1);                                           // a1 b0
+                        for (int kk = 0; kk < 4; kk++) mma_n<64, KIND>(acc, A(2, kk), Bd(0, kk), kk > 0);     // a2 b0
+                        mma_n<64, KIND>(acc + 64, A(1, 0), Bd(1, 0), 0);                                      // a1 b1
+                        mma_n<64, KIND>(acc, A(1, 0), Bd(0, 0), 1);                                           // a1 b0
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<128, F16>(acc, A(1, kk), Bd(0, kk), 1);         // a1 [b0 b1]
-                        mma_n<64, F16>(acc + 128, A(0, 0), Bd(2, 0), 0);                                     // a0 b2
-                        mma_n<128, F16>(acc, A(0, 0), Bd(0, 0), 1);                                          // a0 [b0 b1]
+                        for (int kk = 1; kk < 4; kk++) mma_n<128, KIND>(acc, A(1, kk), Bd(0, kk), 1);         // a1 [b0 b1]
+                        mma_n<64, KIND>(acc + 128, A(0, 0), Bd(2, 0), 0);                                     // a0 b2
+                        mma_n<128, KIND>(acc, A(0, 0), Bd(0, 0), 1);                                          // a0 [b0 b1]
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<192, F16>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1 b2]
+                        for (int kk = 1; kk < 4; kk++) mma_n<192, KIND>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1 b2]
                     } else {
 #pragma unroll
-                        for (int kk = 0; kk < 4; kk++) mma_n<64, F16>(acc, A(1, kk), Bd(0, kk), kk > 0);     // a1 b0
-                        mma_n<64, F16>(acc + 64, A(0, 0), Bd(1, 0), 0);                                      // a0 b1
-                        mma_n<64, F16>(acc, A(0, 0), Bd(0, 0), 1);                                           // a0 b0
+                        for (int kk = 0; kk < 4; kk++) mma_n<64, KIND>(acc, A(1, kk), Bd(0, kk), kk > 0);     // a1 b0
+                        mma_n<64, KIND>(acc + 64, A(0, 0), Bd(1, 0), 0);                                      // a0 b1
+                        mma_n<64, KIND>(acc, A(0, 0), Bd(0, 0), 1);                                           // a0 b0
 #pragma unroll
-                        for (int kk = 1; kk < 4; kk++) mma_n<128, F16>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1]
+                        for (int kk = 1; kk < 4; kk++) mma_n<128, KIND>(acc, A(0, kk), Bd(0, kk), 1);         // a0 [b0 b1]
                     }
                 } else {
 #pragma unroll
                     for (int q = 0; q < NPROD; q++)
 #pragma unroll
                         for (int kk = 0; kk < TC_BK / 16; kk++)
-                            mma_n<BN, F16>(acc, A(prod_a(X6, q), kk), Bd(prod_b(X6, q), kk), (q > 0 || kk > 0) ? 1u : 0u);
+                            mma_n<BN, KIND>(acc, A(prod_a(X6, q), kk), Bd(prod_b(X6, q), kk), (q > 0 || kk > 0) ? 1u : 0u);
                 }
                 mma_commit(empty_bar(s));
                 mma_commit(accf_bar(b));
@@ -518,9 +533,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t sbase = smem_u32(smem);
         // the weighted epilogue's column weights: this tile's BN entries into shared memory (one wave of loads, read
         // back as broadcasts), behind the six output boxes
-        const float4* wsh = (const float4*)(smem + 6 * EPI_BOX);
+        constexpr int WSH_BOX = TF32 ? 8 : 6;                    // (tf32: Kx and Ky as 2 terms x 2 boxes each)
+        const float4* wsh = (const float4*)(smem + WSH_BOX * EPI_BOX);
         if (EPI == EPI_WEIGHT2) {
-            if (r_in < BN) ((float4*)(smem + 6 * EPI_BOX))[r_in] = P.wcol[n0 + r_in];
+            if (r_in < BN) ((float4*)(smem + WSH_BOX * EPI_BOX))[r_in] = P.wcol[n0 + r_in];
             asm volatile("bar.sync 1, 128;" ::: "memory");
         }
         // MIRROR: box row of this thread's row of the mirror tile (stored upside down: tile row r_in is output row
@@ -619,6 +635,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         st_shared_v4(sbase + chunk(1 * (BN / 64) + g, c), *(const float4*)tb);
                     }
                 }
+            } else if (EPI == EPI_SPLIT && TF32) {               // tf32 terms (float32): boxes of 32 columns, term-major
+#pragma unroll
+                for (int c = 0; c < BN / 4; c++) {
+                    float a[4], b[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        a[i] = tf32_round(r[4 * c + i]);
+                        b[i] = tf32_round(__fsub_rn(r[4 * c + i], a[i]));
+                    }
+                    const int g = c >> 3;
+                    st_shared_v4(sbase + chunk(0 * (BN / 32) + g, c & 7), make_float4(a[0], a[1], a[2], a[3]));
+                    st_shared_v4(sbase + chunk(1 * (BN / 32) + g, c & 7), make_float4(b[0], b[1], b[2], b[3]));
+                }
             } else if (EPI == EPI_SPLIT) {                       // bf16 terms: boxes of 64 columns, term-major
 #pragma unroll
                 for (int c = 0; c < BN / 8; c++) {
@@ -629,6 +658,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     st_shared_v4(sbase + chunk(0 * (BN / 64) + g, c & 7), *(const float4*)ta);
                     st_shared_v4(sbase + chunk(1 * (BN / 64) + g, c & 7), *(const float4*)tb);
                     st_shared_v4(sbase + chunk(2 * (BN / 64) + g, c & 7), *(const float4*)tc);
+                }
+            } else if (TF32) {
+                // Kx = K Wx, Ky = K Wy (as below) in tf32 terms, boxes of 32 columns (BN = 64): 0-1 the first term of
+                // Kx, 2-3 its second term, 4-7 the same for Ky
+#pragma unroll
+                for (int c = 0; c < BN / 4; c++) {
+                    float xa[4], xb[4], ya[4], yb[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const float4 wc = wsh[4 * c + i];
+                        const float t = wr.x + wc.x;
+                        const float rr = t > 0.f ? recip(t) : 0.f;
+                        const float kx = r[4 * c + i] * (wr.y * wc.z * rr), ky = r[4 * c + i] * (wc.y * wr.z * rr);
+                        xa[i] = tf32_round(kx);
+                        xb[i] = tf32_round(__fsub_rn(kx, xa[i]));
+                        ya[i] = tf32_round(ky);
+                        yb[i] = tf32_round(__fsub_rn(ky, ya[i]));
+                    }
+                    const int g = c >> 3;
+                    st_shared_v4(sbase + chunk(0 * (BN / 32) + g, c & 7), make_float4(xa[0], xa[1], xa[2], xa[3]));
+                    st_shared_v4(sbase + chunk(1 * (BN / 32) + g, c & 7), make_float4(xb[0], xb[1], xb[2], xb[3]));
+                    st_shared_v4(sbase + chunk(2 * (BN / 32) + g, c & 7), make_float4(ya[0], ya[1], ya[2], ya[3]));
+                    st_shared_v4(sbase + chunk(3 * (BN / 32) + g, c & 7), make_float4(yb[0], yb[1], yb[2], yb[3]));
                 }
             } else if (F16) {
                 // Kx = K Wx, Ky = K Wy as below, each row's 64 columns scaled by a power of two taken from an upper
@@ -726,12 +778,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     tma_store_3d(mo, sbase + t * EPI_BOX, 64 * (int)blockIdx.x, om0, t);
                     tma_store_3d(mo2, sbase + (2 + t) * EPI_BOX, 64 * (int)blockIdx.x, om0, t);
                 }
+            } else if (EPI == EPI_SPLIT && TF32) {               // 2 terms of BN / 32 boxes of 32 float32 columns
+#pragma unroll
+                for (int t = 0; t < 2; t++)
+#pragma unroll
+                    for (int g = 0; g < BN / 32; g++)
+                        tma_store_3d(mo, sbase + (t * (BN / 32) + g) * EPI_BOX, n0 + 32 * g, om0, t);
             } else if (EPI == EPI_SPLIT) {
                 constexpr int OT = F16 ? 2 : 3;                  // output terms
 #pragma unroll
                 for (int t = 0; t < OT; t++)
 #pragma unroll
                     for (int g = 0; g < BN / 64; g++) tma_store_3d(mo, sbase + (t * (BN / 64) + g) * EPI_BOX, n0 + 64 * g, om0, t);
+            } else if (TF32) {                                   // WEIGHT2: Kx, Ky: 2 terms x BN / 32 boxes each
+#pragma unroll
+                for (int t = 0; t < 2; t++)
+#pragma unroll
+                    for (int g = 0; g < BN / 32; g++) {
+                        tma_store_3d(mo, sbase + (t * (BN / 32) + g) * EPI_BOX, n0 + 32 * g, om0, t);
+                        tma_store_3d(mo2, sbase + ((2 + t) * (BN / 32) + g) * EPI_BOX, n0 + 32 * g, om0, t);
+                    }
             } else {
                 constexpr int OT = F16 ? 2 : 3;
 #pragma unroll
@@ -772,16 +838,20 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 16-bit term planes [terms][rows][K] as a 3-D tensor (K, rows, term); box = 64 x box_rows x 1. Three bf16 planes
-// (the bf16 modes; bf16x3 reads two of them) or two float16 planes (f16x3).
-static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows, bool f16 = false) {
+// Term planes [terms][rows][K] as a 3-D tensor (K, rows, term); box = one 128-byte row of K x box_rows x 1. Three
+// bf16 planes (the bf16 modes; bf16x3 reads two of them), two float16 planes (f16x3, MODE 2) or two float32 planes
+// holding tf32 terms (tf32x3, MODE 3: a box row is 32 elements).
+static bool make_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows, int mode = 0) {
     auto fn = encode_fn();
     if (!fn) return false;
-    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, f16 ? 2u : 3u};
-    cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
-    cuuint32_t box[3] = {TC_BK, (cuuint32_t)box_rows, 1};
+    const bool f16 = mode == 2, tf = mode == 3;
+    const cuuint64_t es = tf ? 4 : 2;
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, f16 || tf ? 2u : 3u};
+    cuuint64_t strides[2] = {(cuuint64_t)K * es, (cuuint64_t)rows * K * es};
+    cuuint32_t box[3] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = fn(m, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+    CUresult r = fn(m, tf ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
                     const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -838,8 +908,8 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s, i
                     !o.p.b_exp || (EPI != EPI_PLAIN && EPI != EPI_MPLAIN && !o.p.o_exp) ||
                     ((EPI == EPI_WEIGHT2 || EPI == EPI_FOLD) && !o.p.o2_exp)))
             return GP103_ERR_ARG;
-        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM, F16) ||
-            !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, EPI == EPI_FOLD ? 64 : BN, F16))
+        if (!make_map(&maps[2 * z], o.a, o.arows, o.p.K, TC_BM, MODE) ||
+            !make_map(&maps[2 * z + 1], o.b, o.brows, o.p.K, EPI == EPI_FOLD ? 64 : BN, MODE))
             return GP103_ERR_CUDA;
         // outputs (stored by TMA): bf16 terms [3][M][N] as (N, M, term) boxes of 64 x 128; float32 [M][N]
         CUtensorMap* oa = &maps[4 + 2 * z];
@@ -850,8 +920,8 @@ static int launch_tc_mode(const TcOp* ops, int nops, int* err, cudaStream_t s, i
             *ob = *oa;
         } else {
             const int ncols = EPI == EPI_FOLD ? o.p.N / 2 : o.p.N;
-            ok = make_map(oa, o.p.o_terms, o.p.M_out, ncols, TC_BM, F16);
-            if (ok && (EPI == EPI_WEIGHT2 || EPI == EPI_FOLD)) ok = make_map(ob, o.p.o2_terms, o.p.M_out, ncols, TC_BM, F16);
+            ok = make_map(oa, o.p.o_terms, o.p.M_out, ncols, TC_BM, MODE);
+            if (ok && (EPI == EPI_WEIGHT2 || EPI == EPI_FOLD)) ok = make_map(ob, o.p.o2_terms, o.p.M_out, ncols, TC_BM, MODE);
             else *ob = *oa;
         }
         if (!ok) return GP103_ERR_CUDA;
@@ -875,6 +945,7 @@ template <int BN, int EPI>
 static int launch_tc_bn(const TcOp* ops, int nops, int mode, int* err, cudaStream_t s, int early) {
     if (mode == GP103_FIELD_BF16X3) return launch_tc_mode<BN, EPI, 0>(ops, nops, err, s, early);
     if (mode == GP103_FIELD_F16X3) return launch_tc_mode<BN, EPI, 2>(ops, nops, err, s, early);
+    if (mode == GP103_FIELD_TF32X3) return launch_tc_mode<BN, EPI, 3>(ops, nops, err, s, early);
     return launch_tc_mode<BN, EPI, 1>(ops, nops, err, s, early);
 }
 
@@ -906,6 +977,16 @@ __global__ void split_density_kernel(const float* d, size_t n, float shift, __nv
         t[e] = a;
         t[n + e] = b;
         t[2 * n + e] = c;
+    }
+}
+
+// tf32x3: the shifted float32 density into two tf32 terms (float32 planes t[0 .. n), t[n .. 2n))
+__global__ void split_density_tf32_kernel(const float* d, size_t n, float shift, float* t) {
+    pdl_wait();
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const float x = __fsub_rn(d[e], shift), a = tf32_round(x);
+        t[e] = a;
+        t[n + e] = tf32_round(__fsub_rn(x, a));
     }
 }
 
@@ -996,6 +1077,11 @@ int field_tc(const FieldLayout& L, const void* cbuf, void* wbuf, const float* de
     if (density && L.fold) {
         if (launch_k(split_density_fold_kernel, dim3(grid_for((size_t)X * Y / 4, 256, 8)), dim3(256), 0, s, density,
                      X, Y, L.shift, (__half*)(w + L.w_a), E(L.e_a)) != cudaSuccess)
+            return GP103_ERR_CUDA;
+        GP103_CHECK_LAUNCH();
+    } else if (density && L.mode == GP103_FIELD_TF32X3) {
+        if (launch_k(split_density_tf32_kernel, dim3(grid_for((size_t)X * Y, 256, 8)), dim3(256), 0, s, density,
+                     (size_t)X * Y, L.shift, (float*)(w + L.w_a)) != cudaSuccess)
             return GP103_ERR_CUDA;
         GP103_CHECK_LAUNCH();
     } else if (density && f16) {

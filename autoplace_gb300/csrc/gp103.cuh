@@ -70,6 +70,14 @@ __device__ __forceinline__ int f16_chunk_exp(float mx) {
     return min(max(e, -100), 100);
 }
 
+// x rounded to tf32 (10 mantissa bits, to nearest, ties away from zero), as a float32 with its low 13 bits zero: the
+// first term of a tf32 split; x - tf32_round(x) is exact, and its own rounding is the second term.
+__device__ __forceinline__ float tf32_round(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r & 0xffffe000u);
+}
+
 // Grid for a grid-stride loop over n items: at most `per_sm` blocks per SM, at least one block.
 inline int grid_for(long long n, int threads, int per_sm) {
     long long g = (n + threads - 1) / threads;

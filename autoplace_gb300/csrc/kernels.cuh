@@ -101,6 +101,7 @@ struct PostJob {
     float* dens;                // plain density, may be null
     __nv_bfloat16 *t0, *t1, *t2;  // bf16 split terms of the density, may be null
     int terms;
+    float *tf0, *tf1;           // tf32 split terms of the density (float32 planes), may be null
     signed char* exps;          // non-null: float16 terms (t0, t1 hold __half) of each 64-bin chunk of a row scaled by
                                 // 2^e, e = exps[(y / 64) * nbx + x] (nby a multiple of 64)
     int fold;                   // with exps (nby a multiple of 128): the terms of the density folded about the middle

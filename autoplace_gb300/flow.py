@@ -46,6 +46,8 @@ class Flow(object):
         self.field, self.coarse_field = field, coarse_field or field
         self.fine = Placer(prob, field=field, host=host, **self.kw)
         self.last_coarse = None
+        self.keep_coarse_placer = False             # keep the clusters' Placer of the last run (last_cplacer)
+        self.last_cplacer = None
         # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws)
         self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
 
@@ -119,6 +121,7 @@ class Flow(object):
             stats["coarse_reason"] = level["reason"]
             pos0 = pos
             self.last_coarse = coarse
+            self.last_cplacer = cplacer if self.keep_coarse_placer else None
             del cplacer, cp, cpos                                   # the clusters' buffers are not needed any more
         level = fine.run(pos0, log=log, resume=resume)
         torch.cuda.synchronize(dev)

@@ -12,8 +12,9 @@ OPT_PDL, OPT_WAIT_MS, OPT_TEST_STALL_FIELD, OPT_WA_FUSED, OPT_FIELD_EARLY = 0, 1
 # the waits of the tensor-core field (gp103_device_error codes)
 DEVICE_ERRORS = {1: "a TMA stage's slot", 2: "an accumulator's buffer", 3: "a TMA stage's data",
                  4: "an accumulator's result"}
-FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6, FIELD_F16X3 = 0, 1, 2, 3
-FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6, "f16x3": FIELD_F16X3}
+FIELD_FP32, FIELD_BF16X3, FIELD_BF16X6, FIELD_F16X3, FIELD_TF32X3 = 0, 1, 2, 3, 4
+FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X6, "f16x3": FIELD_F16X3,
+               "tf32x3": FIELD_TF32X3}
 PHASE_START, PHASE_DENSITY = 0, 1
 PASS_SORT = 0x100
 T = dict(alpha=0, a=1, iter=2, loop_it=3, done=4, stop=5, accept=6, hpwl=7, wa=8, evals=9, nwa=10, start_tol=11,

@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2")
-    p.add_argument("--field", default="f16x3", choices=["f16x3", "bf16x6", "bf16x3", "fp32"])
+    p.add_argument("--field", default="f16x3", choices=["f16x3", "bf16x6", "bf16x3", "tf32x3", "fp32"])
     p.add_argument("--start", default="auto", choices=["auto", "learned", "plain"],
                    help="the clusters' start: the learned proposal (auto: when a trained model is present) or the "
                         "reference's wirelength-only start")
@@ -217,7 +217,7 @@ def cpu_baseline_dict(per, threads, iters, gpu_iters):
 def kernel_bytes(prob, field="f16x3"):
     """Algorithmic bytes (or flops) per launch of each kernel, by launcher name."""
     terms = 3 if field in ("bf16x6", "bf16x3") else 2 if field == "f16x3" else 0     # 16-bit density terms out
-    dens = 2 * terms if terms else 4
+    dens = 8 if field == "tf32x3" else 2 * terms if terms else 4                      # (tf32x3: 2 float32 terms)
     cs, n, c = prob.csr, prob.num_nodes, prob.num_mov
     P, N = len(cs.cell32), cs.num_nets
     nb = prob.force_bin * prob.force_bin
@@ -237,7 +237,7 @@ def tc_flops(prob, field):
     the height and half the depth, each inverse one into half-height products that also give the mirror rows -- half
     the products in all."""
     nb = prob.force_bin
-    terms = {"bf16x6": 6, "bf16x3": 3, "f16x3": 3}.get(field, 0)
+    terms = {"bf16x6": 6, "bf16x3": 3, "f16x3": 3, "tf32x3": 3}.get(field, 0)
     gemms = 3.0 if field == "f16x3" and nb % 256 == 0 else 6.0
     return 2.0 * nb ** 3 * terms * gemms
 
@@ -298,6 +298,11 @@ def roofline(prob, field, prof, peaks, config="c2"):
              "traffic": round(traffic[name] / max(d["launches_per_pass"], 1e-9)) if name in traffic else None,
              "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
     return r, table
+
+
+def native_modes():
+    from autoplace_gb300 import native
+    return native.FIELD_MODES
 
 
 def load_peaks():
@@ -441,6 +446,18 @@ def run_gb300(args):
     prof, _ = profile_pass(flow.fine)
     peaks = load_peaks()
     roof, table = roofline(prob, args.field, prof, peaks, args.config)
+    ctable = None
+    if flow.last_coarse is not None:
+        # the clusters' level too: one more placement keeping its Placer, profiled at the state it handed over at
+        flow.keep_coarse_placer = True
+        flow.run(dpos, start=start)
+        flow.keep_coarse_placer = False
+        cpl = flow.last_cplacer
+        if cpl is not None:
+            cprof, _ = profile_pass(cpl)
+            cfield = {v: k for k, v in native_modes().items()}.get(cpl.mode, args.field)
+            ctable = roofline(cpl.p, cfield, cprof, peaks, "none")[1]
+        flow.last_cplacer = None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -452,7 +469,7 @@ def run_gb300(args):
             "data": "synthetic (seeded generator standing in for ISPD 2015/2019)",
             "config": config_dict(prob, args, world, start_name), "result": result, "plain": plain,
             "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": roof, "kernels": table, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roof, "kernels": table, "kernels_clusters": ctable, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": int(launches)}
     if rank == 0:
         print(json.dumps(line))

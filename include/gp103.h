@@ -135,8 +135,10 @@ enum {
     GP103_FIELD_FP32 = 0,     /* cosine / sine transforms as float32 CUDA-core GEMMs (any grid) */
     GP103_FIELD_BF16X3 = 1,   /* tensor cores (tcgen05), bf16 operands split in 2 terms, 3 products, fp32 accumulation */
     GP103_FIELD_BF16X6 = 2,   /* tensor cores, bf16 operands split in 3 terms, 6 products (error ~1e-7 of the max) */
-    GP103_FIELD_F16X3 = 3     /* tensor cores, float16 operands split in 2 terms, 3 products, each row's 64-wide chunk
+    GP103_FIELD_F16X3 = 3,    /* tensor cores, float16 operands split in 2 terms, 3 products, each row's 64-wide chunk
                                * of K scaled by its own power of two (error ~1e-7 of the max, half the products) */
+    GP103_FIELD_TF32X3 = 4    /* tensor cores (tcgen05 kind::tf32), float32 operands split in 2 tf32 terms (each the
+                               * value rounded to 10 mantissa bits, then the rest), 3 products, fp32 accumulation */
 };
 
 /* Phases of gp103_pass. */

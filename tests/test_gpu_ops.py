@@ -252,7 +252,9 @@ def _density_plane(nb, seed=0):
                                          (256, native.FIELD_F16X3, 1e-6), (1024, native.FIELD_F16X3, 1e-6),
                                          (1024, native.FIELD_BF16X6, 1e-6), ((256, 512), native.FIELD_F16X3, 1e-6),
                                          ((512, 256), native.FIELD_F16X3, 1e-6),
-                                         ((256, 384), native.FIELD_F16X3, 1e-6)])
+                                         ((256, 384), native.FIELD_F16X3, 1e-6), (128, native.FIELD_TF32X3, 1e-6),
+                                         (256, native.FIELD_TF32X3, 1e-6), (1024, native.FIELD_TF32X3, 1e-6),
+                                         ((256, 384), native.FIELD_TF32X3, 1e-6)])
 def test_field_matches_fp64(nb, mode, tol):
     """The field against its float64 statement and the reference's mirrored FFT. f16x3 folds the transforms on grids
     whose sides are multiples of 256 (256, 1024, 256 x 512, 512 x 256: the x and y folds each on a grid where the

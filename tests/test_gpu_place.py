@@ -30,7 +30,8 @@ def _positions(prob, seed=0):
     return np.clip(pos, gr.pos_lo, gr.pos_hi).astype(np.float32)
 
 
-@pytest.mark.parametrize("field,tol", [("bf16x6", 1e-5), ("f16x3", 1e-5), ("fp32", 1e-5), ("bf16x3", 1e-4)])
+@pytest.mark.parametrize("field,tol", [("bf16x6", 1e-5), ("f16x3", 1e-5), ("fp32", 1e-5), ("bf16x3", 1e-4),
+                                       ("tf32x3", 1e-5)])
 def test_fused_gradient_matches_oracle(field, tol):
     from autoplace_gb300.engine import Placer
     prob = _problem()
@@ -96,7 +97,7 @@ def test_level_matches_reference_run(gold):
     assert abs(h - float(g["hpwl"])) <= 0.005 * float(g["hpwl"])
 
 
-@pytest.mark.parametrize("field", ["bf16x6", "f16x3", "bf16x3"])
+@pytest.mark.parametrize("field", ["bf16x6", "f16x3", "bf16x3", "tf32x3"])
 def test_level_matches_oracle_with_tensor_core_field(field):
     """10,000 cells on a 128 x 128 force grid: GPU run (tensor-core field) vs the oracle's CPU run."""
     from autoplace_gb300.engine import Placer

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 # f16x3's two float16 terms are exact to 2^-22 of their 64-wide chunk's largest value, bf16x6's three bf16 terms to
 # 2^-24 of each value: bf16x6 holds the 1e-6 bar at every pass, f16x3 (the faster default) 1.5e-6
-MODES = [("f16x3", 1.5e-6), ("bf16x6", 1e-6), ("bf16x3", 3e-5), ("fp32", 1e-6)]
+MODES = [("f16x3", 1.5e-6), ("bf16x6", 1e-6), ("bf16x3", 3e-5), ("tf32x3", 1e-6), ("fp32", 1e-6)]
 
 
 @pytest.fixture(scope="module")
