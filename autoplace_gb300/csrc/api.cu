@@ -210,7 +210,7 @@ extern "C" int gp103_plan_offsets(size_t* out, int n) {
         OFF(field_work), OFF(ex), OFF(ey), OFF(u), OFF(v), OFF(g), OFF(best), OFF(cur), OFF(S), OFF(T), OFF(kp),
         OFF(c), OFF(pin_grad), OFF(map), OFF(jmap), OFF(red), OFF(counters), OFF(pin_slot), OFF(net_split),
         OFF(order), OFF(order_counts), OFF(order_cursor), OFF(net_mid), OFF(net_two), OFF(net_three),
-        OFF(field_shift), OFF(net_g8), OFF(net_g16)};
+        OFF(field_shift), OFF(net_g8), OFF(net_g16), OFF(wa_long_share)};
 #undef OFF
     const int count = (int)(sizeof(off) / sizeof(off[0]));
     for (int i = 0; i < count && i < n; i++) out[i] = off[i];
@@ -243,6 +243,7 @@ static int check_plan(const gp103_plan* p) {
     REQUIRE(p->net_three == 0 || (p->net_two >= 0 && p->net_two <= p->net_three && p->net_three <= p->net_split &&
                                   2LL * p->net_two + 3LL * (p->net_three - p->net_two) <= (long long)p->num_pins));
     REQUIRE(p->pin_slot || p->cell_pin || p->num_pins == 0);
+    REQUIRE(p->wa_long_share >= 0 && p->wa_long_share <= 99);
     REQUIRE((p->order == nullptr) == (p->order_counts == nullptr) && (p->order == nullptr) == (p->order_cursor == nullptr));
     if (p->field_mode != GP103_FIELD_FP32 && !field_tc_supported(p->nbx, p->nby)) return GP103_ERR_SHAPE;
     return GP103_OK;
@@ -420,6 +421,7 @@ static WaJob wa_job(const gp103_plan* p) {
     w.gamma = p->kp;
     w.pin_grad = (float2*)p->pin_grad;
     w.red = reduce_slot(p->red, p->counters, R_WA);
+    w.long_share = p->wa_long_share;
     return w;
 }
 

@@ -50,6 +50,7 @@ struct WaJob {
     float2* pin_grad;
     float2* out;            // per-net (WA, HPWL), may be null
     Reduce red;             // (WA, HPWL) totals; red.partials == nullptr: none
+    int long_share;         // percent of the fused launch's blocks on the long nets (0: GP103_OPT_WA_FUSED)
 };
 
 struct ScatterJob {

@@ -385,7 +385,8 @@ int launch_wa_net(const WaJob& j, cudaStream_t s) {
     const bool inline_long = j.split == j.num_nets;     // any order: long nets where they are met
     static const int res_short = resident_blocks(wa_short_kernel<false>, 256);
     static const int res_long = resident_blocks(wa_long_kernel, 256);
-    const int pct = wa_long_share();
+    // the plan's share where it gives one, while the process option has the launch fused (0 there: two launches)
+    const int pct = wa_long_share() > 0 && j.long_share > 0 ? j.long_share : wa_long_share();
     if (pct > 0 && !inline_long && chunks > 0 && longs > 0) {
         // one resident wave: pct % of its blocks on the long nets, the rest on the short ones
         static const int res = resident_blocks(wa_fused_kernel, 256);

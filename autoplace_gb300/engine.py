@@ -70,6 +70,16 @@ def launches():
     return native.launch_count() - _GRAPH_LAUNCHES["captured"] + _GRAPH_LAUNCHES["replayed"]
 
 
+def wa_long_share(num_pins, first_long_pin):
+    """The share (percent) of the fused WA launch's blocks given to the long nets (9 pins or more), from the share f
+    of the pins they hold: 30 + 60 f, within 40 .. 75. Measured best shares: 50-55 on the 1.2M-cell netlist
+    (f = 0.38: 53 here), 60-65 on its clusters (f = 0.53: 62)."""
+    if num_pins <= 0:
+        return 0
+    f = (num_pins - first_long_pin) / float(num_pins)
+    return int(min(75, max(40, round(30 + 60 * f))))
+
+
 def field_mode(mode, nbx, nby):
     """The field mode a grid of nbx x nby bins runs in: `mode`, or fp32 where the tensor-core field cannot tile the
     grid (gp103_plan_sizes answers GP103_ERR_SHAPE)."""
@@ -248,6 +258,7 @@ class Placer(object):
         # the default partition of the long nets: 9-16 pins by 4 lanes, longer ones a warp each (the 8- and 16-lane
         # groups of 17-32 and 33-64 pins are an autotuner choice: tune.apply_wa)
         pl.net_g8 = pl.net_g16 = 0
+        pl.wa_long_share = wa_long_share(P, int(self.net_start[pl.net_split]) if P else 0)
         self.plan = pl
         self._ref = ctypes.byref(pl)
 

@@ -286,11 +286,21 @@ def cluster_inputs(coarse, prob, device="cuda", stream=None):
     g = Graph(cp.csr, K, device=device, stream=stream)
     with torch.cuda.stream(stream):
         area = torch.as_tensor(synth.areas(cp.node_size[:K]).astype(np.float32)).to(device)
-        cell_pins = np.asarray(prob.nl.cell_pins, np.float64)
-        pin_count = torch.as_tensor(np.bincount(coarse.cid, weights=cell_pins, minlength=K).astype(np.float32)).to(
-            device)
-    x = g.features(area, prob.nl.width, prob.nl.height, pin_count)
+        # the member cells' pins of each cluster, summed on the device (whole numbers: any order gives the same sums)
+        pin_count = torch.zeros(max(K, 1), dtype=torch.float32, device=device)
+        pin_count.index_add_(0, coarse.cid_dev.to(device=device, dtype=torch.long), _cell_pins(prob, device))
+    x = g.features(area, prob.nl.width, prob.nl.height, pin_count[:K])
     return g, x
+
+
+def _cell_pins(prob, device):
+    """Pins of every movable cell (all nets) as a float32 device tensor, uploaded once per problem."""
+    dev = torch.device(device)
+    got = prob.__dict__.get("_cell_pins_dev")
+    if got is None or got.device != dev:
+        got = torch.as_tensor(np.asarray(prob.nl.cell_pins, np.float32)).to(dev)
+        prob.__dict__["_cell_pins_dev"] = got
+    return got
 
 
 class Proposal(object):
@@ -303,10 +313,14 @@ class Proposal(object):
         self.net = Net(model["params"], device=self.dev)
         self.lam_scale = float(model.get("lam_scale", 1.0))
         self.last = None
+        self._pass = None           # the forward workspace, kept for the next design of at most its size
 
     def positions(self, coarse, prob, stream):
         g, x = cluster_inputs(coarse, prob, self.dev, stream)
-        y = Pass.for_graph(self.net, g).forward(g, x)
+        ps = self._pass
+        if ps is None or ps.stream is not stream or g.K > ps.cap[0] or g.N > ps.cap[1]:
+            ps = self._pass = Pass.for_graph(self.net, g)
+        y = ps.forward(g, x)
         return y, g
 
     def applies(self, prob):

@@ -44,6 +44,7 @@ class Plan(ctypes.Structure):
         ("net_mid", _i), ("net_two", _i), ("net_three", _i),
         ("field_shift", _f),
         ("net_g8", _i), ("net_g16", _i),
+        ("wa_long_share", _i),
     ]
 
 

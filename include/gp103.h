@@ -213,6 +213,11 @@ typedef struct {
     /* nets [net_mid, net_g8) have 17 to 32 pins (eight lanes each, four nets per warp), [net_g8, net_g16) 33 to 64
      * (sixteen lanes each, two per warp), the rest a warp each (net_g16 = 0: every net from net_mid on a warp) */
     int net_g8; int net_g16;
+    /* the share (percent, 1 .. 99) of the fused WA launch's blocks that take the long nets (net_split on) in this
+     * plan's passes; 0: the process option GP103_OPT_WA_FUSED's (which, at 0, makes every plan's WA two launches).
+     * The best share follows the share of the pins on long nets: measured at 1.2M cells (38 % of the pins on nets of
+     * 9 pins or more) 50-55, on its 272k clusters (53 %) 60-65. */
+    int wa_long_share;
 } gp103_plan;
 
 typedef struct {
