@@ -311,7 +311,8 @@ static OrderJob order_job(const gp103_plan* p) {
 }
 
 static int density_and_field(const gp103_plan* p, const float* pos_a, const float* pos_b, const int* sel,
-                             const int* order, cudaStream_t s, const WaJob* wa = nullptr) {
+                             const int* order, cudaStream_t s, const WaJob* wa = nullptr,
+                             cudaEvent_t before_field = nullptr) {
     const size_t nb = (size_t)p->nbx * p->nby;
     ScatterJob sj = {};
     sj.pos_a = (const float2*)pos_a;
@@ -382,6 +383,7 @@ static int density_and_field(const gp103_plan* p, const float* pos_a, const floa
     }
     TRY(launch_post_plain(posts, p->jnbx > 0 ? 2 : 1, s));
     if (wa) TRY(launch_wa_net(*wa, s));                     // (see run_pass)
+    if (before_field && cudaStreamWaitEvent(s, before_field, 0) != cudaSuccess) return GP103_ERR_CUDA;
     return run_field(p, nullptr, s);
 }
 
@@ -457,8 +459,9 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
                     cudaEvent_t fork, cudaEvent_t join) {
     TRY(check_plan(plan));
     const gp103_plan* p = plan;
-    const int phase = phase_flags & ~GP103_PASS_SORT;
+    const int phase = phase_flags & ~(GP103_PASS_SORT | GP103_PASS_JOIN_FIELD);
     const bool sort = (phase_flags & GP103_PASS_SORT) != 0;
+    const bool join_field = (phase_flags & GP103_PASS_JOIN_FIELD) != 0;
     REQUIRE(phase == GP103_PHASE_START || phase == GP103_PHASE_DENSITY);
     REQUIRE(!sort || (phase == GP103_PHASE_DENSITY && p->order != nullptr));
     REQUIRE(p->u[0] && p->u[1] && p->v[0] && p->v[1] && p->g[0] && p->g[1] && p->cur && p->lo && p->hi);
@@ -517,8 +520,9 @@ static int run_pass(const gp103_plan* plan, int phase_flags, cudaStream_t stream
         TRY(launch_gather(g, stream));
         return launch_control_start(p->T, p->kp, r_grad, pre, p->cur, field_error_flag(p), stream);
     }
-    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream, wa_late ? &w : nullptr));
-    if (split && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
+    TRY(density_and_field(p, p->v[0], p->v[1], p->cur, ordered ? p->order : nullptr, stream, wa_late ? &w : nullptr,
+                          split && join_field ? join : nullptr));
+    if (split && !join_field && cudaStreamWaitEvent(stream, join, 0) != cudaSuccess) return GP103_ERR_CUDA;
     g.ex = p->ex;
     g.ey = p->ey;
     g.weight_p = p->kp + 1;

@@ -80,6 +80,16 @@ def wa_long_share(num_pins, first_long_pin):
     return int(min(75, max(40, round(30 + 60 * f))))
 
 
+def side_stream(stream):
+    """A stream other than `stream` for the WA kernels of split passes. torch hands out its streams from a small
+    pool, round robin, so a new torch.cuda.Stream can be `stream` itself: draw until it is not."""
+    for _ in range(64):
+        s = torch.cuda.Stream(stream.device)
+        if s.cuda_stream != stream.cuda_stream:
+            return s
+    raise RuntimeError("no CUDA stream other than the pass's own")
+
+
 def field_mode(mode, nbx, nby):
     """The field mode a grid of nbx x nby bins runs in: `mode`, or fp32 where the tensor-core field cannot tile the
     grid (gp103_plan_sizes answers GP103_ERR_SHAPE)."""
@@ -124,16 +134,17 @@ def pinned_inputs(prob):
 
 class Placer(object):
     def __init__(self, prob, field="f16x3", device=None, check_every=16, use_graphs=True, stream=None,
-                 sort_every=None, host=None, handover_gamma=0.0, split=False):
+                 sort_every=None, host=None, handover_gamma=0.0, split=False, side=None):
         """host: optional {name: pinned CPU tensor} holding the problem's arrays (pinned_inputs), uploaded instead
         of the Problem's numpy arrays. handover_gamma: a run on clusters stops ("handover") once its smoothing is
         down to this (the smoothing the cells start with); 0 = never.
         A tensor-core field (f16x3, bf16x6, bf16x3) needs a grid of multiples of 128 bins per side: on a smaller grid
         (clusters, small designs) the field runs in fp32.
-        split: density passes with the WA kernels on a second stream, beside the density map and the field
-        (gp103_pass_split); the same results. Off by default: at c2 it measured 151.7 ms per placement against
-        146.8 ms in one stream (the fork and join replace programmatic launch edges; the two halves gain nothing
-        from sharing the GPU)."""
+        split: density passes with the WA kernels on a second stream (`side`, or one drawn by side_stream), beside
+        the density map and the field (gp103_pass_split); the same results. Off for a Placer of its own; Flow turns
+        it on for both levels (at the 1.2M-cell netlist: the clusters' level 38.2 -> 35.5 ms, the cells' 46.3 ->
+        44.9 ms). split="field": the passes wait for the WA kernels before the field instead of before the gather
+        (GP103_PASS_JOIN_FIELD; the same time at the 1.2M-cell netlist)."""
         self.p = prob
         self.dev = torch.device(device or "cuda")
         self.mode = field_mode(native.FIELD_MODES[field] if isinstance(field, str) else int(field),
@@ -145,7 +156,12 @@ class Placer(object):
         self.sort_every = max(int(sort_every or check_every), 1)
         self.stream = stream or torch.cuda.Stream(self.dev)
         self.split = bool(split)
-        self.side = torch.cuda.Stream(self.dev) if self.split else None
+        # where the passes wait for the WA kernels of the side stream: before the gather (split=True) or before the
+        # field (split="field": the WA kernels share the GPU with the density map only)
+        self.split_join = "field" if split == "field" else "gather"
+        self.side = (side or side_stream(self.stream)) if self.split else None
+        if self.side is not None and self.side.cuda_stream == self.stream.cuda_stream:
+            raise ValueError("the side stream of a split pass must differ from the pass's stream")
         self._events = []
         if self.split:
             for _ in range(2):
@@ -315,6 +331,8 @@ class Placer(object):
             sort = phase == native.PHASE_DENSITY and i % self.sort_every == 0
             flags = phase | (native.PASS_SORT if sort else 0)
             if split and phase == native.PHASE_DENSITY:
+                if self.split_join == "field":
+                    flags |= native.PASS_JOIN_FIELD
                 native.call("gp103_pass_split", self._ref, flags, s, self.side.cuda_stream, self._events[0],
                             self._events[1])
             else:

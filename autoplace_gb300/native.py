@@ -17,6 +17,7 @@ FIELD_MODES = {"fp32": FIELD_FP32, "bf16x3": FIELD_BF16X3, "bf16x6": FIELD_BF16X
                "tf32x3": FIELD_TF32X3}
 PHASE_START, PHASE_DENSITY = 0, 1
 PASS_SORT = 0x100
+PASS_JOIN_FIELD = 0x200
 T = dict(alpha=0, a=1, iter=2, loop_it=3, done=4, stop=5, accept=6, hpwl=7, wa=8, evals=9, nwa=10, start_tol=11,
          inner=12, ring=16)
 T_SIZE = 32

@@ -145,7 +145,10 @@ enum {
 enum {
     GP103_PHASE_START = 0,    /* wirelength-only start (density weight 0), src/run_placement.py:60-65 */
     GP103_PHASE_DENSITY = 1,  /* the device loop of src/gpu_loop.py:58-68 */
-    GP103_PASS_SORT = 0x100   /* or-ed to GP103_PHASE_DENSITY: refresh plan->order from this pass's positions */
+    GP103_PASS_SORT = 0x100,  /* or-ed to GP103_PHASE_DENSITY: refresh plan->order from this pass's positions */
+    GP103_PASS_JOIN_FIELD = 0x200 /* or-ed, gp103_pass_split only: `stream` waits for the WA kernels before the field
+                                   * instead of before the gather (the WA kernels share the GPU with the density map
+                                   * only; the field has all of it) */
 };
 
 /* Layout of the start-phase state T [32] (float64): what NesterovOptimizer (alpha, a) and

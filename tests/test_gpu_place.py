@@ -67,18 +67,27 @@ def test_fused_pass_is_repeatable():
 
 
 def test_split_pass_matches_single_stream():
-    """The WA kernels on a second stream beside the density map and the field (gp103_pass_split): the same run, bit
-    for bit, graphs or not."""
+    """The WA kernels on a second stream beside the density map and the field (gp103_pass_split), joined before the
+    gather or before the field (GP103_PASS_JOIN_FIELD): the same run, bit for bit, graphs or not."""
     from autoplace_gb300.engine import Placer
     prob = _problem(cells=6000, nb=128, judge=64, seed=3)
     pos0 = synth.init_positions(prob.nl, prob.num_nodes, seed=1)
     res = []
-    for split, graphs in ((False, True), (True, True), (True, False)):
+    for split, graphs in ((False, True), (True, True), (True, False), ("field", True), ("field", False)):
         r = Placer(prob, field="f16x3", check_every=8, split=split, use_graphs=graphs).run(pos0)
         res.append((r["iters"], r["hpwl"], r["overflow"], r["pos"].cpu().numpy()))
     for r in res[1:]:
         assert r[:3] == res[0][:3]
         assert np.array_equal(r[3], res[0][3])
+
+
+def test_side_stream_never_the_pass_stream():
+    """torch hands out streams round robin from a small pool: however many were drawn before, a split Placer's side
+    stream is not its own stream (gp103_pass_split refuses side == stream)."""
+    from autoplace_gb300.engine import side_stream
+    s = torch.cuda.Stream()
+    for _ in range(100):
+        assert side_stream(s).cuda_stream != s.cuda_stream
 
 
 def test_level_matches_reference_run(gold):

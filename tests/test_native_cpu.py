@@ -47,6 +47,21 @@ def test_plan_sizes_and_shape_errors():
     native.call("gp103_plan_sizes", 96, 96, native.FIELD_FP32, ctypes.byref(s))
     with pytest.raises(RuntimeError, match="invalid argument"):
         native.call("gp103_plan_sizes", 0, 96, native.FIELD_FP32, ctypes.byref(s))
+    # tf32x3: two float32 term planes per operand (8 bytes an element), on the tensor cores' grids only
+    native.call("gp103_plan_sizes", 256, 256, native.FIELD_TF32X3, ctypes.byref(s))
+    assert s.field_const > 6 * 256 * 256 * 8 and s.field_work > 6 * 256 * 256 * 8
+    assert native.lib().gp103_plan_sizes(96, 96, native.FIELD_TF32X3, ctypes.byref(s)) == native.ERR_SHAPE
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        native.call("gp103_plan_sizes", 256, 256, 5, ctypes.byref(s))
+
+
+def test_wa_long_share_rule():
+    """The fused WA launch's long-net share from the share of the pins on long nets: 30 + 60 f within 40 .. 75."""
+    from autoplace_gb300 import engine
+    assert engine.wa_long_share(0, 0) == 0
+    assert engine.wa_long_share(1000, 620) == 53          # 38 % of the pins on long nets (the 1.2M-cell netlist)
+    assert engine.wa_long_share(1000, 470) == 62          # 53 % (its clusters)
+    assert engine.wa_long_share(1000, 1000) == 40 and engine.wa_long_share(1000, 0) == 75
 
 
 def test_argument_errors_without_gpu():
