@@ -165,7 +165,8 @@ def c2_states(c2):
 
 
 @pytest.mark.parametrize("state", ["start", "mid", "final"])
-@pytest.mark.parametrize("mode,tol", [(native.FIELD_F16X3, 1e-6), (native.FIELD_BF16X6, 1e-6)])
+@pytest.mark.parametrize("mode,tol", [(native.FIELD_F16X3, 1e-6), (native.FIELD_BF16X6, 1e-6),
+                                      (native.FIELD_TF32X3, 1e-6)])
 def test_full_size_field_error_on_real_states(c2, c2_states, state, mode, tol):
     """The tensor-core field of the 1024 x 1024 force grid against float64 (the cosine-transform statement of the
     reference's mirrored FFT) on the densities of a real run: max |E - E64| / max |E64| <= 1e-6. The density plane
