@@ -55,6 +55,17 @@ class Stream(object):
         return self.buf
 
 
+def seeded_uniform(seed, count, device="cuda", stream=None):
+    """torch.rand(count, generator=torch.Generator().manual_seed(seed)) (the CPU generator's stream, the same bits)
+    made on the device (gp103_seeded_uniform). -> float32 device tensor [count]."""
+    dev = torch.device(device)
+    stream = stream or torch.cuda.current_stream(dev)
+    with torch.cuda.stream(stream):
+        out = torch.empty(max(int(count), 1), dtype=torch.float32, device=dev)
+    native.call("gp103_seeded_uniform", int(seed), int(count), ctypes.c_void_p(out.data_ptr()), stream.cuda_stream)
+    return out[:int(count)]
+
+
 def device_pair_bound(pin_net, num_nets, max_degree=8):
     """pair_bound of the pins' nets already on the device (int32 [P]), one host read."""
     deg = torch.bincount(pin_net.long(), minlength=max(int(num_nets), 1))
@@ -80,18 +91,18 @@ def prepare(prob, device="cuda", stream=None, max_degree=8):
         bound = device_pair_bound(pn, nl.num_nets, max_degree)
     size = np.asarray(prob.node_size[:n], np.float32)
     area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
-    heads = Stream(o.seed, n)                  # (extended n draws at a time when the rounds need more)
-    heads.upto(4 * n)
-    gen = torch.Generator().manual_seed(int(o.seed))
+    # the seeded draws, made on the device: the heads' stream (six per cell; the 12 rounds of the 1.2M-cell netlist
+    # read 4.07 per cell; a longer need extends it from the host's generator) and expand's draws, which are the same
+    # stream's start (the reference seeds expand's generator with the same seed: its first 2 n values)
+    heads = Stream(o.seed, n)
+    heads_dev = seeded_uniform(o.seed, 6 * n, dev, stream)
     with torch.cuda.stream(stream):
         area_dev = torch.as_tensor(area).to(dev, non_blocking=True)
         size_dev = torch.as_tensor(size).to(dev, non_blocking=True)
-        draws_dev = torch.rand(n, 2, generator=gen).to(dev, non_blocking=True)
-        heads_dev = torch.as_tensor(heads.buf[:4 * n]).to(dev, non_blocking=True)
     return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, area_dev=area_dev, size_dev=size_dev,
                            limits=limits(area, o.cluster_ratio), pair_bound=max(bound, 1),
                            num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, heads_dev=heads_dev,
-                           expand_draws=draws_dev, size=size)
+                           expand_draws=heads_dev[:2 * n].view(n, 2), size=size)
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",

@@ -537,10 +537,72 @@ __global__ void single_size_kernel(const int* cid, int n, const unsigned char* s
     }
 }
 
+// ----------------------------------------------------------------------------- seeded draws
+// The float32 stream of torch.rand(count, generator=torch.Generator().manual_seed(seed)) on the CPU, which the
+// reference's clustering and expand draw from: the MT19937 generator (Matsumoto and Nishimura, 1998) with its
+// standard initialisation from the seed's low 32 bits, each tempered 32-bit output x giving (x mod 2^24) 2^-24.
+// One block of 624 threads, one state word each. A twist of the state runs in three parallel phases: words
+// [0, 227) read only words of the old state, [227, 454) also the first phase's new words (i + 397 - 624), and
+// [454, 624) the second phase's (and word 0, new, for word 623); each phase reads, waits, then writes. Then every
+// thread tempers its word and writes one value.
+constexpr int MT_N = 624, MT_M = 397;
+constexpr unsigned MT_UPPER = 0x80000000u, MT_LOWER = 0x7fffffffu, MT_A = 0x9908b0dfu;
+
+__device__ __forceinline__ unsigned mt_word(unsigned cur, unsigned next, unsigned far) {
+    const unsigned y = (cur & MT_UPPER) | (next & MT_LOWER);
+    return far ^ (y >> 1) ^ ((y & 1u) ? MT_A : 0u);
+}
+
+__global__ void __launch_bounds__(MT_N) mt_uniform_kernel(unsigned long long seed, long long count, float* out) {
+    __shared__ unsigned mt[MT_N];
+    pdl_wait();
+    const int i = threadIdx.x;
+    if (i == 0) {
+        unsigned v = (unsigned)(seed & 0xffffffffull);
+        mt[0] = v;
+        for (int k = 1; k < MT_N; k++) {
+            v = 1812433253u * (v ^ (v >> 30)) + (unsigned)k;
+            mt[k] = v;
+        }
+    }
+    __syncthreads();
+    const bool a = i < MT_N - MT_M, b = i >= MT_N - MT_M && i < 2 * (MT_N - MT_M), c = i >= 2 * (MT_N - MT_M);
+    for (long long base = 0; base < count; base += MT_N) {
+        unsigned w = 0u;
+        if (a) w = mt_word(mt[i], mt[i + 1], mt[i + MT_M]);
+        __syncthreads();
+        if (a) mt[i] = w;
+        __syncthreads();
+        if (b) w = mt_word(mt[i], mt[i + 1], mt[i + MT_M - MT_N]);
+        __syncthreads();
+        if (b) mt[i] = w;
+        __syncthreads();
+        if (c) w = mt_word(mt[i], mt[(i + 1) % MT_N], mt[i + MT_M - MT_N]);
+        __syncthreads();
+        if (c) mt[i] = w;
+        __syncthreads();
+        unsigned y = mt[i];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        if (base + i < count) out[base + i] = (float)(y & 0xffffffu) * 5.9604644775390625e-8f;   // 2^-24
+    }
+}
+
 }  // namespace
 }  // namespace gp103
 
 using namespace gp103;
+
+extern "C" int gp103_seeded_uniform(unsigned long long seed, long long count, float* out, cudaStream_t s) {
+    if (count < 0 || (count > 0 && !out)) return GP103_ERR_ARG;
+    if (count == 0) return GP103_OK;
+    if (launch_k(mt_uniform_kernel, dim3(1), dim3(MT_N), 0, s, seed, count, out) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
 
 extern "C" int gp103_cluster_members(const int* cid, int n, int num, const long long* carea, const float* size,
                                      int* count, unsigned char* single, float* csize, cudaStream_t s) {

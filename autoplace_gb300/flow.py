@@ -49,12 +49,13 @@ class Flow(object):
         # the cells' level 46.3 -> 44.9 ms
         self.split = bool(split)
         self.side = side_stream(self.stream) if self.split else None
+        # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws);
+        # first, so that its seeded draws (on background threads) run beside the cells' Placer's set-up
+        self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
         self.fine = Placer(prob, field=field, host=host, split=self.split, side=self.side, **self.kw)
         self.last_coarse = None
         self.keep_coarse_placer = False             # keep the clusters' Placer of the last run (last_cplacer)
         self.last_cplacer = None
-        # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws)
-        self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
 
     def run(self, pos0, log=None, start=None, fallback=True):
         """Place from pos0 ([num_nodes, 2], movable cells then fillers). -> dict of statistics as the reference's

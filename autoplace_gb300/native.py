@@ -86,6 +86,7 @@ _SIGS = {
     "gp103_coarse_pins_scratch": ([_i], ctypes.c_size_t),
     "gp103_coarse_pins": ([_vp, _vp, _vp, _i, _i, _vp, _i, _vp, _vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_expand": ([_vp] * 5 + [_i, _vp, _vp], _i),
+    "gp103_seeded_uniform": ([ctypes.c_ulonglong, ctypes.c_longlong, _vp, _vp], _i),
     "gp103_cluster_members": ([_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_pass_split": ([ctypes.POINTER(Plan), _i, _vp, _vp, _vp, _vp], _i),
     "gp103_event_create": ([ctypes.POINTER(_vp)], _i),

@@ -346,6 +346,12 @@ int gp103_coarse_pins(const int* pin_cell, const float* pin_off, const int* pin_
 int gp103_expand(const float* cpos, const int* cid, const float* csize, const float* size, const float* draws, int n,
                  float* pos, cudaStream_t stream);
 
+/* The seeded draws of the clustering's heads (src/cluster.py:62, a share of 0.5) and of expand (src/cluster.py:142),
+ * on the device: out[0 .. count) = the float32 values of torch.rand(count, generator=torch.Generator().manual_seed(
+ * seed)) on the CPU, the same bits (the generator's MT19937 stream, each 32-bit output x giving (x mod 2^24) 2^-24;
+ * consecutive torch.rand calls on one generator continue this one stream). One block; count any size. */
+int gp103_seeded_uniform(unsigned long long seed, long long count, float* out, cudaStream_t stream);
+
 /* Problem build on the device: the arrays AutoPlace builds once per level before the first iteration.
  *
  * gp103_build_csr: the optimised pin set (Wirelength.__init__ net filter and Wirelength._pin_set,

@@ -32,6 +32,19 @@ def _edges(pin_cell, pin_net, n):
     return i, col.cpu().numpy()[:m], w.cpu().numpy()[:m], int(counts[1]), E
 
 
+@pytest.mark.parametrize("seed", [0, 1, 12345, 2**40 + 7])
+def test_seeded_uniform_matches_torch_cpu(seed):
+    """gp103_seeded_uniform: torch.rand's CPU stream of a seeded generator (MT19937, 24-bit floats), the same bits, at
+    counts on both sides of the 624-word state and at millions of values; consecutive calls continue one stream."""
+    for count in (1, 623, 624, 625, 3 * 624 + 5, 2_000_003):
+        dev = cluster.seeded_uniform(seed, count).cpu().numpy()
+        ref = torch.rand(count, generator=torch.Generator().manual_seed(seed)).numpy()
+        assert np.array_equal(dev, ref), (seed, count)
+    g = torch.Generator().manual_seed(seed)
+    two = np.concatenate([torch.rand(1000, generator=g).numpy(), torch.rand(500, 2, generator=g).numpy().ravel()])
+    assert np.array_equal(cluster.seeded_uniform(seed, 2000).cpu().numpy(), two)
+
+
 def test_pair_edges_match_reference(gold_cluster):
     g = gold_cluster
     i, j, w, found, E = _edges(g["pin_cell"], g["pin_net"], int(g["n"]))
