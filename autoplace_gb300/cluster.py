@@ -37,6 +37,17 @@ def limits(area, ratio):
     return int(big), int(math.floor(float(cap)))
 
 
+def device_limits(area_dev, ratio):
+    """limits() of the cells' areas on the device (int64 [n]): the integer sums there (two host reads), the float32
+    scalar arithmetic of the reference on the CPU as limits() does it -> the same (big, cap)."""
+    n = int(area_dev.numel())
+    big = 20 * int(area_dev.sum()) // n
+    small = area_dev < big
+    s, count = (int(x) for x in torch.stack([(area_dev * small).sum(), small.sum()]).cpu())
+    cap = 3 * ratio * torch.tensor(s) // (2 * count)
+    return int(big), int(math.floor(float(cap)))
+
+
 class Stream(object):
     """The seeded CPU generator's float32 draws as one stream (torch.rand of torch.Generator().manual_seed(seed)):
     consecutive torch.rand calls on a generator give the consecutive pieces of one long draw, so the stream is drawn
@@ -89,20 +100,25 @@ def prepare(prob, device="cuda", stream=None, max_degree=8):
             pn = torch.as_tensor(np.asarray(nl.pin_net, np.int32)).to(dev, non_blocking=True)
             po = torch.as_tensor(np.asarray(nl.pin_off, np.float32)).to(dev, non_blocking=True)
         bound = device_pair_bound(pn, nl.num_nets, max_degree)
-    size = np.asarray(prob.node_size[:n], np.float32)
-    area = np.round((size[:, 0] * size[:, 1]).astype(np.float64) * 1024).astype(np.int64)
     # the seeded draws, made on the device: the heads' stream (six per cell; the 12 rounds of the 1.2M-cell netlist
     # read 4.07 per cell; a longer need extends it from the host's generator) and expand's draws, which are the same
     # stream's start (the reference seeds expand's generator with the same seed: its first 2 n values)
     heads = Stream(o.seed, n)
     heads_dev = seeded_uniform(o.seed, 6 * n, dev, stream)
     with torch.cuda.stream(stream):
-        area_dev = torch.as_tensor(area).to(dev, non_blocking=True)
-        size_dev = torch.as_tensor(size).to(dev, non_blocking=True)
-    return SimpleNamespace(pins=(pc, pn), pin_off=po, area=area, area_dev=area_dev, size_dev=size_dev,
-                           limits=limits(area, o.cluster_ratio), pair_bound=max(bound, 1),
+        on_dev = getattr(prob, "node_size_dev", None)
+        if torch.is_tensor(on_dev) and on_dev.device == dev:
+            size_dev = on_dev[:n].float()
+        else:
+            size_dev = torch.as_tensor(np.asarray(prob.node_size[:n], np.float32)).to(dev, non_blocking=True)
+        # the areas in 1/1024 of a site area, rounded from the float32 area (the reference's, bit for bit: float32
+        # products, then exact float64 scaling and half-to-even rounding)
+        area_dev = torch.round((size_dev[:, 0] * size_dev[:, 1]).double() * 1024).long()
+        lim = device_limits(area_dev, o.cluster_ratio)
+    return SimpleNamespace(pins=(pc, pn), pin_off=po, area=None, area_dev=area_dev, size_dev=size_dev,
+                           limits=lim, pair_bound=max(bound, 1),
                            num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, heads_dev=heads_dev,
-                           expand_draws=heads_dev[:2 * n].view(n, 2), size=size)
+                           expand_draws=heads_dev[:2 * n].view(n, 2))
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
@@ -112,10 +128,13 @@ def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3
     stand in for the seeded generator (tests). dev_pins: (pin_cell, pin_net) already on the device as int32. prep:
     prepare()'s result for this design (pins, limits, pair bound, the seeded stream), made once per design.
     on_device: -> (cluster of every cell [n] int32, area of every cluster [K] int64) as device tensors instead."""
-    area = np.ascontiguousarray(area, np.int64)
-    n = len(area)
+    if prep is not None:                        # (the areas and limits on the device)
+        n = int(prep.area_dev.numel())
+    else:
+        area = np.ascontiguousarray(area, np.int64)
+        n = len(area)
     if n == 0:
-        return np.zeros(0, np.int64), area
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
     dev = torch.device(device)
     stream = stream or torch.cuda.current_stream(dev)
     s = stream.cuda_stream
@@ -220,7 +239,7 @@ def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
     P_ = len(nl.pin_cell)
     if prep is None:
         prep = prepare(prob, device=dev, stream=stream)
-    (pc, pn), po, size, area = prep.pins, prep.pin_off, prep.size, prep.area
+    (pc, pn), po, area = prep.pins, prep.pin_off, prep.area
     cd, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
                               prep=prep, on_device=True)
     num = int(carea.shape[0])

@@ -55,6 +55,20 @@ def test_plan_sizes_and_shape_errors():
         native.call("gp103_plan_sizes", 256, 256, 5, ctypes.byref(s))
 
 
+def test_device_limits_equal_host_limits():
+    """The clustering's merge limits from the areas as the device computes them (integer sums, then the reference's
+    float32 scalar arithmetic) equal the host statement's, here on CPU tensors."""
+    import numpy as np
+    import torch
+    from autoplace_gb300 import cluster
+    rng = np.random.default_rng(3)
+    for n, hi in ((10, 50), (100_000, 9 * 1024 * 10), (7, 3)):
+        area = rng.integers(1, hi, n).astype(np.int64)
+        area[: n // 50] *= 40                   # a few cells at or above the lone-cell bound
+        for ratio in (5.0, 3.0, 1.5):
+            assert cluster.device_limits(torch.as_tensor(area), ratio) == cluster.limits(area, ratio)
+
+
 def test_wa_long_share_rule():
     """The fused WA launch's long-net share from the share of the pins on long nets: 30 + 60 f within 40 .. 75."""
     from autoplace_gb300 import engine
