@@ -84,7 +84,7 @@ def device_pair_bound(pin_net, num_nets, max_degree=8):
     return int((d * (d - 1)).sum())
 
 
-def prepare(prob, device="cuda", stream=None, max_degree=8):
+def prepare(prob, device="cuda", stream=None, max_degree=8, draw_stream=None):
     """What a placement's clustering needs of its design, made once per design (like the cells' own uploads): the
     pins on the device (int32 cells and nets, float32 offsets: the device problem's own, else uploaded), the cells'
     areas and the merge limits, the pair bound, the heads' seeded stream drawn ahead (four draws per cell) and
@@ -104,7 +104,13 @@ def prepare(prob, device="cuda", stream=None, max_degree=8):
     # read 4.07 per cell; a longer need extends it from the host's generator) and expand's draws, which are the same
     # stream's start (the reference seeds expand's generator with the same seed: its first 2 n values)
     heads = Stream(o.seed, n)
-    heads_dev = seeded_uniform(o.seed, 6 * n, dev, stream)
+    # (on draw_stream when given: the draws, ~2 ms in one block, then run beside the caller's set-up on `stream`;
+    # coarse_problem waits for them before the first round)
+    heads_dev = seeded_uniform(o.seed, 6 * n, dev, draw_stream or stream)
+    ready = None
+    if draw_stream is not None:
+        ready = torch.cuda.Event()
+        ready.record(draw_stream)
     with torch.cuda.stream(stream):
         on_dev = getattr(prob, "node_size_dev", None)
         if torch.is_tensor(on_dev) and on_dev.device == dev:
@@ -118,7 +124,7 @@ def prepare(prob, device="cuda", stream=None, max_degree=8):
     return SimpleNamespace(pins=(pc, pn), pin_off=po, area=None, area_dev=area_dev, size_dev=size_dev,
                            limits=lim, pair_bound=max(bound, 1),
                            num_nets=int(nl.num_nets), seed=int(o.seed), heads=heads, heads_dev=heads_dev,
-                           expand_draws=heads_dev[:2 * n].view(n, 2))
+                           expand_draws=heads_dev[:2 * n].view(n, 2), draws_ready=ready)
 
 
 def cluster_cells(pin_cell, pin_net, area, ratio, seed, max_degree=8, per_head=3, max_rounds=12, device="cuda",
@@ -240,6 +246,9 @@ def coarse_problem(prob, device="cuda", stream=None, build="device", prep=None):
     if prep is None:
         prep = prepare(prob, device=dev, stream=stream)
     (pc, pn), po, area = prep.pins, prep.pin_off, prep.area
+    if getattr(prep, "draws_ready", None) is not None:
+        stream.wait_event(prep.draws_ready)         # the seeded draws, made on another stream
+        prep.draws_ready = None
     cd, carea = cluster_cells(nl.pin_cell, nl.pin_net, area, o.cluster_ratio, o.seed, device=device, stream=stream,
                               prep=prep, on_device=True)
     num = int(carea.shape[0])

@@ -51,7 +51,8 @@ class Flow(object):
         self.side = side_stream(self.stream) if self.split else None
         # what every placement's clustering needs of the design (pins on the device, areas, limits, seeded draws);
         # first, so that its seeded draws (on background threads) run beside the cells' Placer's set-up
-        self.prep = cluster.prepare(prob, device=self.dev, stream=self.stream) if prob.opts.cluster_ratio > 1 else None
+        self.prep = (cluster.prepare(prob, device=self.dev, stream=self.stream, draw_stream=self.side)
+                     if prob.opts.cluster_ratio > 1 else None)
         self.fine = Placer(prob, field=field, host=host, split=self.split, side=self.side, **self.kw)
         self.last_coarse = None
         self.keep_coarse_placer = False             # keep the clusters' Placer of the last run (last_cplacer)
