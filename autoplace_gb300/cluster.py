@@ -41,6 +41,8 @@ def device_limits(area_dev, ratio):
     """limits() of the cells' areas on the device (int64 [n]): the integer sums there (two host reads), the float32
     scalar arithmetic of the reference on the CPU as limits() does it -> the same (big, cap)."""
     n = int(area_dev.numel())
+    if n == 0:
+        return 0, 0
     big = 20 * int(area_dev.sum()) // n
     small = area_dev < big
     s, count = (int(x) for x in torch.stack([(area_dev * small).sum(), small.sum()]).cpu())
