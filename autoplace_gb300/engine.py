@@ -269,12 +269,15 @@ class Placer(object):
             setattr(pl, k, self._p(getattr(self, k)))
         native.call("gp103_field_constants", ctypes.byref(pl), self.stream.cuda_stream)
         # the one host synchronisation of the set-up: the net classes of the WA order (launch sizes of the passes)
-        (pl.net_split, pl.net_mid, pl.net_two, pl.net_three, self.net_g8,
-         self.net_g16) = (int(x) for x in split.cpu().tolist())
+        # and the first pin of the long nets (gathered on the device)
+        with torch.cuda.stream(self.stream):
+            first_long = self.net_start[split[0].long()].view(1)
+        (pl.net_split, pl.net_mid, pl.net_two, pl.net_three, self.net_g8, self.net_g16,
+         first_long) = (int(x) for x in torch.cat([split, first_long]).cpu().tolist())
         # the default partition of the long nets: 9-16 pins by 4 lanes, longer ones a warp each (the 8- and 16-lane
         # groups of 17-32 and 33-64 pins are an autotuner choice: tune.apply_wa)
         pl.net_g8 = pl.net_g16 = 0
-        pl.wa_long_share = wa_long_share(P, int(self.net_start[pl.net_split]) if P else 0)
+        pl.wa_long_share = wa_long_share(P, first_long)
         self.plan = pl
         self._ref = ctypes.byref(pl)
 
