@@ -423,6 +423,18 @@ class Placer(object):
             left.append(int(o.settle_iter) + 1 - int(Sh[SK["settled"]]))
         return max(min(left), 1)
 
+    def _handover_bound(self, Sh):
+        """A lower bound on the passes before a run on clusters stops for the hand-over (its smoothing down to
+        handover_gamma), or None when that stop is not bounded: with the accuracy rule a pass changes the smoothing by a
+        factor within [1/m, m], m = max(mu, 1/mu) <= 1.05 (mu within [1.05 x 0.95, 1.05]), so the smoothing needs at
+        least log(gam / handover_gamma) / log(1.05) more passes to reach it."""
+        if self.handover_gamma <= 0 or Sh[SK["lam"]] <= 0 or self.p.opts.wa_rule != "accuracy":
+            return None
+        g = float(Sh[SK["gam"]])
+        if g <= self.handover_gamma:
+            return 1
+        return max(int(math.log(g / self.handover_gamma) / math.log(1.0501)), 1)
+
     # ------------------------------------------------------------------ one level
     def run(self, pos0, log=None, resume=None):
         """Place from pos0 ([num_nodes, 2], host or device) to the stop. -> dict (reason, iters, start_iters, hpwl,
@@ -536,7 +548,9 @@ class Placer(object):
         logged = ctx["it0"] // o.log_freq
         # Batches of passes, each followed by an asynchronous copy of the state into pinned memory. While no stop can
         # come within two batches, the next batch is queued before the host waits for the state of the last one, so
-        # the GPU does not idle through the poll; near a predictable stop the host runs exactly the passes left.
+        # the GPU does not idle through the poll; near a predictable stop the host runs exactly the passes left. Near a
+        # possible hand-over (its bound below two batches) no batch is queued ahead: a queued batch after the stop
+        # would be check_every passes that change nothing.
         inflight, launched = [], [0]
 
         def launch(k):
@@ -551,15 +565,17 @@ class Placer(object):
                 ev.record(self.stream)
             inflight.append((buf, ev))
 
-        left = None
+        left, hand = None, None
         launch(None)
         while True:
-            if (left is None or left >= 2 * self.check_every) and len(inflight) < 2:
+            if ((left is None or left >= 2 * self.check_every) and (hand is None or hand >= 2 * self.check_every)
+                    and len(inflight) < 2):
                 launch(None)
             sbuf, ev = inflight.pop(0)
             ev.synchronize()
             Sh = sbuf.numpy().copy()
             left = self._passes_left(Sh)
+            hand = self._handover_bound(Sh)
             if not Sh[SK["stop"]] and not inflight:
                 launch(None if left >= self.check_every else left)
             it = int(Sh[SK["loop_it"]])
