@@ -69,6 +69,30 @@ def test_device_limits_equal_host_limits():
             assert cluster.device_limits(torch.as_tensor(area), ratio) == cluster.limits(area, ratio)
 
 
+def test_handover_bound_never_overshoots():
+    """The lower bound on the passes before the clusters' hand-over (Placer._handover_bound) is at most the passes
+    the fastest smoothing decrease the accuracy rule allows (a factor 1 / 1.05 per pass, in float64) takes."""
+    from types import SimpleNamespace
+    from autoplace_gb300 import engine
+    SK = engine.SK
+    fake = SimpleNamespace(handover_gamma=2.0, p=SimpleNamespace(opts=SimpleNamespace(wa_rule="accuracy")))
+    for g0 in (2.0, 2.05, 2.1, 3.0, 17.0, 400.0, 1e4):
+        Sh = [0.0] * len(engine.S_FIELDS)
+        Sh[SK["lam"]], Sh[SK["gam"]] = 1e-3, g0
+        bound = engine.Placer._handover_bound(fake, Sh)
+        g, passes = g0, 0
+        while g > fake.handover_gamma:
+            g = g * (1.0 / 1.05)
+            passes += 1
+        assert 1 <= bound <= max(passes, 1), (g0, bound, passes)
+    Sh = [0.0] * len(engine.S_FIELDS)
+    Sh[SK["gam"]] = 10.0                        # no density weight yet: no hand-over bound
+    assert engine.Placer._handover_bound(fake, Sh) is None
+    fake.p.opts.wa_rule = "overflow"            # the overflow rule's smoothing is not bounded per pass
+    Sh[SK["lam"]] = 1e-3
+    assert engine.Placer._handover_bound(fake, Sh) is None
+
+
 def test_wa_long_share_rule():
     """The fused WA launch's long-net share from the share of the pins on long nets: 30 + 60 f within 40 .. 75."""
     from autoplace_gb300 import engine
