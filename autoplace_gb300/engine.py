@@ -327,12 +327,12 @@ class Placer(object):
         self.sync()
         return float(self.scal[0].cpu())
 
-    def _passes(self, phase, k, split=None):
+    def _passes(self, phase, k, split=None, sort=True):
         s = self.stream.cuda_stream
         split = self.split if split is None else split
         for i in range(k):
-            sort = phase == native.PHASE_DENSITY and i % self.sort_every == 0
-            flags = phase | (native.PASS_SORT if sort else 0)
+            sort_now = sort and phase == native.PHASE_DENSITY and i % self.sort_every == 0
+            flags = phase | (native.PASS_SORT if sort_now else 0)
             if split and phase == native.PHASE_DENSITY:
                 if self.split_join == "field":
                     flags |= native.PASS_JOIN_FIELD
@@ -553,11 +553,11 @@ class Placer(object):
         # would be check_every passes that change nothing.
         inflight, launched = [], [0]
 
-        def launch(k):
+        def launch(k, sort=True):
             if k is None:
                 self._replay(native.PHASE_DENSITY)
             else:
-                self._passes(native.PHASE_DENSITY, k)             # up to the predicted stop, eagerly
+                self._passes(native.PHASE_DENSITY, k, sort=sort)  # up to the predicted stop, eagerly
             buf, ev = self._s_host[launched[0] % 2]               # (at most two batches are in flight)
             launched[0] += 1
             with torch.cuda.stream(self.stream):
@@ -577,7 +577,12 @@ class Placer(object):
             left = self._passes_left(Sh)
             hand = self._handover_bound(Sh)
             if not Sh[SK["stop"]] and not inflight:
-                launch(None if left >= self.check_every else left)
+                if left < self.check_every:
+                    launch(left)                                   # exactly the passes to a certain stop
+                elif hand is not None and hand < self.check_every:
+                    launch(hand, sort=False)                       # no further than the hand-over's lower bound
+                else:
+                    launch(None)
             it = int(Sh[SK["loop_it"]])
             if log and it // o.log_freq > logged:
                 logged = it // o.log_freq
