@@ -550,7 +550,8 @@ class Placer(object):
         # come within two batches, the next batch is queued before the host waits for the state of the last one, so
         # the GPU does not idle through the poll; near a predictable stop the host runs exactly the passes left. Near a
         # possible hand-over (its bound below two batches) no batch is queued ahead: a queued batch after the stop
-        # would be check_every passes that change nothing.
+        # would be check_every passes that change nothing; below one batch the host runs just the bound's passes and
+        # polls again, so that no pass runs past the hand-over.
         inflight, launched = [], [0]
 
         def launch(k, sort=True):
