@@ -1,18 +1,18 @@
-"""Batches of uneven placement instances (floorplan variants, seeds, blocks) in one CUDA graph per phase.
+"""Batches of uneven placement instances (floorplan variants, seeds, blocks) in one CUDA graph.
 
 The reference places one design per process, with a host poll every 16 passes (src/gpu_loop.py:58-70). Here a batch
 of N independent instances -- each with its own netlist, grid and field mode -- runs as:
   1. the host part of every instance (Placer.begin: the step-length probes);
-  2. ONE graph for the wirelength-only starts: a conditional WHILE node per instance (gp103_batch_add), looping
-     4 passes at a time until that instance's start phase ends;
-  3. the first density weight of every instance (Placer.start_end: its tension unit);
-  4. ONE graph for the density phases: a WHILE node per instance looping 8 passes (the first refreshing the scatter's
-     spatial order) until its control stops it;
-  5. the placements (Placer.end).
-The instances are separate branches of each graph, so the GPU runs them side by side; no host poll happens inside a
-phase. Results are those of Placer.run for each instance, bit for bit (the same kernels in the same order; passes
-after a stop change nothing). The device time at which each instance's loop ends is recorded, which gives each
-instance's time to the stop from the batch's start.
+  2. ONE graph with every instance's whole placement (gp103_batch_add_run): per instance a conditional WHILE node
+     looping 4 passes of the wirelength-only start until that instance's start phase ends, an IF node with the
+     hand-over to the density phase (the first density weight from the tension unit, the density phase's state, all
+     on the device), and a WHILE node looping 8 passes (the first refreshing the scatter's spatial order) until the
+     instance's control stops it;
+  3. the placements (Placer.start_over, Placer.end).
+The instances are separate branches of the graph, so the GPU runs them side by side; no host step happens between
+the first pass and the last. Results are those of Placer.run for each instance, bit for bit (the same kernels in
+the same order; passes after a stop change nothing). The device time at which each instance's density loop ends is
+recorded, which gives each instance's time to the stop from the batch's start.
 """
 import ctypes
 import time
@@ -21,26 +21,27 @@ import numpy as np
 import torch
 
 from . import native
-from .engine import Placer, SK
+from .engine import Placer
 
 START_PASSES, DENSITY_PASSES = 4, 8
 
 
 class _Graph(object):
-    def __init__(self, placers, phase, passes, sort_first, stream, dev):
+    def __init__(self, placers, stream, dev):
         n = len(placers)
-        self.loops = torch.zeros(n, dtype=torch.int32, device=dev)
-        self.stop_ns = torch.zeros(n, dtype=torch.int64, device=dev)
+        self.loops = torch.zeros((n, 2), dtype=torch.int32, device=dev)       # bodies of the start, density loops
+        self.stop_ns = torch.zeros((n, 2), dtype=torch.int64, device=dev)
         self.t0 = torch.zeros(1, dtype=torch.int64, device=dev)
         h = ctypes.c_void_p()
         native.call("gp103_batch_create", ctypes.byref(h))
         self.h = h
         for k, pl in enumerate(placers):
             o = pl.p.opts
-            max_loops = int(o.inner_iter) // passes + 2
-            native.call("gp103_batch_add", h, pl._ref, phase, passes, int(sort_first), max_loops,
-                        ctypes.c_void_p(self.loops.data_ptr() + 4 * k),
-                        ctypes.c_void_p(self.stop_ns.data_ptr() + 8 * k), stream.cuda_stream)
+            native.call("gp103_batch_add_run", h, pl._ref, START_PASSES, DENSITY_PASSES,
+                        int(o.inner_iter) // START_PASSES + 2, int(o.inner_iter) // DENSITY_PASSES + 2,
+                        float(o.density_weight), float(pl.p.total_pins), float(pl.start_gamma), pl._p(pl.tmp[0]),
+                        pl._p(pl.scal), ctypes.c_void_p(self.loops.data_ptr() + 8 * k),
+                        ctypes.c_void_p(self.stop_ns.data_ptr() + 16 * k), stream.cuda_stream)
 
     def launch(self, stream):
         with torch.cuda.stream(stream):
@@ -56,7 +57,7 @@ class _Graph(object):
 
 class Batch(object):
     """N instances (Problems) placed together. fields: one field mode per instance (or one for all); tuned: per-
-    instance settings from tune.py (field mode and the WA lane groups), applied before the graphs are captured."""
+    instance settings from tune.py (field mode and the WA lane groups), applied before the graph is captured."""
 
     def __init__(self, problems, fields="f16x3", device="cuda", tuned=None):
         self.dev = torch.device(device)
@@ -72,8 +73,7 @@ class Batch(object):
             for pl, t in zip(self.placers, tuned):
                 tune.apply_wa(pl, t.get("wa", "default"))
         self.stream.synchronize()
-        self.start_graph = _Graph(self.placers, native.PHASE_START, START_PASSES, False, self.stream, self.dev)
-        self.density_graph = _Graph(self.placers, native.PHASE_DENSITY, DENSITY_PASSES, True, self.stream, self.dev)
+        self.graph = _Graph(self.placers, self.stream, self.dev)
 
     def run(self, pos0s):
         """Place every instance from its start positions. -> (list of Placer.run result dicts, per-instance seconds
@@ -81,22 +81,13 @@ class Batch(object):
         torch.cuda.synchronize(self.dev)
         t0 = time.time()
         ctxs = [pl.begin(p0) for pl, p0 in zip(self.placers, pos0s)]
-        self.start_graph.launch(self.stream)
+        self.graph.launch(self.stream)
         self.stream.synchronize()
-        results = [None] * len(self.placers)
-        for k, (pl, ctx) in enumerate(zip(self.placers, ctxs)):
-            results[k] = pl.start_end(ctx)                 # None, or the result when the start phase stopped
-        with torch.cuda.stream(self.stream):
-            for k, pl in enumerate(self.placers):          # a finished instance's density loop ends at once
-                if results[k] is not None:
-                    pl.S[SK["stop"]] = results[k].get("stop_code", 4)
-        self.density_graph.launch(self.stream)
-        self.stream.synchronize()
-        for k, (pl, ctx) in enumerate(zip(self.placers, ctxs)):
-            if results[k] is None:
-                results[k] = pl.end(ctx)
+        results = []
+        for pl, ctx in zip(self.placers, ctxs):
+            out = pl.start_over(ctx, pl.T.cpu().numpy())         # the result when the start phase stopped the run
+            results.append(out if out is not None else pl.end(ctx))
         wall = time.time() - t0
-        start_t0 = int(self.start_graph.t0.cpu()[0])
-        stop = self.density_graph.stop_ns.cpu().numpy().astype(np.int64)
-        per = (stop - start_t0) / 1e9
+        stop = self.graph.stop_ns[:, 1].cpu().numpy().astype(np.int64)
+        per = (stop - int(self.graph.t0.cpu()[0])) / 1e9
         return results, per, wall

@@ -577,6 +577,35 @@ extern "C" int gp103_probe(const gp103_plan* plan, const float* v, const float* 
     return launch_totals(&r, &k0, 1, out1, stream);
 }
 
+extern "C" int gp103_start_to_density(const gp103_plan* plan, double density_weight, double total_pins,
+                                      double gamma, float* g_tmp, double* out5, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    const gp103_plan* p = plan;
+    REQUIRE(g_tmp && out5 && p->T && p->S && p->kp && p->cur && p->best && p->v[0] && p->v[1]);
+    // the plain density gradient at v[*cur] (weight 1, no preconditioner, no wirelength term): gp103_eval's kernels
+    // with the positions picked on the device (pick(a, b, sel) = *sel ? a : b, so a = v[1], b = v[0])
+    TRY(density_and_field(p, p->v[1], p->v[0], p->cur, nullptr, stream));
+    GatherJob g = gather_job(p);
+    g.pos_a = (const float2*)p->v[1];
+    g.pos_b = (const float2*)p->v[0];
+    g.sel = p->cur;
+    g.gout_a = g.gout_b = (float2*)g_tmp;
+    g.with_wl = 0;
+    g.ex = p->ex;
+    g.ey = p->ey;
+    g.weight = 1.f;
+    g.precond = -1.f;
+    TRY(launch_gather(g, stream));
+    const Reduce r_wa = reduce_slot(p->red, p->counters, R_WA);
+    const Reduce r_grad = reduce_slot(p->red, p->counters, R_GRAD);
+    const Reduce ovf = reduce_slot(p->red, p->counters, p->jnbx > 0 ? R_JOVF : R_OVF);
+    const Reduce rs[5] = {r_grad, r_wa, r_wa, ovf, r_grad};
+    const int ks[5] = {0, 0, 1, 0, 1};
+    TRY(launch_totals(rs, ks, 5, out5, stream));
+    return launch_handover(p->T, p->S, p->kp, p->cur, p->v[0], p->v[1], p->best, out5 + 4, total_pins,
+                           density_weight, gamma, 2 * p->num_nodes, stream);
+}
+
 extern "C" int gp103_finish(const gp103_plan* plan, cudaStream_t stream) {
     REQUIRE(plan && plan->S && plan->cur && plan->v[0] && plan->v[1] && plan->best);
     return launch_finish(plan->S, plan->cur, plan->v[0], plan->v[1], plan->best, 2 * plan->num_nodes, stream);

@@ -15,6 +15,12 @@
 
 using namespace gp103;
 
+#define TRY(call)                \
+    do {                         \
+        int st_ = (call);        \
+        if (st_) return st_;     \
+    } while (0)
+
 namespace {
 
 struct Batch {
@@ -64,23 +70,30 @@ extern "C" int gp103_batch_destroy(void* batch) {
     return GP103_OK;
 }
 
-extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first,
-                               int max_loops, int* loops, unsigned long long* stop_ns, cudaStream_t capture) {
-    Batch* b = (Batch*)batch;
-    if (!b || !plan || !loops || !stop_ns || passes < 1 || max_loops < 1 || b->exec) return GP103_ERR_ARG;
-    if (phase != GP103_PHASE_START && phase != GP103_PHASE_DENSITY) return GP103_ERR_ARG;
-    if (phase == GP103_PHASE_START ? !plan->T : !plan->S) return GP103_ERR_ARG;
-    cudaGraphConditionalHandle h;
-    if (cudaGraphConditionalHandleCreate(&h, b->graph, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+// A conditional node of type `type` after the nodes deps[0..ndeps), its handle set to `value` at every launch of the
+// graph (a WHILE node whose condition kernel clears it, or an IF node that runs its body once). -> its body graph.
+static int add_conditional(Batch* b, cudaGraphConditionalNodeType type, unsigned int value,
+                           const cudaGraphNode_t* deps, size_t ndeps, cudaGraphConditionalHandle* h,
+                           cudaGraphNode_t* node, cudaGraph_t* body) {
+    if (cudaGraphConditionalHandleCreate(h, b->graph, value, cudaGraphCondAssignDefault) != cudaSuccess)
         return GP103_ERR_CUDA;
     cudaGraphNodeParams p = {};
     p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = h;
-    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.handle = *h;
+    p.conditional.type = type;
     p.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (cudaGraphAddNode(&node, b->graph, nullptr, nullptr, 0, &p) != cudaSuccess) return GP103_ERR_CUDA;
-    cudaGraph_t body = p.conditional.phGraph_out[0];
+    if (cudaGraphAddNode(node, b->graph, deps, nullptr, ndeps, &p) != cudaSuccess) return GP103_ERR_CUDA;
+    *body = p.conditional.phGraph_out[0];
+    return GP103_OK;
+}
+
+// The loop of one phase of one instance after deps: `passes` passes and the condition kernel per body.
+static int add_loop(Batch* b, const gp103_plan* plan, int phase, int passes, int sort_first, int max_loops,
+                    int* loops, unsigned long long* stop_ns, const cudaGraphNode_t* deps, size_t ndeps,
+                    cudaStream_t capture, cudaGraphNode_t* node) {
+    cudaGraphConditionalHandle h;
+    cudaGraph_t body;
+    TRY(add_conditional(b, cudaGraphCondTypeWhile, 1, deps, ndeps, &h, node, &body));
     if (cudaStreamBeginCaptureToGraph(capture, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
         cudaSuccess)
         return GP103_ERR_CUDA;
@@ -90,7 +103,7 @@ extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, i
         st = gp103_pass(plan, flags, capture);
     }
     const double* state = phase == GP103_PHASE_START ? plan->T : plan->S;
-    const int stop_at = phase == GP103_PHASE_START ? GP103_T_STOP : S_STOP;
+    const int stop_at = phase == GP103_PHASE_START ? (int)GP103_T_STOP : (int)S_STOP;
     const int done_at = phase == GP103_PHASE_START ? GP103_T_DONE : -1;
     if (!st && launch_k(batch_cond_kernel, dim3(1), dim3(1), 0, capture, h, state, stop_at, done_at, loops, max_loops,
                         stop_ns) != cudaSuccess)
@@ -98,7 +111,45 @@ extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, i
     cudaGraph_t out = nullptr;
     const cudaError_t e = cudaStreamEndCapture(capture, &out);      // (ends the capture whatever happened above)
     if (st) return st;
+    return e == cudaSuccess ? GP103_OK : GP103_ERR_CUDA;
+}
+
+extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first,
+                               int max_loops, int* loops, unsigned long long* stop_ns, cudaStream_t capture) {
+    Batch* b = (Batch*)batch;
+    if (!b || !plan || !loops || !stop_ns || passes < 1 || max_loops < 1 || b->exec) return GP103_ERR_ARG;
+    if (phase != GP103_PHASE_START && phase != GP103_PHASE_DENSITY) return GP103_ERR_ARG;
+    if (phase == GP103_PHASE_START ? !plan->T : !plan->S) return GP103_ERR_ARG;
+    cudaGraphNode_t node;
+    TRY(add_loop(b, plan, phase, passes, sort_first, max_loops, loops, stop_ns, nullptr, 0, capture, &node));
+    b->count++;
+    return GP103_OK;
+}
+
+extern "C" int gp103_batch_add_run(void* batch, const gp103_plan* plan, int start_passes, int density_passes,
+                                   int max_start_loops, int max_density_loops, double density_weight,
+                                   double total_pins, double gamma, float* g_tmp, double* out5, int* loops,
+                                   unsigned long long* stop_ns, cudaStream_t capture) {
+    Batch* b = (Batch*)batch;
+    if (!b || !plan || !plan->T || !plan->S || !g_tmp || !out5 || !loops || !stop_ns || start_passes < 1 ||
+        density_passes < 1 || max_start_loops < 1 || max_density_loops < 1 || b->exec)
+        return GP103_ERR_ARG;
+    cudaGraphNode_t start, hand, density;
+    TRY(add_loop(b, plan, GP103_PHASE_START, start_passes, 0, max_start_loops, loops, stop_ns, nullptr, 0, capture,
+                 &start));
+    cudaGraphConditionalHandle h;
+    cudaGraph_t body;
+    TRY(add_conditional(b, cudaGraphCondTypeIf, 1, &start, 1, &h, &hand, &body));
+    if (cudaStreamBeginCaptureToGraph(capture, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+        cudaSuccess)
+        return GP103_ERR_CUDA;
+    const int st = gp103_start_to_density(plan, density_weight, total_pins, gamma, g_tmp, out5, capture);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(capture, &out);
+    if (st) return st;
     if (e != cudaSuccess) return GP103_ERR_CUDA;
+    TRY(add_loop(b, plan, GP103_PHASE_DENSITY, density_passes, 1, max_density_loops, loops + 1, stop_ns + 1, &hand, 1,
+                 capture, &density));
     b->count++;
     return GP103_OK;
 }

@@ -362,6 +362,55 @@ int launch_finish(const double* S, const int* cur, const float* v0, const float*
     return GP103_OK;
 }
 
+// The hand-over from the wirelength-only start to the density phase, on the device (src/run_placement.py:60-64 and
+// the state set-up of src/gpu_loop.py:38-48). l1 = the L1 norm over the cells of the plain density gradient at v[cur];
+// the density weight is density_weight x (total_pins / l1), the tension unit; S is the density phase's state
+// (iteration, last HPWL, step length alpha and momentum a carried over from T), kp its float32 parameters with the
+// Nesterov coefficient (a - 1) / ((1 + sqrt(4 a^2 + 1)) / 2), and best = v[cur]. Every float64 operation is a
+// rounded IEEE operation in the order of the host's statement of the same rule, so the state is the same bits. When
+// the start itself stopped the run (T[stop] != 0), only S[stop] is set: the density passes then do nothing.
+__global__ void handover_kernel(const double* T, double* S, float* kp, const int* cur, const float* v0,
+                                const float* v1, float* best, const double* l1, double total_pins,
+                                double density_weight, double gamma, int n) {
+    pdl_wait();
+    const double stop = T[GP103_T_STOP];
+    if (stop != 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) S[S_STOP] = stop;
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double lam = __dmul_rn(density_weight, __ddiv_rn(total_pins, *l1));
+        const double alpha = T[GP103_T_ALPHA], a = T[GP103_T_A];
+        const double a_next = __ddiv_rn(__dadd_rn(1.0, __dsqrt_rn(__dadd_rn(__dmul_rn(__dmul_rn(4.0, a), a), 1.0))), 2.0);
+        for (int i = 0; i < S_SIZE; i++) S[i] = 0.0;
+        S[S_LAM] = lam;
+        S[S_GAM] = gamma;
+        S[S_ALPHA] = alpha;
+        S[S_A] = a;
+        S[S_ITER] = T[GP103_T_ITER];
+        S[S_HPWL_PREV] = T[GP103_T_HPWL];
+        S[S_MU] = 1.0;
+        S[S_BEST_HPWL] = S[S_BEST_OVF] = __longlong_as_double(0x7ff0000000000000LL);     // +inf
+        S[S_LOOP_IT] = T[GP103_T_LOOP_IT];
+        kp[0] = __double2float_rn(gamma);
+        kp[1] = kp[2] = __double2float_rn(lam);
+        kp[3] = __double2float_rn(alpha);
+        kp[4] = __double2float_rn(__ddiv_rn(__dsub_rn(a, 1.0), a_next));
+    }
+    const float* v = *cur ? v1 : v0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) best[i] = v[i];
+}
+
+int launch_handover(const double* T, double* S, float* kp, const int* cur, const float* v0, const float* v1,
+                    float* best, const double* l1, double total_pins, double density_weight, double gamma, int n,
+                    cudaStream_t s) {
+    if (launch_k(handover_kernel, dim3(grid_for(n > 0 ? n : 1, 256, 8)), dim3(256), 0, s, T, S, kp, cur, v0, v1,
+                 best, l1, total_pins, density_weight, gamma, n) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
 // out[i] = value k[i] of reduction r[i] (i < n <= 8): the scalars of an evaluation, for the host.
 struct Totals {
     Reduce r[8];

@@ -46,6 +46,10 @@ int launch_control_start(double* T, float* kp, Reduce grad, const double* pre, i
                          cudaStream_t s);
 int launch_finish(const double* S, const int* cur, const float* v0, const float* v1, float* best, int n,
                   cudaStream_t s);
+// The start-to-density hand-over of the state (handover_kernel); l1: the device L1 norm of the tension unit.
+int launch_handover(const double* T, double* S, float* kp, const int* cur, const float* v0, const float* v1,
+                    float* best, const double* l1, double total_pins, double density_weight, double gamma, int n,
+                    cudaStream_t s);
 int launch_totals(const Reduce* r, const int* k, int n, double* out, cudaStream_t s);
 // out[0] = value 0 of r times mul
 int launch_scale_total(const Reduce& r, double mul, double* out, cudaStream_t s);

@@ -150,6 +150,7 @@ class Placer(object):
         self.mode = field_mode(native.FIELD_MODES[field] if isinstance(field, str) else int(field),
                                prob.force.nbx, prob.force.nby)
         self.handover_gamma = float(handover_gamma or 0.0)
+        self.start_gamma = 10 * prob.base_gamma     # the WA smoothing of a fresh run (src/param_scheduler.py:31)
         self.check_every = check_every
         self.use_graphs = use_graphs
         # density passes between refreshes of the scatter's spatial order (an order only speeds the scatter up)
@@ -467,7 +468,7 @@ class Placer(object):
         t0 = time.time()
         r = resume or {}
         lam0 = float(r.get("lam", 0.0))
-        gam = float(r["gam"]) if resume else 10 * p.base_gamma
+        gam = float(r["gam"]) if resume else self.start_gamma
         first = int(r.get("first_iter", 0))
         w, pc = (lam0, lam0) if lam0 > 0 else (0.0, -1.0)
         with torch.cuda.stream(self.stream):
@@ -505,10 +506,21 @@ class Placer(object):
         return ctx
 
     def start_end(self, ctx, log=None):
-        """After the wirelength-only start's passes: the first density weight (density_weight x tension unit) and
-        the density phase's state. -> None, or the result dict when the start phase itself stopped the run."""
-        o = self.p.opts
+        """After the wirelength-only start's passes: the density phase's state. -> None, or the result dict when the
+        start phase itself stopped the run."""
         Th = self.T.cpu().numpy()
+        out = self.start_over(ctx, Th)
+        if out is not None:
+            return out
+        self.hand_over(ctx)
+        if log:
+            log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
+                % (ctx["start_iters"], Th[TI["hpwl"]], float(self.S[SK["lam"]].cpu())))
+        return None
+
+    def start_over(self, ctx, Th):
+        """The host's part of the end of the start phase, from its final state Th (T on the host): -> the result dict
+        when the start phase stopped the run, else None, with ctx set for the density phase."""
         ctx["evals"] += int(Th[TI["evals"]])
         start_iters = int(Th[TI["loop_it"]])
         if Th[TI["stop"]] == STOP_DEVICE_ERROR:
@@ -519,15 +531,15 @@ class Placer(object):
             return dict(reason=reason, iters=start_iters, start_iters=start_iters, hpwl=float(Th[TI["hpwl"]]),
                         overflow=float("nan"), evals=ctx["evals"], seconds=time.time() - ctx["t0"], pos=self.V[cur],
                         iter=int(Th[TI["iter"]]), lam=0.0, gam=ctx["gam"], density_iters=0)
-        cur = int(self.cur.cpu())
-        # first density weight: density_weight x tension unit (Objective.tension_unit)
-        lam = o.density_weight * self.tension_unit(self.V[cur])[0]
-        if log:
-            log("wirelength-only start over after %d iterations (hpwl %.4E): density weight %.4E"
-                % (start_iters, Th[TI["hpwl"]], lam))
-        self._density_state(ctx, lam=lam, alpha=Th[TI["alpha"]], a=Th[TI["a"]], it0=start_iters,
-                            iter0=Th[TI["iter"]], hpwl_prev=Th[TI["hpwl"]], cur=cur, start_iters=start_iters)
+        ctx.update(it0=start_iters, start_iters=start_iters)
         return None
+
+    def hand_over(self, ctx):
+        """Queue the hand-over to the density phase (gp103_start_to_density, no host synchronisation): the first
+        density weight, density_weight x the tension unit at the current positions (src/run_placement.py:60-64,
+        Objective.tension_unit), and the density phase's state S, kp and best, all set on the device from T."""
+        native.call("gp103_start_to_density", self._ref, float(self.p.opts.density_weight), float(self.p.total_pins),
+                    float(ctx["gam"]), self._p(self.tmp[0]), self._p(self.scal), self.stream.cuda_stream)
 
     def _density_state(self, ctx, lam, alpha, a, it0, iter0, hpwl_prev, cur, start_iters):
         gam = ctx["gam"]

@@ -75,6 +75,7 @@ _SIGS = {
     "gp103_probe": ([ctypes.POINTER(Plan), _vp, _vp, _d, _vp, _vp, _vp], _i),
     "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
+    "gp103_start_to_density": ([ctypes.POINTER(Plan), _d, _d, _d, _vp, _vp, _vp], _i),
     "gp103_device_error": ([ctypes.POINTER(Plan), _i, ctypes.POINTER(_i), _vp], _i),
     "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
     "gp103_net_order_scratch": ([_i, _i, _i], ctypes.c_size_t),
@@ -100,6 +101,7 @@ _SIGS = {
     # batches of instances in one graph
     "gp103_batch_create": ([ctypes.POINTER(_vp)], _i),
     "gp103_batch_add": ([_vp, ctypes.POINTER(Plan), _i, _i, _i, _i, _vp, _vp, _vp], _i),
+    "gp103_batch_add_run": ([_vp, ctypes.POINTER(Plan), _i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_batch_launch": ([_vp, _vp, _vp], _i),
     "gp103_batch_destroy": ([_vp], _i),
     # the learned start

@@ -477,7 +477,7 @@ def run_gb300(args):
 
 def run_batch(args):
     """--config c3: 64 uneven instances (5k-150k cells, grids 64-512, 0-10 macros), tuned per size class, placed as
-    one batch (one CUDA graph per phase) and one by one; aggregate iterations/s and p50 / p99 time to the stop."""
+    one batch (one CUDA graph) and one by one; aggregate iterations/s and p50 / p99 time to the stop."""
     import numpy as np
     import torch
     from autoplace_gb300 import engine, problem, synth, tune
@@ -523,7 +523,7 @@ def run_batch(args):
         singles.append(time.time() - t0)
         del pl
     single_total = float(np.sum(singles))
-    line = {"metric": "aggregate iterations/s, batch of %d uneven instances in one CUDA graph per phase"
+    line = {"metric": "aggregate iterations/s, batch of %d uneven instances in one CUDA graph"
                       % len(probs),
             "value": round(iters / wall, 1), "unit": "iter/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(wall * 1000, 2), "higher_is_better": True, "scaling": "weak",
@@ -533,7 +533,7 @@ def run_batch(args):
                                    "0-10 macros, grids %d .. %d, one level each"
                                    % (len(probs), min(p.num_mov for p in probs), max(p.num_mov for p in probs),
                                       min(p.force.nbx for p in probs), max(p.force.nbx for p in probs)),
-                       "instances": len(probs), "graphs_per_batch": 2},
+                       "instances": len(probs), "graphs_per_batch": 1},
             "result": {"iterations": iters, "batch_s": round(wall, 4),
                        "time_to_stop_p50_s": round(float(np.percentile(per, 50)), 4),
                        "time_to_stop_p99_s": round(float(np.percentile(per, 99)), 4),

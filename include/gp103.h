@@ -270,6 +270,17 @@ int gp103_pass_split(const gp103_plan* plan, int phase_flags, cudaStream_t strea
 int gp103_event_create(void** event);
 int gp103_event_destroy(void* event);
 
+/* The hand-over from the wirelength-only start to the density phase, queued on `stream` with no host
+ * synchronisation (src/run_placement.py:60-64 with the state set-up of src/gpu_loop.py:38-48): the plain density
+ * gradient at v[*cur] (gp103_eval's kernels with weight 1, precond -1, no wirelength term; into g_tmp
+ * [num_nodes, 2], its 5 totals into out5, device doubles), then on the device the first density weight
+ * lam = density_weight x (total_pins / out5[4]) (the tension unit), S = the density phase's state (lam, gamma, the
+ * step length, momentum, iteration, last HPWL and loop count of T; mu 1; best HPWL and overflow +inf; the rest 0),
+ * kp = (gamma, lam, lam, alpha, Nesterov coefficient) in float32 and best = v[*cur]. If the start phase stopped the
+ * run (T[GP103_T_STOP] != 0), only S[14] = T[GP103_T_STOP] is written, and density passes change nothing. */
+int gp103_start_to_density(const gp103_plan* plan, double density_weight, double total_pins, double gamma,
+                           float* g_tmp, double* out5, cudaStream_t stream);
+
 /* After the last pass: copy the pending best placement (S[is_best] of the last control) from v[*cur]. */
 int gp103_finish(const gp103_plan* plan, cudaStream_t stream);
 
@@ -478,6 +489,15 @@ int gp103_learn_features(const int* net_start, const int* pin_cell, const float*
 int gp103_batch_create(void** batch);
 int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first, int max_loops,
                     int* loops, unsigned long long* stop_ns, cudaStream_t capture);
+/* A whole placement of one instance in the batch's graph: the start phase's WHILE node (start_passes per body,
+ * at most max_start_loops bodies), then an IF node that runs gp103_start_to_density once (density_weight,
+ * total_pins, gamma, g_tmp, out5 as there), then the density phase's WHILE node (density_passes per body, the first
+ * refreshing the spatial order, at most max_density_loops bodies). loops[0], stop_ns[0] belong to the start loop,
+ * loops[1], stop_ns[1] to the density loop. No host step between the phases. */
+int gp103_batch_add_run(void* batch, const gp103_plan* plan, int start_passes, int density_passes,
+                        int max_start_loops, int max_density_loops, double density_weight, double total_pins,
+                        double gamma, float* g_tmp, double* out5, int* loops, unsigned long long* stop_ns,
+                        cudaStream_t capture);
 int gp103_batch_launch(void* batch, unsigned long long* t0_ns, cudaStream_t stream);
 int gp103_batch_destroy(void* batch);
 

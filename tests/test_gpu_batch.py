@@ -1,6 +1,9 @@
-"""Batches of uneven instances in one CUDA graph per phase (autoplace_gb300/batch.py, gp103_batch_*): every instance
-ends exactly where its own Placer.run ends (the same kernels in the same order: positions bit for bit, the same stop
-and iterations), and the autotuner's choices are valid launches that place as well."""
+"""Batches of uneven instances in one CUDA graph (autoplace_gb300/batch.py, gp103_batch_*): every instance ends
+exactly where its own Placer.run ends (the same kernels in the same order: positions bit for bit, the same stop and
+iterations), the hand-over between the phases, made on the device, gives the state of the host's statement of the
+rule bit for bit, and the autotuner's choices are valid launches that place as well."""
+import math
+
 import numpy as np
 import pytest
 
@@ -36,6 +39,41 @@ def test_batch_matches_one_by_one(instances):
     res2, _, _ = b.run(pos)
     for r, r2 in zip(res, res2):
         assert np.array_equal(r["pos"].cpu().numpy(), r2["pos"].cpu().numpy())
+
+
+def test_hand_over_matches_the_host_rule(instances):
+    """gp103_start_to_density against the rule stated on the host in float64 (src/run_placement.py:60-64: density
+    weight x tension unit; src/gpu_loop.py:38-48: the density phase's state, kp with the Nesterov coefficient)."""
+    from autoplace_gb300 import native
+    from autoplace_gb300.engine import Placer, SK, S_FIELDS, TI
+    probs, pos = instances
+    for p, p0 in list(zip(probs, pos))[:3]:
+        pl = Placer(p, use_graphs=False)
+        ctx = pl.begin(p0)
+        while True:
+            pl._replay(native.PHASE_START)
+            pl.sync()
+            Th = pl.T.cpu().numpy()
+            if Th[TI["done"]] or Th[TI["stop"]]:
+                break
+        assert pl.start_over(ctx, Th) is None
+        cur = int(pl.cur.cpu())
+        lam = p.opts.density_weight * pl.tension_unit(pl.V[cur])[0]
+        a = Th[TI["a"]]
+        coef = (a - 1) / ((1 + math.sqrt(4 * a * a + 1)) / 2)
+        S = np.zeros(len(S_FIELDS))
+        S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, pl.start_gamma, Th[TI["alpha"]], a
+        S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = Th[TI["iter"]], Th[TI["hpwl"]], 1.0
+        S[SK["best_hpwl"]] = S[SK["best_ovf"]] = math.inf
+        S[SK["loop_it"]] = ctx["start_iters"]
+        kp = np.array([pl.start_gamma, lam, lam, Th[TI["alpha"]], coef], dtype=np.float32)
+        with torch.cuda.stream(pl.stream):
+            pl.best.zero_()
+        pl.hand_over(ctx)
+        pl.sync()
+        assert np.array_equal(pl.S.cpu().numpy().view(np.uint64), S.view(np.uint64))
+        assert np.array_equal(pl.kp.cpu().numpy().view(np.uint32), kp.view(np.uint32))
+        assert np.array_equal(pl.best.cpu().numpy().view(np.uint32), pl.V[cur].cpu().numpy().view(np.uint32))
 
 
 def test_tuned_batch_places_as_well(instances):
