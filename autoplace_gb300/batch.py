@@ -2,15 +2,15 @@
 
 The reference places one design per process, with a host poll every 16 passes (src/gpu_loop.py:58-70). Here a batch
 of N independent instances -- each with its own netlist, grid and field mode -- runs as:
-  1. the host part of every instance (Placer.begin: the step-length probes);
-  2. ONE graph with every instance's whole placement (gp103_batch_add_run): per instance a conditional WHILE node
-     looping 4 passes of the wirelength-only start until that instance's start phase ends, an IF node with the
-     hand-over to the density phase (the first density weight from the tension unit, the density phase's state, all
-     on the device), and a WHILE node looping 8 passes (the first refreshing the scatter's spatial order) until the
-     instance's control stops it;
+  1. the start positions of every instance uploaded (Placer.load);
+  2. ONE graph with every instance's whole placement (gp103_batch_add_run): per instance an IF node with the level's
+     set-up (gp103_begin: the step-length probes and the start's state), a conditional WHILE node looping 4 passes
+     of the wirelength-only start until that instance's start phase ends, an IF node with the hand-over to the
+     density phase (the first density weight from the tension unit, the density phase's state), and a WHILE node
+     looping 8 passes (the first refreshing the scatter's spatial order) until the instance's control stops it;
   3. the placements (Placer.start_over, Placer.end).
 The instances are separate branches of the graph, so the GPU runs them side by side; no host step happens between
-the first pass and the last. Results are those of Placer.run for each instance, bit for bit (the same kernels in
+the set-up and the stop. Results are those of Placer.run for each instance, bit for bit (the same kernels in
 the same order; passes after a stop change nothing). The device time at which each instance's density loop ends is
 recorded, which gives each instance's time to the stop from the batch's start.
 """
@@ -37,10 +37,11 @@ class _Graph(object):
         self.h = h
         for k, pl in enumerate(placers):
             o = pl.p.opts
-            native.call("gp103_batch_add_run", h, pl._ref, START_PASSES, DENSITY_PASSES,
+            args = pl.begin_args(pl.start_gamma)
+            native.call("gp103_batch_add_run", h, pl._ref, ctypes.byref(args), START_PASSES, DENSITY_PASSES,
                         int(o.inner_iter) // START_PASSES + 2, int(o.inner_iter) // DENSITY_PASSES + 2,
                         float(o.density_weight), float(pl.p.total_pins), float(pl.start_gamma), pl._p(pl.tmp[0]),
-                        pl._p(pl.scal), ctypes.c_void_p(self.loops.data_ptr() + 8 * k),
+                        pl._p(pl.tmp[1]), pl._p(pl.scal), ctypes.c_void_p(self.loops.data_ptr() + 8 * k),
                         ctypes.c_void_p(self.stop_ns.data_ptr() + 16 * k), stream.cuda_stream)
 
     def launch(self, stream):
@@ -80,11 +81,13 @@ class Batch(object):
         from the batch's start to the end of its density loop, device-timed, and the batch's wall seconds)."""
         torch.cuda.synchronize(self.dev)
         t0 = time.time()
-        ctxs = [pl.begin(p0) for pl, p0 in zip(self.placers, pos0s)]
+        for pl, p0 in zip(self.placers, pos0s):
+            pl.load(p0)
         self.graph.launch(self.stream)
         self.stream.synchronize()
         results = []
-        for pl, ctx in zip(self.placers, ctxs):
+        for pl in self.placers:
+            ctx = pl.context(t0)
             out = pl.start_over(ctx, pl.T.cpu().numpy())         # the result when the start phase stopped the run
             results.append(out if out is not None else pl.end(ctx))
         wall = time.time() - t0

@@ -577,6 +577,36 @@ extern "C" int gp103_probe(const gp103_plan* plan, const float* v, const float* 
     return launch_totals(&r, &k0, 1, out1, stream);
 }
 
+extern "C" int gp103_begin(const gp103_plan* plan, const gp103_begin_args* a, float* tmp0, float* tmp1,
+                           double* scal8, cudaStream_t stream) {
+    TRY(check_plan(plan));
+    const gp103_plan* p = plan;
+    REQUIRE(a && tmp0 && tmp1 && scal8 && p->T && p->S && p->kp && p->cur && p->best && p->v[0] && p->u[0] &&
+            p->g[0] && p->lo && p->hi);
+    const float* v = p->v[0];
+    float* g = p->g[0];
+    const double w = a->lam > 0 ? a->lam : 0.0, pc = a->lam > 0 ? a->lam : -1.0;
+    const Reduce r = reduce_slot(p->red, p->counters, R_MOVED);
+    const int k0 = 0;
+    TRY(launch_begin(p->kp, p->cur, a->gamma, a->lam, stream));
+    // estimate_initial_learning_rate: the gradient at v, a probe step of lr, the gradient there; the step length
+    // sqrt(|probe - v|^2) / sqrt(|g(probe) - g|^2) into scal8[6]
+    TRY(gp103_eval(p, v, g, nullptr, w, pc, 1, scal8, stream));
+    TRY(launch_probe(v, g, p->lo, p->hi, (float)a->lr, p->num_nodes, tmp0, r, stream));
+    TRY(launch_totals(&r, &k0, 1, scal8 + 5, stream));
+    TRY(gp103_eval(p, tmp0, tmp1, g, w, pc, 1, scal8, stream));
+    TRY(launch_sqrt_ratio(scal8 + 5, scal8, scal8 + 6, stream));
+    // NesterovOptimizer.__init__: the gradient at v again, u = v, the probe with that step length; alpha into scal8[7]
+    TRY(gp103_eval(p, v, g, nullptr, w, pc, 1, scal8, stream));
+    TRY(launch_copy(v, p->u[0], 2 * p->num_nodes, stream));
+    TRY(launch_probe(v, g, p->lo, p->hi, 0.f, p->num_nodes, tmp0, r, stream, scal8 + 6));
+    TRY(launch_totals(&r, &k0, 1, scal8 + 5, stream));
+    TRY(gp103_eval(p, tmp0, tmp1, g, w, pc, 1, scal8, stream));
+    TRY(launch_sqrt_ratio(scal8 + 5, scal8, scal8 + 7, stream));
+    return launch_first_state(p->T, p->S, p->kp, p->best, v, 2 * p->num_nodes, scal8 + 7, a->gamma, a->lam,
+                              a->start_tol, a->inner_iter, a->iter, a->loop_it, a->hpwl_prev, stream);
+}
+
 extern "C" int gp103_start_to_density(const gp103_plan* plan, double density_weight, double total_pins,
                                       double gamma, float* g_tmp, double* out5, cudaStream_t stream) {
     TRY(check_plan(plan));

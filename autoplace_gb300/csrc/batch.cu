@@ -126,28 +126,41 @@ extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, i
     return GP103_OK;
 }
 
-extern "C" int gp103_batch_add_run(void* batch, const gp103_plan* plan, int start_passes, int density_passes,
-                                   int max_start_loops, int max_density_loops, double density_weight,
-                                   double total_pins, double gamma, float* g_tmp, double* out5, int* loops,
-                                   unsigned long long* stop_ns, cudaStream_t capture) {
-    Batch* b = (Batch*)batch;
-    if (!b || !plan || !plan->T || !plan->S || !g_tmp || !out5 || !loops || !stop_ns || start_passes < 1 ||
-        density_passes < 1 || max_start_loops < 1 || max_density_loops < 1 || b->exec)
-        return GP103_ERR_ARG;
-    cudaGraphNode_t start, hand, density;
-    TRY(add_loop(b, plan, GP103_PHASE_START, start_passes, 0, max_start_loops, loops, stop_ns, nullptr, 0, capture,
-                 &start));
+// An IF node after deps[0..ndeps) whose body (run once per launch) is what `queue` puts on the capture stream.
+template <typename F>
+static int add_once(Batch* b, const cudaGraphNode_t* deps, size_t ndeps, cudaStream_t capture, cudaGraphNode_t* node,
+                    F queue) {
     cudaGraphConditionalHandle h;
     cudaGraph_t body;
-    TRY(add_conditional(b, cudaGraphCondTypeIf, 1, &start, 1, &h, &hand, &body));
+    TRY(add_conditional(b, cudaGraphCondTypeIf, 1, deps, ndeps, &h, node, &body));
     if (cudaStreamBeginCaptureToGraph(capture, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
         cudaSuccess)
         return GP103_ERR_CUDA;
-    const int st = gp103_start_to_density(plan, density_weight, total_pins, gamma, g_tmp, out5, capture);
+    const int st = queue();
     cudaGraph_t out = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(capture, &out);
+    const cudaError_t e = cudaStreamEndCapture(capture, &out);      // (ends the capture whatever happened above)
     if (st) return st;
-    if (e != cudaSuccess) return GP103_ERR_CUDA;
+    return e == cudaSuccess ? GP103_OK : GP103_ERR_CUDA;
+}
+
+extern "C" int gp103_batch_add_run(void* batch, const gp103_plan* plan, const gp103_begin_args* begin,
+                                   int start_passes, int density_passes, int max_start_loops, int max_density_loops,
+                                   double density_weight, double total_pins, double gamma, float* tmp0, float* tmp1,
+                                   double* scal8, int* loops, unsigned long long* stop_ns, cudaStream_t capture) {
+    Batch* b = (Batch*)batch;
+    if (!b || !plan || !plan->T || !plan->S || !tmp0 || !scal8 || !loops || !stop_ns || start_passes < 1 ||
+        density_passes < 1 || max_start_loops < 1 || max_density_loops < 1 || b->exec || (begin && !tmp1))
+        return GP103_ERR_ARG;
+    cudaGraphNode_t set_up, start, hand, density;
+    const gp103_begin_args args = begin ? *begin : gp103_begin_args{};
+    if (begin)
+        TRY(add_once(b, nullptr, 0, capture, &set_up,
+                     [&] { return gp103_begin(plan, &args, tmp0, tmp1, scal8, capture); }));
+    TRY(add_loop(b, plan, GP103_PHASE_START, start_passes, 0, max_start_loops, loops, stop_ns, begin ? &set_up : nullptr,
+                 begin ? 1 : 0, capture, &start));
+    TRY(add_once(b, &start, 1, capture, &hand, [&] {
+        return gp103_start_to_density(plan, density_weight, total_pins, gamma, tmp0, scal8, capture);
+    }));
     TRY(add_loop(b, plan, GP103_PHASE_DENSITY, density_passes, 1, max_density_loops, loops + 1, stop_ns + 1, &hand, 1,
                  capture, &density));
     b->count++;

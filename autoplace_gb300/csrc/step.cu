@@ -212,9 +212,10 @@ int launch_step(const StepJob& j, cudaStream_t s) {
 }
 
 // probe = clamp(v - step g, lo, hi); |probe - v|^2
-__global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step, int n,
-                             float2* probe, Reduce red) {
+__global__ void probe_kernel(const float2* v, const float2* g, const float2* lo, const float2* hi, float step,
+                             const double* step_p, int n, float2* probe, Reduce red) {
     pdl_wait();
+    if (step_p) step = __double2float_rn(*step_p);
     float d2 = 0.f;                            // per-thread partial (a few nodes); float32 warp tree, float64 across warps and blocks
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float2 vi = v[i], gi = g[i], l = lo[i], h = hi[i];
@@ -229,9 +230,9 @@ __global__ void probe_kernel(const float2* v, const float2* g, const float2* lo,
 }
 
 int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
-                 Reduce red, cudaStream_t s) {
+                 Reduce red, cudaStream_t s, const double* step_p) {
     if (launch_k(probe_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, (const float2*)v, (const float2*)g, (const float2*)lo,
-                                                      (const float2*)hi, step, n, (float2*)probe, red) != cudaSuccess) return GP103_ERR_CUDA;
+                                                      (const float2*)hi, step, step_p, n, (float2*)probe, red) != cudaSuccess) return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }
@@ -358,6 +359,99 @@ int launch_finish(const double* S, const int* cur, const float* v0, const float*
                   cudaStream_t s) {
     if (n == 0) return GP103_OK;
     if (launch_k(finish_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, S, cur, nullptr, v0, v1, best, n) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+// The set-up of a level's state before its first pass (the scalars of Placer.begin): kp = (gamma, lam, lam, 0, 0)
+// and cur = 0 before the probes (the WA kernels read gamma from kp[0]).
+__global__ void begin_kernel(float* kp, int* cur, double gamma, double lam) {
+    pdl_wait();
+    kp[0] = __double2float_rn(gamma);
+    kp[1] = kp[2] = __double2float_rn(lam);
+    kp[3] = kp[4] = 0.f;
+    *cur = 0;
+}
+
+// *out = sqrt(*a) / sqrt(*b) in float64: the step length of a probe (src/nesterov_optimizer.py:56-63 and :15-32,
+// estimate_initial_learning_rate and NesterovOptimizer.__init__), correctly rounded operations.
+__global__ void sqrt_ratio_kernel(const double* a, const double* b, double* out) {
+    pdl_wait();
+    *out = __ddiv_rn(__dsqrt_rn(*a), __dsqrt_rn(*b));
+}
+
+__global__ void copy_kernel(const float* src, float* dst, int n) {
+    pdl_wait();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// The first phase's state after the probes, alpha = *alpha_p. A fresh run (lam <= 0): T of the wirelength-only start
+// (alpha, a = 1, the start rule's tolerance and pass limit, the iteration counts; the rest 0) and kp = (gamma, 0, 0,
+// alpha, 0). Resumed with the density term on (lam > 0): S of the density phase (lam, gamma, alpha, a = 1, iteration,
+// last HPWL, mu 1, best HPWL and overflow +inf, loop count; the rest 0), kp = (gamma, lam, lam, alpha, 0) (the
+// Nesterov coefficient of a = 1) and best = v.
+__global__ void first_state_kernel(double* T, double* S, float* kp, float* best, const float* v, int n,
+                                   const double* alpha_p, double gamma, double lam, double start_tol, double inner,
+                                   double iter, double loop_it, double hpwl_prev) {
+    pdl_wait();
+    const double alpha = *alpha_p;
+    const bool resumed = lam > 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!resumed) {
+            for (int i = 0; i < GP103_T_SIZE; i++) T[i] = 0.0;
+            T[GP103_T_ALPHA] = alpha;
+            T[GP103_T_A] = 1.0;
+            T[GP103_T_START_TOL] = start_tol;
+            T[GP103_T_INNER] = inner;
+            T[GP103_T_ITER] = iter;
+            T[GP103_T_LOOP_IT] = loop_it;
+        } else {
+            for (int i = 0; i < S_SIZE; i++) S[i] = 0.0;
+            S[S_LAM] = lam;
+            S[S_GAM] = gamma;
+            S[S_ALPHA] = alpha;
+            S[S_A] = 1.0;
+            S[S_ITER] = iter;
+            S[S_HPWL_PREV] = hpwl_prev;
+            S[S_MU] = 1.0;
+            S[S_BEST_HPWL] = S[S_BEST_OVF] = __longlong_as_double(0x7ff0000000000000LL);     // +inf
+            S[S_LOOP_IT] = loop_it;
+        }
+        kp[0] = __double2float_rn(gamma);
+        kp[1] = kp[2] = resumed ? __double2float_rn(lam) : 0.f;
+        kp[3] = __double2float_rn(alpha);
+        kp[4] = 0.f;
+    }
+    if (resumed)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) best[i] = v[i];
+}
+
+int launch_begin(float* kp, int* cur, double gamma, double lam, cudaStream_t s) {
+    if (launch_k(begin_kernel, dim3(1), dim3(1), 0, s, kp, cur, gamma, lam) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+int launch_sqrt_ratio(const double* a, const double* b, double* out, cudaStream_t s) {
+    if (launch_k(sqrt_ratio_kernel, dim3(1), dim3(1), 0, s, a, b, out) != cudaSuccess) return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+int launch_copy(const float* src, float* dst, int n, cudaStream_t s) {
+    if (n == 0) return GP103_OK;
+    if (launch_k(copy_kernel, dim3(grid_for(n, 256, 8)), dim3(256), 0, s, src, dst, n) != cudaSuccess)
+        return GP103_ERR_CUDA;
+    GP103_CHECK_LAUNCH();
+    return GP103_OK;
+}
+
+int launch_first_state(double* T, double* S, float* kp, float* best, const float* v, int n, const double* alpha_p,
+                       double gamma, double lam, double start_tol, double inner, double iter, double loop_it,
+                       double hpwl_prev, cudaStream_t s) {
+    if (launch_k(first_state_kernel, dim3(grid_for(n > 0 ? n : 1, 256, 8)), dim3(256), 0, s, T, S, kp, best, v, n,
+                 alpha_p, gamma, lam, start_tol, inner, iter, loop_it, hpwl_prev) != cudaSuccess)
+        return GP103_ERR_CUDA;
     GP103_CHECK_LAUNCH();
     return GP103_OK;
 }

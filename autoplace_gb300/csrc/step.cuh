@@ -35,8 +35,16 @@ int launch_control(double* S, float* kp, const double* c, const float* moved, co
 int launch_select(const double* S, float* u, float* v, float* g, const float* u_next, const float* v_next,
                   const float* g_next, float* best, int n, cudaStream_t s);
 int launch_step(const StepJob& j, cudaStream_t s);
+// step_p (device, or null): the step as a float64 written by an earlier kernel, instead of `step`
 int launch_probe(const float* v, const float* g, const float* lo, const float* hi, float step, int n, float* probe,
-                 Reduce red, cudaStream_t s);
+                 Reduce red, cudaStream_t s, const double* step_p = nullptr);
+// The scalars of a level's set-up (begin_kernel, sqrt_ratio_kernel, first_state_kernel) and a device copy.
+int launch_begin(float* kp, int* cur, double gamma, double lam, cudaStream_t s);
+int launch_sqrt_ratio(const double* a, const double* b, double* out, cudaStream_t s);
+int launch_copy(const float* src, float* dst, int n, cudaStream_t s);
+int launch_first_state(double* T, double* S, float* kp, float* best, const float* v, int n, const double* alpha_p,
+                       double gamma, double lam, double start_tol, double inner, double iter, double loop_it,
+                       double hpwl_prev, cudaStream_t s);
 // ferr: the tensor-core field's device error flag (or null): when set, the control stops the run with reason
 // STOP_DEVICE_ERROR and changes nothing else.
 constexpr int STOP_DEVICE_ERROR = 6;

@@ -461,49 +461,44 @@ class Placer(object):
         return self.end(ctx)
 
     def begin(self, pos0, resume=None):
-        """The host part before the passes: positions clamped into the region, the two probe steps of the step length
-        (estimate_initial_learning_rate and NesterovOptimizer.__init__, four gradient evaluations), and the state of the
-        first phase (T of the wirelength-only start, or S when resumed with the density term on). -> context dict."""
-        p, o = self.p, self.p.opts
+        """The part before the passes: positions clamped into the region, then the level's set-up on the device
+        (gp103_begin: the two probe steps of the step length, estimate_initial_learning_rate and
+        NesterovOptimizer.__init__, four gradient evaluations, and the state of the first phase: T of the
+        wirelength-only start, or S when resumed with the density term on), with no host synchronisation unless
+        resumed. -> context dict."""
         t0 = time.time()
         r = resume or {}
         lam0 = float(r.get("lam", 0.0))
         gam = float(r["gam"]) if resume else self.start_gamma
         first = int(r.get("first_iter", 0))
-        w, pc = (lam0, lam0) if lam0 > 0 else (0.0, -1.0)
+        self.load(pos0)
+        args = self.begin_args(gam, lam0, int(r.get("iter", 0)), first, float(r.get("hpwl", 0.0)))
+        native.call("gp103_begin", self._ref, ctypes.byref(args), self._p(self.tmp[0]), self._p(self.tmp[1]),
+                    self._p(self.scal), self.stream.cuda_stream)
+        ctx = self.context(t0, gam, lam0)
+        if lam0 > 0:
+            self.check_device("the level's set-up")           # (synchronises the stream)
+            ctx.update(it0=first, start_iters=0)
+        return ctx
+
+    def context(self, t0, gam=None, lam0=0.0):
+        """The context of a run that gp103_begin set up: its start time, WA smoothing, the four gradient evaluations of
+        the probes, and whether the wirelength-only start comes first (a fresh run by default)."""
+        return dict(t0=t0, gam=self.start_gamma if gam is None else gam, evals=4, start=lam0 <= 0)
+
+    def load(self, pos0):
+        """v[0] = pos0 ([num_nodes, 2], host or device) clamped into the region, queued on the Placer's stream."""
         with torch.cuda.stream(self.stream):
             v = self.V[0]
             v.copy_(torch.as_tensor(pos0, dtype=torch.float32).to(self.dev, non_blocking=True))
             torch.max(torch.min(v, self.hi), self.lo, out=v)
-            self.kp.copy_(torch.tensor([gam, lam0, lam0, 0, 0], dtype=torch.float32))
-            self.cur.zero_()
-        g, probe, g2 = self.G[0], self.tmp[0], self.tmp[1]
-        # estimate_initial_learning_rate (with the density term once its weight is on)
-        self.eval(v, g, weight=w, precond=pc)
-        d1 = self.probe(v, g, o.lr, probe)
-        d2 = self.eval(probe, g2, g_ref=g, weight=w, precond=pc)[0]
-        lr = math.sqrt(d1) / math.sqrt(d2)
-        # NesterovOptimizer.__init__: the gradient again (same point, same bits), then the optimiser's own probe
-        self.eval(v, g, weight=w, precond=pc)
-        with torch.cuda.stream(self.stream):
-            self.U[0].copy_(v)
-        d1 = self.probe(v, g, lr, probe)
-        d2 = self.eval(probe, g2, g_ref=g, weight=w, precond=pc)[0]
-        alpha = math.sqrt(d1) / math.sqrt(d2)
-        ctx = dict(t0=t0, gam=gam, evals=4, start=lam0 <= 0)
-        if lam0 > 0:
-            self._density_state(ctx, lam=lam0, alpha=alpha, a=1.0, it0=first, iter0=int(r["iter"]),
-                                hpwl_prev=float(r["hpwl"]), cur=0, start_iters=0)
-        else:
-            # the wirelength-only start
-            Th = np.zeros(T_SIZE)
-            Th[TI["alpha"]], Th[TI["a"]] = alpha, 1.0
-            Th[TI["start_tol"]], Th[TI["inner"]] = o.start_tol, o.inner_iter
-            Th[TI["iter"]], Th[TI["loop_it"]] = int(r.get("iter", 0)), first
-            with torch.cuda.stream(self.stream):
-                self.T.copy_(torch.as_tensor(Th))
-                self.kp.copy_(torch.tensor([gam, 0, 0, alpha, 0.0], dtype=torch.float32))
-        return ctx
+
+    def begin_args(self, gam, lam0=0.0, it=0, first=0, hpwl_prev=0.0):
+        """The scalars of gp103_begin: a fresh run by default (lam0 0, the scheduler's iteration count 0)."""
+        o = self.p.opts
+        return native.BeginArgs(lr=float(o.lr), gamma=float(gam), lam=float(lam0), start_tol=float(o.start_tol),
+                                inner_iter=float(o.inner_iter), iter=float(it), loop_it=float(first),
+                                hpwl_prev=float(hpwl_prev))
 
     def start_end(self, ctx, log=None):
         """After the wirelength-only start's passes: the density phase's state. -> None, or the result dict when the
@@ -540,20 +535,6 @@ class Placer(object):
         Objective.tension_unit), and the density phase's state S, kp and best, all set on the device from T."""
         native.call("gp103_start_to_density", self._ref, float(self.p.opts.density_weight), float(self.p.total_pins),
                     float(ctx["gam"]), self._p(self.tmp[0]), self._p(self.scal), self.stream.cuda_stream)
-
-    def _density_state(self, ctx, lam, alpha, a, it0, iter0, hpwl_prev, cur, start_iters):
-        gam = ctx["gam"]
-        S = np.zeros(len(S_FIELDS))
-        S[SK["lam"]], S[SK["gam"]], S[SK["alpha"]], S[SK["a"]] = lam, gam, alpha, a
-        S[SK["iter"]], S[SK["hpwl_prev"]], S[SK["mu"]] = iter0, hpwl_prev, 1.0
-        S[SK["best_hpwl"]] = S[SK["best_ovf"]] = math.inf
-        S[SK["loop_it"]] = it0
-        coef = (a - 1) / ((1 + math.sqrt(4 * a * a + 1)) / 2)
-        with torch.cuda.stream(self.stream):
-            self.S.copy_(torch.as_tensor(S))
-            self.kp.copy_(torch.tensor([gam, lam, lam, alpha, coef], dtype=torch.float32))
-            self.best.copy_(self.V[cur])
-        ctx.update(it0=it0, start_iters=start_iters)
 
     def _density_loop(self, ctx, log=None):
         o = self.p.opts

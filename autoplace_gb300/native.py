@@ -53,6 +53,11 @@ class Sizes(ctypes.Structure):
     _fields_ = [("field_const", ctypes.c_size_t), ("field_work", ctypes.c_size_t), ("red", ctypes.c_size_t)]
 
 
+class BeginArgs(ctypes.Structure):
+    """gp103_begin_args, field for field."""
+    _fields_ = [(n, _d) for n in ("lr", "gamma", "lam", "start_tol", "inner_iter", "iter", "loop_it", "hpwl_prev")]
+
+
 _SIGS = {
     "gp103_version": ([], _i),
     "gp103_status_string": ([_i], ctypes.c_char_p),
@@ -76,6 +81,7 @@ _SIGS = {
     "gp103_field": ([ctypes.POINTER(Plan), _vp, _vp, _vp, _vp], _i),
     "gp103_finish": ([ctypes.POINTER(Plan), _vp], _i),
     "gp103_start_to_density": ([ctypes.POINTER(Plan), _d, _d, _d, _vp, _vp, _vp], _i),
+    "gp103_begin": ([ctypes.POINTER(Plan), ctypes.POINTER(BeginArgs), _vp, _vp, _vp, _vp], _i),
     "gp103_device_error": ([ctypes.POINTER(Plan), _i, ctypes.POINTER(_i), _vp], _i),
     "gp103_hpwl": ([_vp] * 4 + [_i, _i, _vp, _vp, _vp], _i),
     "gp103_net_order_scratch": ([_i, _i, _i], ctypes.c_size_t),
@@ -101,7 +107,8 @@ _SIGS = {
     # batches of instances in one graph
     "gp103_batch_create": ([ctypes.POINTER(_vp)], _i),
     "gp103_batch_add": ([_vp, ctypes.POINTER(Plan), _i, _i, _i, _i, _vp, _vp, _vp], _i),
-    "gp103_batch_add_run": ([_vp, ctypes.POINTER(Plan), _i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp], _i),
+    "gp103_batch_add_run": ([_vp, ctypes.POINTER(Plan), ctypes.POINTER(BeginArgs), _i, _i, _i, _i, _d, _d, _d, _vp,
+                             _vp, _vp, _vp, _vp, _vp], _i),
     "gp103_batch_launch": ([_vp, _vp, _vp], _i),
     "gp103_batch_destroy": ([_vp], _i),
     # the learned start

@@ -270,6 +270,30 @@ int gp103_pass_split(const gp103_plan* plan, int phase_flags, cudaStream_t strea
 int gp103_event_create(void** event);
 int gp103_event_destroy(void* event);
 
+/* The scalars of a level's set-up (gp103_begin). */
+typedef struct {
+    double lr;                /* the first probe's step (--lr) */
+    double gamma;             /* WA smoothing */
+    double lam;               /* density weight: <= 0 a fresh run (the wirelength-only start follows), > 0 resumed */
+    double start_tol;         /* the start phase's rule: relative WA decrease per pass ... */
+    double inner_iter;        /* ... and its limit of passes (fresh runs) */
+    double iter;              /* the scheduler's iteration count */
+    double loop_it;           /* the level's first loop iteration */
+    double hpwl_prev;         /* resumed: the last HPWL */
+} gp103_begin_args;
+
+/* A level's set-up before its first pass, queued on `stream` with no host synchronisation: the two probe steps of the
+ * step length (estimate_initial_learning_rate and NesterovOptimizer.__init__, src/nesterov_optimizer.py:56-63 and :15-32; four
+ * gradient evaluations at v[0], the start positions, and two probes of v[0] along g[0]) and the first phase's state.
+ * kp = (gamma, lam, lam, 0, 0) and *cur = 0 first; the gradients with the density weight lam and preconditioner
+ * weight lam when lam > 0 (else the wirelength-only gradient); u[0] = v[0]; the step length into scal8[7] (the first
+ * probe's into scal8[6]; scal8: 8 device doubles, scratch too), tmp0 and tmp1 [num_nodes, 2] scratch. Then for a
+ * fresh run T = the wirelength-only start's state and kp = (gamma, 0, 0, alpha, 0); resumed, S = the density phase's
+ * state (lam, gamma, alpha, a = 1, iter, hpwl_prev, mu 1, best HPWL and overflow +inf, loop_it), kp = (gamma, lam,
+ * lam, alpha, 0) and best = v[0]. Float64 scalars by correctly rounded operations, the same bits as on the host. */
+int gp103_begin(const gp103_plan* plan, const gp103_begin_args* args, float* tmp0, float* tmp1, double* scal8,
+                cudaStream_t stream);
+
 /* The hand-over from the wirelength-only start to the density phase, queued on `stream` with no host
  * synchronisation (src/run_placement.py:60-64 with the state set-up of src/gpu_loop.py:38-48): the plain density
  * gradient at v[*cur] (gp103_eval's kernels with weight 1, precond -1, no wirelength term; into g_tmp
@@ -489,15 +513,17 @@ int gp103_learn_features(const int* net_start, const int* pin_cell, const float*
 int gp103_batch_create(void** batch);
 int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first, int max_loops,
                     int* loops, unsigned long long* stop_ns, cudaStream_t capture);
-/* A whole placement of one instance in the batch's graph: the start phase's WHILE node (start_passes per body,
- * at most max_start_loops bodies), then an IF node that runs gp103_start_to_density once (density_weight,
- * total_pins, gamma, g_tmp, out5 as there), then the density phase's WHILE node (density_passes per body, the first
- * refreshing the spatial order, at most max_density_loops bodies). loops[0], stop_ns[0] belong to the start loop,
- * loops[1], stop_ns[1] to the density loop. No host step between the phases. */
-int gp103_batch_add_run(void* batch, const gp103_plan* plan, int start_passes, int density_passes,
-                        int max_start_loops, int max_density_loops, double density_weight, double total_pins,
-                        double gamma, float* g_tmp, double* out5, int* loops, unsigned long long* stop_ns,
-                        cudaStream_t capture);
+/* A whole placement of one instance in the batch's graph: when `begin` is not NULL, an IF node that runs gp103_begin
+ * once (begin, tmp0, tmp1, scal8 as there; the start positions must be in v[0] when the graph is launched); then the
+ * start phase's WHILE node (start_passes per body, at most max_start_loops bodies), an IF node that runs
+ * gp103_start_to_density once (density_weight, total_pins, gamma; tmp0 as g_tmp, scal8 as out5), and the density
+ * phase's WHILE node (density_passes per body, the first refreshing the spatial order, at most max_density_loops
+ * bodies). loops[0], stop_ns[0] belong to the start loop, loops[1], stop_ns[1] to the density loop. No host step
+ * from the set-up to the stop. */
+int gp103_batch_add_run(void* batch, const gp103_plan* plan, const gp103_begin_args* begin, int start_passes,
+                        int density_passes, int max_start_loops, int max_density_loops, double density_weight,
+                        double total_pins, double gamma, float* tmp0, float* tmp1, double* scal8, int* loops,
+                        unsigned long long* stop_ns, cudaStream_t capture);
 int gp103_batch_launch(void* batch, unsigned long long* t0_ns, cudaStream_t stream);
 int gp103_batch_destroy(void* batch);
 
