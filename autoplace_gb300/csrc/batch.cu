@@ -27,6 +27,7 @@ struct Batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int count = 0;
+    bool broken = false;        // an add failed after it changed the graph: the graph holds a partial instance
 };
 
 __device__ __forceinline__ unsigned long long now_ns() {
@@ -121,7 +122,11 @@ extern "C" int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, i
     if (phase != GP103_PHASE_START && phase != GP103_PHASE_DENSITY) return GP103_ERR_ARG;
     if (phase == GP103_PHASE_START ? !plan->T : !plan->S) return GP103_ERR_ARG;
     cudaGraphNode_t node;
-    TRY(add_loop(b, plan, phase, passes, sort_first, max_loops, loops, stop_ns, nullptr, 0, capture, &node));
+    const int st = add_loop(b, plan, phase, passes, sort_first, max_loops, loops, stop_ns, nullptr, 0, capture, &node);
+    if (st) {
+        b->broken = true;
+        return st;
+    }
     b->count++;
     return GP103_OK;
 }
@@ -153,23 +158,31 @@ extern "C" int gp103_batch_add_run(void* batch, const gp103_plan* plan, const gp
         return GP103_ERR_ARG;
     cudaGraphNode_t set_up, start, hand, density;
     const gp103_begin_args args = begin ? *begin : gp103_begin_args{};
+    int st = GP103_OK;
     if (begin)
-        TRY(add_once(b, nullptr, 0, capture, &set_up,
-                     [&] { return gp103_begin(plan, &args, tmp0, tmp1, scal8, capture); }));
-    TRY(add_loop(b, plan, GP103_PHASE_START, start_passes, 0, max_start_loops, loops, stop_ns, begin ? &set_up : nullptr,
-                 begin ? 1 : 0, capture, &start));
-    TRY(add_once(b, &start, 1, capture, &hand, [&] {
-        return gp103_start_to_density(plan, density_weight, total_pins, gamma, tmp0, scal8, capture);
-    }));
-    TRY(add_loop(b, plan, GP103_PHASE_DENSITY, density_passes, 1, max_density_loops, loops + 1, stop_ns + 1, &hand, 1,
-                 capture, &density));
+        st = add_once(b, nullptr, 0, capture, &set_up,
+                      [&] { return gp103_begin(plan, &args, tmp0, tmp1, scal8, capture); });
+    if (!st)
+        st = add_loop(b, plan, GP103_PHASE_START, start_passes, 0, max_start_loops, loops, stop_ns,
+                      begin ? &set_up : nullptr, begin ? 1 : 0, capture, &start);
+    if (!st)
+        st = add_once(b, &start, 1, capture, &hand, [&] {
+            return gp103_start_to_density(plan, density_weight, total_pins, gamma, tmp0, scal8, capture);
+        });
+    if (!st)
+        st = add_loop(b, plan, GP103_PHASE_DENSITY, density_passes, 1, max_density_loops, loops + 1, stop_ns + 1,
+                      &hand, 1, capture, &density);
+    if (st) {
+        b->broken = true;
+        return st;
+    }
     b->count++;
     return GP103_OK;
 }
 
 extern "C" int gp103_batch_launch(void* batch, unsigned long long* t0_ns, cudaStream_t stream) {
     Batch* b = (Batch*)batch;
-    if (!b || b->count == 0) return GP103_ERR_ARG;
+    if (!b || b->count == 0 || b->broken) return GP103_ERR_ARG;
     if (!b->exec && cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) return GP103_ERR_CUDA;
     if (t0_ns) {
         batch_clock_kernel<<<1, 1, 0, stream>>>(t0_ns);

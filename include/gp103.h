@@ -509,7 +509,9 @@ int gp103_learn_features(const int* net_start, const int* pin_cell, const float*
  * launch) counts an instance's bodies; *stop_ns (device) receives the device time (ns) at which its loop ended.
  * gp103_batch_add captures the passes on `capture` (a stream of the plan's device, not the legacy default stream);
  * the plans and their buffers must outlive the batch. gp103_batch_launch instantiates the graph on its first call and
- * launches it on `stream`, after writing the device time to *t0_ns (when not NULL). */
+ * launches it on `stream`, after writing the device time to *t0_ns (when not NULL). An add that fails after its
+ * argument checks may leave part of an instance in the graph: gp103_batch_launch then refuses the batch
+ * (GP103_ERR_ARG), and the caller destroys it. */
 int gp103_batch_create(void** batch);
 int gp103_batch_add(void* batch, const gp103_plan* plan, int phase, int passes, int sort_first, int max_loops,
                     int* loops, unsigned long long* stop_ns, cudaStream_t capture);
